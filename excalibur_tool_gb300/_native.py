@@ -1,0 +1,139 @@
+"""ctypes view of libexcalibur_gb300.so (include/excalibur_gb300.h).
+
+The structs below mirror the header field by field. The library is loaded
+from this package directory only (it is built in-tree by build.py); a missing
+library or a missing CUDA device raises -- there is no host fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import threading
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libexcalibur_gb300.so")
+
+EXC_ABI_VERSION = 1
+EXC_MAX_FIELDS = 32
+
+# return codes
+EXC_SUCCESS, EXC_ERR_INVALID, EXC_ERR_CUDA, EXC_ERR_UNSUPPORTED, EXC_ERR_NO_DEVICE = 0, -1, -2, -3, -4
+
+# per-photon status
+PH_STEPS, PH_LEFT_BOX, PH_A_STOP, PH_MAX_ITER, PH_OUTSIDE_GRID, PH_HORIZON, PH_NONFINITE, \
+    PH_TIMED_OUT, PH_ABORTED, PH_NOT_RUN, PH_BAD_FIELD = range(11)
+STATUS_NAMES = {PH_STEPS: "steps", PH_LEFT_BOX: "left_box", PH_A_STOP: "a_stop",
+                PH_MAX_ITER: "max_iter", PH_OUTSIDE_GRID: "outside_grid", PH_HORIZON: "horizon",
+                PH_NONFINITE: "nonfinite", PH_TIMED_OUT: "timed_out", PH_ABORTED: "aborted",
+                PH_NOT_RUN: "not_run", PH_BAD_FIELD: "bad_field"}
+FAILED_STATUSES = (PH_OUTSIDE_GRID, PH_HORIZON, PH_NONFINITE, PH_TIMED_OUT, PH_ABORTED, PH_NOT_RUN, PH_BAD_FIELD)
+
+METRIC_FLRW, METRIC_SCHWARZSCHILD = 1, 2
+COSMO_STATIC, COSMO_TABLE, COSMO_TABLE_FD = 0, 1, 2
+BOUNDARY = {"periodic": 0, "clamp": 1, "error": 2}
+DTYPE_F64, DTYPE_F32 = 0, 1
+STEPPER = {"rk4": 0, "rk45": 1, "leapfrog4": 2}
+TABLEAU = {"reference": 0, "fehlberg": 1}
+PRECISION = {"fp64": 0, "fp64_fast": 1, "mixed": 2}
+STOP_BOX, STOP_A = 1, 2
+OBS_ENDPOINTS, OBS_PATH, OBS_ISW = 1, 2, 4
+OBS_COLS = ["a_obs", "a_em", "phi_obs", "phi_em", "isw_int", "path", "chord", "excess",
+            "v0x", "v0y", "v0z", "v1x", "v1y", "v1z", "min_r", "eta_obs", "eta_em"]
+OBS_N = 20
+
+
+class ExcField(C.Structure):
+    _fields_ = [("data", C.c_void_p), ("dtype", C.c_int32), ("ndim", C.c_int32),
+                ("boundary", C.c_int32), ("grad_mode", C.c_int32), ("n", C.c_int64 * 4),
+                ("origin", C.c_double * 4), ("spacing", C.c_double * 4)]
+
+
+class ExcMetric(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("analytical", C.c_int32), ("free_time", C.c_int32),
+                ("cosmology", C.c_int32), ("c", C.c_double), ("c2", C.c_double), ("c4", C.c_double),
+                ("two_over_c2", C.c_double), ("mass", C.c_double), ("radius", C.c_double),
+                ("r_s", C.c_double), ("center", C.c_double * 3), ("a_table", C.c_void_p),
+                ("a_table_n", C.c_int64), ("eta_min", C.c_double), ("eta_step", C.c_double),
+                ("H0", C.c_double), ("omega_m", C.c_double), ("omega_r", C.c_double),
+                ("omega_k", C.c_double), ("omega_lambda", C.c_double), ("n_fields", C.c_int32),
+                ("reserved", C.c_int32), ("fields", ExcField * EXC_MAX_FIELDS)]
+
+
+class ExcTraceArgs(C.Structure):
+    _fields_ = [("n_photons", C.c_int64), ("state", C.c_void_p), ("status", C.c_void_p),
+                ("n_steps", C.c_void_p), ("n_iter", C.c_void_p), ("dt_state", C.c_void_p),
+                ("field_index", C.c_void_p), ("obs", C.c_void_p), ("records", C.c_void_p),
+                ("n_records", C.c_void_p), ("record_every", C.c_int32), ("max_records", C.c_int32),
+                ("record_cols", C.c_int32), ("stepper", C.c_int32), ("tableau", C.c_int32),
+                ("precision", C.c_int32), ("renormalize_every", C.c_int32), ("stop_flags", C.c_int32),
+                ("obs_flags", C.c_int32), ("block_size", C.c_int32), ("blocks_per_sm", C.c_int32),
+                ("reserved0", C.c_int32), ("dt", C.c_double), ("dt_min", C.c_double),
+                ("dt_max", C.c_double), ("rtol", C.c_double), ("atol", C.c_double),
+                ("max_iter", C.c_int64), ("max_steps", C.c_int64), ("box_lo", C.c_double * 3),
+                ("box_hi", C.c_double * 3), ("a_stop", C.c_double), ("lens_center", C.c_double * 3),
+                ("queue", C.c_void_p), ("abort_flag", C.c_void_p), ("deadline_cycles", C.c_int64)]
+
+
+EXPORTS = {
+    "exc_abi_version": (C.c_int, []),
+    "exc_strerror": (C.c_char_p, [C.c_int]),
+    "exc_last_error": (C.c_char_p, []),
+    "exc_trace": (C.c_int, [C.POINTER(ExcMetric), C.POINTER(ExcTraceArgs), C.c_void_p]),
+    "exc_geodesic_rhs": (C.c_int, [C.POINTER(ExcMetric), C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p,
+                                   C.c_void_p, C.c_int64, C.c_void_p]),
+    "exc_interp": (C.c_int, [C.POINTER(ExcField), C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]),
+    "exc_eval_cosmology": (C.c_int, [C.POINTER(ExcMetric), C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64,
+                                     C.c_void_p]),
+    "exc_metric_tensor": (C.c_int, [C.POINTER(ExcMetric), C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                    C.c_int64, C.c_void_p]),
+    "exc_null_init": (C.c_int, [C.POINTER(ExcMetric), C.c_void_p, C.c_double, C.c_void_p, C.c_void_p,
+                                C.c_int64, C.c_void_p]),
+    "exc_null_error": (C.c_int, [C.POINTER(ExcMetric), C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                 C.c_int64, C.c_void_p]),
+}
+
+_lib = None
+_lock = threading.Lock()
+
+
+class NativeError(RuntimeError):
+    pass
+
+
+def load(path: str = LIB_PATH):
+    """Load the shared library and bind every exported entry point."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        if not os.path.exists(path):
+            raise NativeError(
+                f"{path} is missing: build it with `python -c 'import __graft_entry__ as g; g.build()'` "
+                "(there is no host fallback for the tracer)")
+        lib = C.CDLL(path)
+        for name, (res, args) in EXPORTS.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        if lib.exc_abi_version() != EXC_ABI_VERSION:
+            raise NativeError("libexcalibur_gb300.so ABI version mismatch")
+        _lib = lib
+        return lib
+
+
+def check(code: int, what: str):
+    if code != EXC_SUCCESS:
+        lib = load()
+        msg = lib.exc_last_error().decode(errors="replace")
+        raise NativeError(f"{what} failed: {lib.exc_strerror(code).decode()} ({code}): {msg}")
+
+
+def ptr(t):
+    """Device pointer of a tensor (None -> NULL)."""
+    return None if t is None else C.c_void_p(t.data_ptr())
+
+
+def stream_handle(device=None):
+    import torch
+
+    return C.c_void_p(torch.cuda.current_stream(device).cuda_stream)

@@ -1,0 +1,498 @@
+// exc_device.cuh -- device-side physics of the photon-geodesic hot path (FP64).
+//
+// Every function restates one reference routine in the reference's own
+// operation order (C and Python share left-to-right associativity for
+// + - * /), so the translation unit compiled without FMA contraction
+// (EXC_FAST == 0) reproduces the reference's IEEE double arithmetic. The unit
+// compiled with contraction (EXC_FAST == 1) also replaces divisions by launch
+// constants (c^2, c^4, grid spacings, table step, 1/a) with multiplications by
+// reciprocals: GB300's FP64 pipe is narrow and each IEEE division costs about
+// ten FP64 pipe slots.
+//
+// Reference quirks kept on purpose (parity):
+//  * gradient = central difference at the base node, piecewise constant per
+//    cell (grid/interpolator_4d_fast.py:86-89, :243-253);
+//  * Phi/c^2 fed into a term that divides by c^4 again, Gamma^i_00 = dPhi/a^2
+//    in SI (metrics/perturbed_flrw_metric_fast.py:36, :46, :57, :67);
+//  * Python's floor-mod for periodic wrap (interpolator_4d_fast.py:10-17);
+//  * exact-integer c**2 / c**4 converted to float64 at the point of use.
+#pragma once
+
+#include <cstdint>
+#include <cmath>
+#include "exc_devmetric.h"
+
+#ifndef EXC_FAST
+#error "EXC_FAST must be defined (0 = exact reference order, 1 = fast)"
+#endif
+
+#ifndef EXC_NS
+#error "EXC_NS must name the precision build's namespace"
+#endif
+
+namespace EXC_NS {
+
+using exc::DevMetric;
+
+// ---------------------------------------------------------------- helpers
+// Python float modulo: result carries the sign of the divisor
+// (CPython float_rem / numpy npy_remainder semantics).
+__device__ __forceinline__ double py_fmod(double a, double b) {
+  double m = fmod(a, b);
+  if (m != 0.0) {
+    if ((b < 0.0) != (m < 0.0)) m += b;
+  } else {
+    m = copysign(0.0, b);
+  }
+  return m;
+}
+
+// Python integer modulo (non-negative for n > 0).
+__device__ __forceinline__ int64_t py_imod(int64_t i, int64_t n) {
+  int64_t r = i % n;
+  if (r != 0 && ((r < 0) != (n < 0))) r += n;
+  return r;
+}
+
+// x**3 and x**4 rounded once. The reference evaluates them with libm pow()
+// (Python float ** int, numpy float64 ** int), which rounds the exact power
+// correctly except in rare near-halfway cases; a double-double product
+// (Dekker's exact square via FMA) gives the same rounding.
+__device__ __forceinline__ double pow3_cr(double x) {
+  double p = x * x;
+  double e = fma(x, x, -p);
+  double hi = p * x;
+  double lo = fma(p, x, -hi) + e * x;
+  return hi + lo;
+}
+__device__ __forceinline__ double pow4_cr(double x) {
+  double p = x * x;
+  double e = fma(x, x, -p);
+  double hi = p * p;
+  double lo = fma(p, p, -hi) + 2.0 * p * e;
+  return hi + lo;
+}
+
+template <class FT>
+__device__ __forceinline__ double ldf(const FT* p, int64_t i) {
+  return (double)__ldg(p + i);
+}
+
+struct InterpOut {
+  double val, gx, gy, gz, dtd;
+};
+
+// x / c on the parity path; x * (1/c) on the fast path.
+__device__ __forceinline__ double div_c(double x, double c, double inv_c) {
+#if EXC_FAST
+  (void)c;
+  return x * inv_c;
+#else
+  (void)inv_c;
+  return x / c;
+#endif
+}
+
+__device__ __forceinline__ double trilinear(double c000, double c100, double c010, double c001,
+                                            double c110, double c101, double c011, double c111,
+                                            double dx, double dy, double dz) {
+  // _interp_trilinear_from_corners, interpolator_4d_fast.py:29-43
+  return c000 * (1.0 - dx) * (1.0 - dy) * (1.0 - dz) +
+         c100 * dx * (1.0 - dy) * (1.0 - dz) +
+         c010 * (1.0 - dx) * dy * (1.0 - dz) +
+         c001 * (1.0 - dx) * (1.0 - dy) * dz +
+         c110 * dx * dy * (1.0 - dz) +
+         c101 * dx * (1.0 - dy) * dz +
+         c011 * (1.0 - dx) * dy * dz +
+         c111 * dx * dy * dz;
+}
+
+// One spatial snapshot `it` (of nt, innermost index) of a 3-D/4-D field.
+// Returns an EXC_PH_* failure code, or 0 with `o` filled (o.dtd = 0).
+template <class FT>
+__device__ __forceinline__ int interp_snapshot(const ExcField& f, const double* fi, const FT* __restrict__ d,
+                                               int64_t nt, int64_t it, double x, double y, double z,
+                                               InterpOut& o) {
+  const int64_t nx = f.n[0], ny = f.n[1], nz = f.n[2];
+  const double ox = f.origin[0], oy = f.origin[1], oz = f.origin[2];
+  const double sx = f.spacing[0], sy = f.spacing[1], sz = f.spacing[2];
+#define EXC_IDX(i, j, k) ((((int64_t)(i) * ny + (j)) * nz + (k)) * nt + it)
+  if (f.boundary == EXC_BOUNDARY_PERIODIC) {
+    // fused_interpolation_gradient_3d_periodic, interpolator_4d_fast.py:195-255
+    const double Lx = (double)nx * sx, Ly = (double)ny * sy, Lz = (double)nz * sz;
+    x = ox + py_fmod(x - ox, Lx);
+    y = oy + py_fmod(y - oy, Ly);
+    z = oz + py_fmod(z - oz, Lz);
+    const double rx = div_c(x - ox, sx, fi[0]), ry = div_c(y - oy, sy, fi[1]), rz = div_c(z - oz, sz, fi[2]);
+    if (!isfinite(rx) || !isfinite(ry) || !isfinite(rz)) return EXC_PH_NONFINITE;
+    int64_t i0 = (int64_t)floor(rx), j0 = (int64_t)floor(ry), k0 = (int64_t)floor(rz);
+    const double dx = rx - (double)i0, dy = ry - (double)j0, dz = rz - (double)k0;
+    i0 = py_imod(i0, nx); j0 = py_imod(j0, ny); k0 = py_imod(k0, nz);
+    const int64_t i1 = py_imod(i0 + 1, nx), j1 = py_imod(j0 + 1, ny), k1 = py_imod(k0 + 1, nz);
+    const int64_t im = py_imod(i0 - 1, nx), jm = py_imod(j0 - 1, ny), km = py_imod(k0 - 1, nz);
+    const double c000 = ldf(d, EXC_IDX(i0, j0, k0)), c100 = ldf(d, EXC_IDX(i1, j0, k0));
+    const double c010 = ldf(d, EXC_IDX(i0, j1, k0)), c001 = ldf(d, EXC_IDX(i0, j0, k1));
+    const double c110 = ldf(d, EXC_IDX(i1, j1, k0)), c101 = ldf(d, EXC_IDX(i1, j0, k1));
+    const double c011 = ldf(d, EXC_IDX(i0, j1, k1)), c111 = ldf(d, EXC_IDX(i1, j1, k1));
+    o.val = trilinear(c000, c100, c010, c001, c110, c101, c011, c111, dx, dy, dz);
+    o.gx = div_c(c100 - ldf(d, EXC_IDX(im, j0, k0)), 2.0 * sx, fi[4]);
+    o.gy = div_c(c010 - ldf(d, EXC_IDX(i0, jm, k0)), 2.0 * sy, fi[5]);
+    o.gz = div_c(c001 - ldf(d, EXC_IDX(i0, j0, km)), 2.0 * sz, fi[6]);
+    o.dtd = 0.0;
+    return 0;
+  }
+  if (f.boundary == EXC_BOUNDARY_CLAMP) {
+    // fused_interpolation_gradient_3d_clamp, interpolator_4d_fast.py:101-188
+    const double ex = 1e-12 * sx, ey = 1e-12 * sy, ez = 1e-12 * sz;
+    const double hx = ox + (double)(nx - 1) * sx - ex;
+    const double hy = oy + (double)(ny - 1) * sy - ey;
+    const double hz = oz + (double)(nz - 1) * sz - ez;
+    if (x < ox) x = ox; else if (x > hx) x = hx;
+    if (y < oy) y = oy; else if (y > hy) y = hy;
+    if (z < oz) z = oz; else if (z > hz) z = hz;
+    const double rx = div_c(x - ox, sx, fi[0]), ry = div_c(y - oy, sy, fi[1]), rz = div_c(z - oz, sz, fi[2]);
+    if (!isfinite(rx) || !isfinite(ry) || !isfinite(rz)) return EXC_PH_NONFINITE;
+    int64_t i0 = (int64_t)floor(rx), j0 = (int64_t)floor(ry), k0 = (int64_t)floor(rz);
+    if (i0 < 0) i0 = 0;
+    if (j0 < 0) j0 = 0;
+    if (k0 < 0) k0 = 0;
+    if (i0 > nx - 2) i0 = nx - 2;
+    if (j0 > ny - 2) j0 = ny - 2;
+    if (k0 > nz - 2) k0 = nz - 2;
+    const double dx = rx - (double)i0, dy = ry - (double)j0, dz = rz - (double)k0;
+    const double c000 = ldf(d, EXC_IDX(i0, j0, k0)), c100 = ldf(d, EXC_IDX(i0 + 1, j0, k0));
+    const double c010 = ldf(d, EXC_IDX(i0, j0 + 1, k0)), c001 = ldf(d, EXC_IDX(i0, j0, k0 + 1));
+    const double c110 = ldf(d, EXC_IDX(i0 + 1, j0 + 1, k0)), c101 = ldf(d, EXC_IDX(i0 + 1, j0, k0 + 1));
+    const double c011 = ldf(d, EXC_IDX(i0, j0 + 1, k0 + 1)), c111 = ldf(d, EXC_IDX(i0 + 1, j0 + 1, k0 + 1));
+    o.val = trilinear(c000, c100, c010, c001, c110, c101, c011, c111, dx, dy, dz);
+    // one-sided at the low edge, central otherwise (the centre index is <= n-2)
+    o.gx = (i0 <= 0) ? div_c(c100 - c000, sx, fi[0]) : div_c(c100 - ldf(d, EXC_IDX(i0 - 1, j0, k0)), 2.0 * sx, fi[4]);
+    o.gy = (j0 <= 0) ? div_c(c010 - c000, sy, fi[1]) : div_c(c010 - ldf(d, EXC_IDX(i0, j0 - 1, k0)), 2.0 * sy, fi[5]);
+    o.gz = (k0 <= 0) ? div_c(c001 - c000, sz, fi[2]) : div_c(c001 - ldf(d, EXC_IDX(i0, j0, k0 - 1)), 2.0 * sz, fi[6]);
+    o.dtd = 0.0;
+    return 0;
+  }
+  // EXC_BOUNDARY_ERROR: fused_interpolation_gradient_3d_error,
+  // interpolator_4d_fast.py:50-91 (same arithmetic as the legacy strict
+  // interpolator, grid/interpolator_fast.py:119-192)
+  const double rx = div_c(x - ox, sx, fi[0]), ry = div_c(y - oy, sy, fi[1]), rz = div_c(z - oz, sz, fi[2]);
+  if (rx < 1.0 || rx >= (double)nx - 2.0 || ry < 1.0 || ry >= (double)ny - 2.0 ||
+      rz < 1.0 || rz >= (double)nz - 2.0)
+    return EXC_PH_OUTSIDE_GRID;
+  if (!isfinite(rx) || !isfinite(ry) || !isfinite(rz)) return EXC_PH_NONFINITE;
+  const int64_t i0 = (int64_t)floor(rx), j0 = (int64_t)floor(ry), k0 = (int64_t)floor(rz);
+  const double dx = rx - (double)i0, dy = ry - (double)j0, dz = rz - (double)k0;
+  const double c000 = ldf(d, EXC_IDX(i0, j0, k0)), c100 = ldf(d, EXC_IDX(i0 + 1, j0, k0));
+  const double c010 = ldf(d, EXC_IDX(i0, j0 + 1, k0)), c001 = ldf(d, EXC_IDX(i0, j0, k0 + 1));
+  const double c110 = ldf(d, EXC_IDX(i0 + 1, j0 + 1, k0)), c101 = ldf(d, EXC_IDX(i0 + 1, j0, k0 + 1));
+  const double c011 = ldf(d, EXC_IDX(i0, j0 + 1, k0 + 1)), c111 = ldf(d, EXC_IDX(i0 + 1, j0 + 1, k0 + 1));
+  o.val = trilinear(c000, c100, c010, c001, c110, c101, c011, c111, dx, dy, dz);
+  o.gx = div_c(c100 - ldf(d, EXC_IDX(i0 - 1, j0, k0)), 2.0 * sx, fi[4]);
+  o.gy = div_c(c010 - ldf(d, EXC_IDX(i0, j0 - 1, k0)), 2.0 * sy, fi[5]);
+  o.gz = div_c(c001 - ldf(d, EXC_IDX(i0, j0, k0 - 1)), 2.0 * sz, fi[6]);
+  o.dtd = 0.0;
+  return 0;
+#undef EXC_IDX
+}
+
+// InterpolatorFast.value_gradient_and_time_derivative (interpolator_4d_fast.py:443-502),
+// including the 4-D snapshot blend (:265-402). A NaN value maps to
+// EXC_PH_OUTSIDE_GRID, like the reference's ValueError at :500-501.
+template <class FT>
+__device__ __forceinline__ int interp_field(const ExcField& f, const double* fi, double x, double y, double z,
+                                            double t, InterpOut& o) {
+  const FT* d = (const FT*)f.data;
+  if (f.ndim != 4) {
+    int st = interp_snapshot<FT>(f, fi, d, 1, 0, x, y, z, o);
+    if (st) return st;
+    if (isnan(o.val)) return EXC_PH_OUTSIDE_GRID;
+    return 0;
+  }
+  const int64_t nt = f.n[3];
+  const double ot = f.origin[3], stp = f.spacing[3];
+  double rt;
+  if (f.boundary == EXC_BOUNDARY_CLAMP) {
+    const double et = 1e-12 * stp;
+    const double ht = ot + (double)(nt - 1) * stp - et;
+    if (t < ot) t = ot; else if (t > ht) t = ht;
+    rt = div_c(t - ot, stp, fi[3]);
+  } else {
+    rt = div_c(t - ot, stp, fi[3]);
+    if (rt < 0.0 || rt >= (double)nt - 1.0) return EXC_PH_OUTSIDE_GRID;
+  }
+  if (!isfinite(rt)) return EXC_PH_NONFINITE;
+  int64_t it0 = (int64_t)floor(rt);
+  if (it0 < 0) it0 = 0;
+  if (it0 > nt - 2) it0 = nt - 2;
+  const double wt = rt - (double)it0;
+  InterpOut a, b;
+  int s0 = interp_snapshot<FT>(f, fi, d, nt, it0, x, y, z, a);
+  if (s0) return s0;
+  int s1 = interp_snapshot<FT>(f, fi, d, nt, it0 + 1, x, y, z, b);
+  if (s1) return s1;
+  if (isnan(a.val) || isnan(b.val)) return EXC_PH_OUTSIDE_GRID;
+  o.val = (1.0 - wt) * a.val + wt * b.val;
+  o.gx = (1.0 - wt) * a.gx + wt * b.gx;
+  o.gy = (1.0 - wt) * a.gy + wt * b.gy;
+  o.gz = (1.0 - wt) * a.gz + wt * b.gz;
+  o.dtd = div_c(b.val - a.val, stp, fi[3]);
+  return 0;
+}
+
+// ------------------------------------------------------------ cosmology
+// a_interp_numba, core/cosmology.py:8-25 (clamped linear interpolation).
+__device__ __forceinline__ double a_interp(const DevMetric& D, double eta, int& st) {
+  const ExcMetric& m = D.m;
+  const double* __restrict__ tab = m.a_table;
+  const int64_t n = m.a_table_n;
+  if (eta <= m.eta_min) return __ldg(tab);
+  const double max_eta = m.eta_min + m.eta_step * (double)(n - 1);
+  if (eta >= max_eta) return __ldg(tab + n - 1);
+  if (isnan(eta)) { st = EXC_PH_NONFINITE; return NAN; }
+  int64_t i = (int64_t)div_c(eta - m.eta_min, m.eta_step, D.i_eta_step);
+  // the quotient can round up to n-1 within an ulp of the table end (the
+  // reference would index past its table there); stay on the last cell
+  if (i > n - 2) i = n - 2;
+  const double t = div_c(eta - (m.eta_min + (double)i * m.eta_step), m.eta_step, D.i_eta_step);
+  return (1.0 - t) * __ldg(tab + i) + t * __ldg(tab + i + 1);
+}
+
+// LCDM_Cosmology.adot_of_eta given a = a_of_eta(eta), inv_a = 1/a (core/cosmology.py:69-93).
+__device__ __forceinline__ double adot_analytic(const ExcMetric& m, double a, double inv_a) {
+#if EXC_FAST
+  const double z = inv_a - 1.0;
+#else
+  (void)inv_a;
+  const double z = 1.0 / a - 1.0;
+#endif
+  const double zp = 1.0 + z;
+  const double E = sqrt(m.omega_m * pow3_cr(zp) + m.omega_r * pow4_cr(zp) +
+                        m.omega_k * (zp * zp) + m.omega_lambda);
+  const double H = m.H0 * E;
+  return a * a * H;
+}
+
+// PerturbedFLRWMetricFast._get_scale_factor_and_derivative
+// (perturbed_flrw_metric_fast.py:190-225), incl. its finite/zero guards.
+// inv_a = 1/a is returned for the fast path (1.0 on the parity path).
+__device__ __forceinline__ int scale_factor(const DevMetric& D, double eta, double& a, double& adot,
+                                            double& inv_a) {
+  const ExcMetric& m = D.m;
+  int st = 0;
+  inv_a = 1.0;
+  if (m.cosmology == EXC_COSMO_STATIC) {
+    a = 1.0;
+    adot = 0.0;
+    return 0;
+  }
+  a = a_interp(D, eta, st);
+  if (m.cosmology == EXC_COSMO_TABLE) {
+#if EXC_FAST
+    inv_a = 1.0 / a;
+#endif
+    adot = adot_analytic(m, a, inv_a);
+  } else {
+    const double ae = fabs(eta);
+    const double h = (1e-6 * ae > 1e-6) ? 1e-6 * ae : 1e-6;
+    const double ap = a_interp(D, eta + h, st);
+    const double am = a_interp(D, eta - h, st);
+    adot = (ap - am) / (2.0 * h);
+  }
+  if (st) return st;
+  if (!isfinite(a) || fabs(a) < 1e-30) a = 1e-30;
+  if (!isfinite(adot)) adot = 0.0;
+#if EXC_FAST
+  inv_a = 1.0 / a;
+#endif
+  return 0;
+}
+
+// ------------------------------------------------------------ FLRW RHS
+// compute_tensorial_acceleration, perturbed_flrw_metric_fast.py:7-76.
+__device__ __forceinline__ void flrw_accel_tensorial(const DevMetric& D, double u0, double u1, double u2,
+                                                     double u3, double a, double adot, double inv_a,
+                                                     double phi, double gx, double gy, double gz,
+                                                     double phi_dot, double du[4]) {
+  const double c2 = D.m.c2, c4 = D.m.c4, ic2 = D.ic2, ic4 = D.ic4;
+  const double a2 = a * a;
+#if EXC_FAST
+  const double adot_a = adot * inv_a;
+  const double ia2 = inv_a * inv_a;
+#else
+  (void)inv_a;
+  const double adot_a = adot / a;
+#endif
+  const double usq = u1 * u1 + u2 * u2 + u3 * u3;
+  const double psi = phi;
+  const double gxc = div_c(gx, c2, ic2), gyc = div_c(gy, c2, ic2), gzc = div_c(gz, c2, ic2);
+  const double pdc = div_c(phi_dot, c2, ic2);
+  const double G000 = pdc * u0 * u0;
+  const double G0ij = (div_c(a * adot, c2, ic2) + div_c(2.0 * a * adot, c4, ic4) * (phi + psi) -
+                       div_c(a2, c4, ic4) * phi_dot) * usq;
+  const double G00i = 2.0 * (gxc * u0 * u1 + gyc * u0 * u2 + gzc * u0 * u3);
+  du[0] = -(G000 + G0ij + G00i);
+  const double hub = 2.0 * (adot_a - pdc);
+#if EXC_FAST
+  const double G100 = gx * ia2 * u0 * u0;
+  const double G200 = gy * ia2 * u0 * u0;
+  const double G300 = gz * ia2 * u0 * u0;
+#else
+  const double G100 = gx / a2 * u0 * u0;
+  const double G200 = gy / a2 * u0 * u0;
+  const double G300 = gz / a2 * u0 * u0;
+#endif
+  const double G1ii = -gxc * u1 * u1 + gxc * (u2 * u2 + u3 * u3) + (-gyc) * u1 * u2 + (-gzc) * u1 * u3;
+  du[1] = -(G100 + hub * u0 * u1 + G1ii);
+  const double G2ii = -gyc * u2 * u2 + gyc * (u1 * u1 + u3 * u3) + (-gxc) * u2 * u1 + (-gzc) * u2 * u3;
+  du[2] = -(G200 + hub * u0 * u2 + G2ii);
+  const double G3ii = -gzc * u3 * u3 + gzc * (u1 * u1 + u2 * u2) + (-gxc) * u3 * u1 + (-gyc) * u3 * u2;
+  du[3] = -(G300 + hub * u0 * u3 + G3ii);
+}
+
+// compute_analytical_acceleration, perturbed_flrw_metric_fast.py:78-99.
+__device__ __forceinline__ void flrw_accel_analytical(const DevMetric& D, double u0, double u1, double u2,
+                                                      double u3, double a, double adot, double inv_a,
+                                                      double phi, double gx, double gy, double gz,
+                                                      double phi_dot, double du[4]) {
+  const double c2 = D.m.c2, c4 = D.m.c4, tc2 = D.m.two_over_c2, ic2 = D.ic2, ic4 = D.ic4;
+  const double vsq = u1 * u1 + u2 * u2 + u3 * u3;
+  const double dphidl = gx * u1 + gy * u2 + gz * u3;
+  const double psi = phi;
+#if EXC_FAST
+  const double aa = adot * inv_a;
+  const double aa2 = 2.0 * adot * inv_a;
+#else
+  (void)inv_a;
+  const double aa = adot / a;
+  const double aa2 = 2.0 * adot / a;
+#endif
+  const double pdc2 = div_c(phi_dot, c2, ic2);
+  du[0] = -(aa + pdc2) * (u0 * u0) - tc2 * u0 * dphidl -
+          (div_c(aa, c2, ic2) - div_c(aa2, c4, ic4) * (phi + psi) - div_c(phi_dot, c4, ic4)) * vsq;
+  const double hub = 2.0 * (aa - pdc2);
+  du[1] = -gx * (u0 * u0) - hub * u0 * u1 + tc2 * u1 * (gy * u2 + gz * u3) +
+          div_c(gx, c2, ic2) * (2.0 * (u1 * u1) - vsq);
+  du[2] = -gy * (u0 * u0) - hub * u0 * u2 + tc2 * u2 * (gx * u1 + gz * u3) +
+          div_c(gy, c2, ic2) * (2.0 * (u2 * u2) - vsq);
+  du[3] = -gz * (u0 * u0) - hub * u0 * u3 + tc2 * u3 * (gy * u2 + gx * u1) +
+          div_c(gz, c2, ic2) * (2.0 * (u3 * u3) - vsq);
+}
+
+// PerturbedFLRWMetricFast.geodesic_equations, perturbed_flrw_metric_fast.py:227-273.
+template <class FT>
+__device__ __forceinline__ int flrw_rhs(const DevMetric& D, int fi, const double s[8], double out[8]) {
+  double a, adot, inv_a;
+  int st = scale_factor(D, s[0], a, adot, inv_a);
+  if (st) return st;
+  InterpOut ip;
+  st = interp_field<FT>(D.m.fields[fi], D.finv[fi], s[1], s[2], s[3], s[0], ip);
+  if (st) return st;
+  const double phi_n = div_c(ip.val, D.m.c2, D.ic2);
+  const double phid_n = div_c(ip.dtd, D.m.c2, D.ic2);
+  double du[4];
+  if (D.m.analytical)
+    flrw_accel_analytical(D, s[4], s[5], s[6], s[7], a, adot, inv_a, phi_n, ip.gx, ip.gy, ip.gz, phid_n, du);
+  else
+    flrw_accel_tensorial(D, s[4], s[5], s[6], s[7], a, adot, inv_a, phi_n, ip.gx, ip.gy, ip.gz, phid_n, du);
+  out[0] = s[4]; out[1] = s[5]; out[2] = s[6]; out[3] = s[7];
+  out[4] = du[0]; out[5] = du[1]; out[6] = du[2]; out[7] = du[3];
+  return 0;
+}
+
+// ----------------------------------------------------- Schwarzschild RHS
+// SchwarzschildMetricFast.geodesic_equations (schwarzschild_metric_fast.py:253-303)
+// with _schw_accel_analytical (:104-157) / _schw_accel_tensorial (:12-101),
+// spherical (t, r, theta, phi) state.
+__device__ __forceinline__ int schw_rhs(const DevMetric& D, const double s[8], double out[8]) {
+  const ExcMetric& m = D.m;
+  double r = s[1];
+  const double th = s[2], ph = s[3];
+  if (!isfinite(r) || !isfinite(th) || !isfinite(ph)) return EXC_PH_NONFINITE;
+  if (r <= m.radius) r = m.radius;
+  if (r <= m.r_s) return EXC_PH_HORIZON;
+  const double rs = m.r_s;
+  const double u0 = s[4], u1 = s[5], u2 = s[6], u3 = s[7];
+  double sn, cs;
+  sincos(th, &sn, &cs);
+  double u0_out, du0, du1, du2, du3;
+  if (m.analytical) {
+    double dtdl_eff;
+    if (m.free_time) {
+      du0 = -(rs / (r * (r - rs))) * u0 * u1;
+      dtdl_eff = u0;
+    } else {
+      const double f = 1.0 - rs / r;
+      const double inv_f = 1.0 / f;
+      const double inv_f2 = inv_f * inv_f;
+      const double v = inv_f2 * (u1 * u1) + (r * r) * inv_f * (u2 * u2) +
+                       (r * r) * (sn * sn) * inv_f * (u3 * u3);
+      dtdl_eff = -(1.0 / m.c) * sqrt(v);
+      du0 = 0.0;
+    }
+    const double r3 = pow3_cr(r);   // Python `r**3` raises OverflowError on overflow
+    if (isinf(r3)) return EXC_PH_NONFINITE;
+    du1 = rs / (2.0 * r * (r - rs)) * u1 * u1 -
+          (r - rs) / (2.0 * r3) * (m.c2 * rs * dtdl_eff * dtdl_eff - 2.0 * r3 * (u2 * u2 + (sn * sn) * u3 * u3));
+    du2 = -2.0 / r * u1 * u2 + sn * cs * u3 * u3;
+    du3 = -2.0 / r * u1 * u3 - 2.0 * (cs / sn) * u2 * u3;
+    u0_out = dtdl_eff;
+  } else {
+    const double inv_r = 1.0 / r;
+    const double rmrs = r - rs;
+    const double inv_rmrs = 1.0 / rmrs;
+    const double u0u1 = u0 * u1, u2u2 = u2 * u2, u3u3 = u3 * u3;
+    const double G010 = 0.5 * rs * inv_r * inv_rmrs;
+    const double G100 = 0.5 * m.c2 * rs * rmrs / (r * r * r);
+    const double G111 = -G010;
+    const double G122 = -rmrs;
+    const double G133 = -rmrs * (sn * sn);
+    const double G212 = inv_r;
+    const double G233 = -sn * cs;
+    const double G313 = inv_r;
+    const double G323 = cs / sn;
+    du0 = -(2.0 * G010 * u0u1);
+    du1 = -(G100 * (u0 * u0) + G111 * (u1 * u1) + G122 * u2u2 + G133 * u3u3);
+    du2 = -(2.0 * G212 * u1 * u2 + G233 * u3u3);
+    du3 = -(2.0 * G313 * u1 * u3 + 2.0 * G323 * u2 * u3);
+    u0_out = u0;
+  }
+  if (!isfinite(du0)) return EXC_PH_NONFINITE;
+  out[0] = u0_out; out[1] = u1; out[2] = u2; out[3] = u3;
+  out[4] = du0; out[5] = du1; out[6] = du2; out[7] = du3;
+  return 0;
+}
+
+// ------------------------------------------------ metric tensor (diagonal)
+// PerturbedFLRWMetricFast.metric_tensor (perturbed_flrw_metric_fast.py:126-141) /
+// SchwarzschildMetricFast.metric_tensor (schwarzschild_metric_fast.py:190-201).
+// Both metrics are diagonal; every off-diagonal entry is 0.
+template <class FT>
+__device__ __forceinline__ int metric_diag(const DevMetric& D, int fi, const double x[4], double g[4]) {
+  const ExcMetric& m = D.m;
+  if (m.kind == EXC_METRIC_SCHWARZSCHILD) {
+    const double r = x[1];
+    const double fr = 1.0 - m.r_s / r;
+    const double sn = sin(x[2]);
+    g[0] = -fr * m.c2;
+    g[1] = 1.0 / fr;
+    g[2] = r * r;
+    g[3] = (r * r) * (sn * sn);
+    return 0;
+  }
+  double a, adot, inv_a;
+  int st = scale_factor(D, x[0], a, adot, inv_a);
+  if (st) return st;
+  InterpOut ip;
+  st = interp_field<FT>(m.fields[fi], D.finv[fi], x[1], x[2], x[3], x[0], ip);
+  if (st) return st;
+  const double phi = ip.val / m.c2;
+  const double psi = phi;
+  const double a2 = a * a;
+  g[0] = -a2 * (1.0 + 2.0 * psi) * m.c2;
+  g[1] = a2 * (1.0 - 2.0 * phi);
+  g[2] = g[1];
+  g[3] = g[1];
+  return 0;
+}
+
+}  // namespace EXC_NS

@@ -1,0 +1,15 @@
+// exc_devmetric.h -- kernel-side view of ExcMetric shared by every build.
+#pragma once
+#include "../../include/excalibur_gb300.h"
+
+namespace exc {
+
+// ExcMetric plus the reciprocals the fast path multiplies by (filled once on
+// the host per launch; the parity path never reads them).
+struct DevMetric {
+  ExcMetric m;
+  double ic2, ic4, i_eta_step;
+  double finv[EXC_MAX_FIELDS][8];   // 1/s0, 1/s1, 1/s2, 1/s3, 1/(2 s0), 1/(2 s1), 1/(2 s2), 0
+};
+
+}  // namespace exc

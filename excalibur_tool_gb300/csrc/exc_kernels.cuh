@@ -1,0 +1,540 @@
+// exc_kernels.cuh -- FP64 tracer kernels and their launchers.
+//
+// Included by exc_exact.cu (EXC_FAST=0, built without FMA contraction) and
+// exc_fast.cu (EXC_FAST=1) inside namespace EXC_NS, so one source yields the
+// parity path and the fast FP64 path.
+//
+// Execution model: one thread owns one photon; its 8-component state, RK
+// stages and running observables stay in registers for the whole trajectory.
+// The kernel is persistent (grid = SMs x blocks_per_sm) and lanes refill:
+// a lane whose photon terminates takes the next photon index from a device
+// counter (warp-aggregated atomicAdd) and keeps stepping in lock-step with
+// the lanes still on their old photons, so uneven trajectory lengths do not
+// idle the warp.
+#pragma once
+
+#include <cooperative_groups.h>
+#include "exc_device.cuh"
+
+namespace EXC_NS {
+
+namespace cg = cooperative_groups;
+
+// ------------------------------------------------------- photon context
+struct Photon {
+  double s[8];
+  double dt;
+  int64_t idx;
+  int32_t steps, it, status;
+  // observables
+  double a_obs, phi_obs, eta_obs;
+  double path, excess, min_r;
+  double p0[3], pprev[3], e0[3], v0[3];
+  double isw, pdot_prev;
+  // records
+  int32_t nrec;
+  double q[6];   // quantities attached to the next record (reference lags them by one record)
+  bool qvalid;
+  bool bad_field;
+};
+
+template <int MK>
+__device__ __forceinline__ void cart_pos(const ExcMetric& m, const double s[8], double out[3]) {
+  if (MK == EXC_METRIC_SCHWARZSCHILD) {
+    // _sph_to_xyz_rel, _postprocessing/analyze_compare_trajectories.py:86-96 (lens-centred)
+    double st, ct, sp, cp;
+    sincos(s[2], &st, &ct);
+    sincos(s[3], &sp, &cp);
+    out[0] = s[1] * st * cp;
+    out[1] = s[1] * st * sp;
+    out[2] = s[1] * ct;
+  } else {
+    out[0] = s[1]; out[1] = s[2]; out[2] = s[3];
+  }
+}
+
+template <int MK>
+__device__ __forceinline__ void cart_vel(const double s[8], double v[3]) {
+  if (MK == EXC_METRIC_SCHWARZSCHILD) {
+    // _sph_vel_to_cart, analyze_compare_trajectories.py:99-112
+    double st, ct, sp, cp;
+    sincos(s[2], &st, &ct);
+    sincos(s[3], &sp, &cp);
+    const double r = s[1], dr = s[5], dth = s[6], dph = s[7];
+    v[0] = dr * (st * cp) + (r * dth) * (ct * cp) + (r * st * dph) * (-sp);
+    v[1] = dr * (st * sp) + (r * dth) * (ct * sp) + (r * st * dph) * (cp);
+    v[2] = dr * (ct) + (r * dth) * (-st);
+  } else {
+    v[0] = s[5]; v[1] = s[6]; v[2] = s[7];
+  }
+}
+
+__device__ __forceinline__ double norm3(const double v[3]) {
+  return sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+}
+
+// |d| - d.e without cancellation (e a unit vector): |d x e|^2 / (|d| + d.e).
+__device__ __forceinline__ double excess_term(const double d[3], const double e[3]) {
+  const double nd = norm3(d);
+  const double de = d[0] * e[0] + d[1] * e[1] + d[2] * e[2];
+  if (de <= 0.0) return nd - de;
+  const double cx = d[1] * e[2] - d[2] * e[1];
+  const double cy = d[2] * e[0] - d[0] * e[2];
+  const double cz = d[0] * e[1] - d[1] * e[0];
+  const double den = nd + de;
+  return den > 0.0 ? (cx * cx + cy * cy + cz * cz) / den : 0.0;
+}
+
+template <int MK, class FT>
+struct Tracer {
+  const DevMetric& D;
+  const ExcTraceArgs& A;
+  int fi;
+
+  __device__ __forceinline__ Tracer(const DevMetric& d, const ExcTraceArgs& a) : D(d), A(a), fi(0) {}
+
+  __device__ __forceinline__ int rhs(const double s[8], double out[8]) const {
+    if (MK == EXC_METRIC_SCHWARZSCHILD) return schw_rhs(D, s, out);
+    return flrw_rhs<FT>(D, fi, s, out);
+  }
+
+  // Metric.metric_physical_quantities (perturbed_flrw_metric_fast.py:275-282;
+  // schwarzschild_metric_fast.py:305-308).
+  __device__ __forceinline__ int quantities(const double s[8], double q[6]) const {
+    if (MK == EXC_METRIC_SCHWARZSCHILD) {
+      q[0] = s[1]; q[1] = D.m.mass; q[2] = D.m.radius; q[3] = D.m.r_s; q[4] = NAN; q[5] = NAN;
+      return 0;
+    }
+    double a, adot, inv_a;
+    int st = scale_factor(D, s[0], a, adot, inv_a);
+    if (st) return st;
+    InterpOut ip;
+    st = interp_field<FT>(D.m.fields[fi], D.finv[fi], s[1], s[2], s[3], s[0], ip);
+    if (st) return st;
+    q[0] = a; q[1] = ip.val; q[2] = ip.gx; q[3] = ip.gy; q[4] = ip.gz; q[5] = ip.dtd;
+    return 0;
+  }
+
+  // ---- steppers (integrator.py:9-152) --------------------------------
+  // RK4.step, integrator.py:10-22
+  __device__ __forceinline__ int step_rk4(const double s[8], double dt, double out[8]) const {
+    double k[8], acc[8], tmp[8];
+    int st = rhs(s, k);
+    if (st) return st;
+    const double h = 0.5 * dt;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) { acc[i] = k[i]; tmp[i] = s[i] + h * k[i]; }
+    st = rhs(tmp, k);
+    if (st) return st;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) { acc[i] = acc[i] + 2.0 * k[i]; tmp[i] = s[i] + h * k[i]; }
+    st = rhs(tmp, k);
+    if (st) return st;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) { acc[i] = acc[i] + 2.0 * k[i]; tmp[i] = s[i] + dt * k[i]; }
+    st = rhs(tmp, k);
+    if (st) return st;
+    const double d6 = dt / 6.0;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) out[i] = s[i] + d6 * (acc[i] + k[i]);
+    return 0;
+  }
+
+  // Leapfrog4.step (Forest-Ruth), integrator.py:24-90. Coefficients are the
+  // float64 values of the reference's class constants.
+  __device__ __forceinline__ int step_lf4(const double s[8], double dt, double out[8]) const {
+    const double w0 = -0x1.b3d16dd72c671p+0, w1 = 0x1.59e8b6eb96339p+0;
+    const double c1 = 0x1.59e8b6eb96339p-1, c2 = -0x1.67a2dbae58ce0p-3;
+    const double cs[4] = {c1, c2, c2, c1};
+    const double ds[3] = {w1, w0, w1};
+    double y[8], k[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) y[i] = s[i];
+#pragma unroll
+    for (int stage = 0; stage < 3; ++stage) {
+      const double cd = cs[stage] * dt;
+#pragma unroll
+      for (int i = 0; i < 4; ++i) y[i] = y[i] + cd * y[4 + i];
+      int st = rhs(y, k);
+      if (st) return st;
+      const double dd = ds[stage] * dt;
+#pragma unroll
+      for (int i = 0; i < 4; ++i) y[4 + i] = y[4 + i] + dd * k[4 + i];
+    }
+    const double cd = cs[3] * dt;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) y[i] = y[i] + cd * y[4 + i];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) out[i] = y[i];
+    return 0;
+  }
+
+  // RK45Adaptive.step, integrator.py:93-152 (Fehlberg 4(5) nodes; weights of
+  // the reference, or Fehlberg's 6656/12825 when tableau == FEHLBERG).
+  __device__ __forceinline__ int step_rk45(const double s[8], double dt, double out[8], double& dt_new,
+                                           bool& accepted) const {
+    const double B1_0 = 1.0 / 4.0;
+    const double B2_0 = 3.0 / 32.0, B2_1 = 9.0 / 32.0;
+    const double B3_0 = 1932.0 / 2197.0, B3_1 = -7200.0 / 2197.0, B3_2 = 7296.0 / 2197.0;
+    const double B4_0 = 439.0 / 216.0, B4_1 = -8.0, B4_2 = 3680.0 / 513.0, B4_3 = -845.0 / 4104.0;
+    const double B5_0 = -8.0 / 27.0, B5_1 = 2.0, B5_2 = -3544.0 / 2565.0, B5_3 = 1859.0 / 4104.0,
+                 B5_4 = -11.0 / 40.0;
+    const double C5_0 = 16.0 / 135.0, C5_3 = 28561.0 / 56430.0, C5_4 = -9.0 / 50.0, C5_5 = 2.0 / 55.0;
+    const double C5_2 = (A.tableau == EXC_TABLEAU_FEHLBERG) ? 6656.0 / 12825.0 : 665.0 / 1287.0;
+    const double C4_0 = 25.0 / 216.0, C4_2 = 1408.0 / 2565.0, C4_3 = 2197.0 / 4104.0, C4_4 = -1.0 / 5.0;
+    double K0[8], K1[8], K2[8], K3[8], K4[8], K5[8], y[8];
+    int st = rhs(s, K0);
+    if (st) return st;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) y[i] = s[i] + dt * (B1_0 * K0[i]);
+    if ((st = rhs(y, K1))) return st;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) y[i] = s[i] + dt * (B2_0 * K0[i] + B2_1 * K1[i]);
+    if ((st = rhs(y, K2))) return st;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) y[i] = s[i] + dt * (B3_0 * K0[i] + B3_1 * K1[i] + B3_2 * K2[i]);
+    if ((st = rhs(y, K3))) return st;
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+      y[i] = s[i] + dt * (B4_0 * K0[i] + B4_1 * K1[i] + B4_2 * K2[i] + B4_3 * K3[i]);
+    if ((st = rhs(y, K4))) return st;
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+      y[i] = s[i] + dt * (B5_0 * K0[i] + B5_1 * K1[i] + B5_2 * K2[i] + B5_3 * K3[i] + B5_4 * K4[i]);
+    if ((st = rhs(y, K5))) return st;
+    // y5, y4 and the weighted RMS error (np.mean of 8 terms = pairwise sum / 8)
+    double q[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const double y5 = s[i] + dt * (C5_0 * K0[i] + 0.0 * K1[i] + C5_2 * K2[i] + C5_3 * K3[i] +
+                                     C5_4 * K4[i] + C5_5 * K5[i]);
+      const double y4 = s[i] + dt * (C4_0 * K0[i] + 0.0 * K1[i] + C4_2 * K2[i] + C4_3 * K3[i] +
+                                     C4_4 * K4[i] + 0.0 * K5[i]);
+      const double err = y5 - y4;
+      const double m0 = fabs(s[i]), m1 = fabs(y5);
+      const double mx = (isnan(m0) || isnan(m1)) ? NAN : fmax(m0, m1);   // np.maximum
+      const double tol = A.atol + A.rtol * mx;
+      const double r = err / tol;
+      q[i] = r * r;
+      out[i] = y5;
+    }
+    const double mean = (((q[0] + q[1]) + (q[2] + q[3])) + ((q[4] + q[5]) + (q[6] + q[7]))) / 8.0;
+    const double err_ratio = sqrt(mean);
+    if (err_ratio <= 1.0) {
+      const double g = (err_ratio > 0.0) ? 0.9 * pow(err_ratio, -0.2) : 5.0;
+      dt_new = dt * ((g < 5.0) ? g : 5.0);
+      accepted = true;
+    } else {
+      const double g = 0.9 * pow(err_ratio, -0.25);
+      dt_new = dt * ((g > 0.1) ? g : 0.1);
+      accepted = false;
+    }
+    return 0;
+  }
+
+  // Integrator._renormalize_state_to_null, integrator.py:298-335.
+  __device__ __forceinline__ int renormalize(double s[8]) const {
+    double g[4];
+    int st = metric_diag<FT>(D, fi, s, g);
+    if (st) return st;
+    const double u1 = s[5], u2 = s[6], u3 = s[7];
+    const double Acoef = g[0];
+    const double Bcoef = 2.0 * (0.0 * u1 + 0.0 * u2 + 0.0 * u3);
+    const double Ccoef = u1 * (g[1] * u1) + u2 * (g[2] * u2) + u3 * (g[3] * u3);
+    if (fabs(Acoef) < 1e-300) return 0;
+    const double disc = Bcoef * Bcoef - 4.0 * Acoef * Ccoef;
+    if (disc < 0.0) return 0;
+    const double sq = sqrt(disc);
+    const double ua = (-Bcoef + sq) / (2.0 * Acoef);
+    const double ub = (-Bcoef - sq) / (2.0 * Acoef);
+    const double cur = s[4];
+    s[4] = (fabs(ua - cur) <= fabs(ub - cur)) ? ua : ub;
+    return 0;
+  }
+};
+
+// np.clip(x, lo, hi) == minimum(maximum(x, lo), hi), NaN-propagating
+__device__ __forceinline__ double np_clip(double x, double lo, double hi) {
+  if (isnan(x) || isnan(lo) || isnan(hi)) return NAN;
+  return fmin(fmax(x, lo), hi);
+}
+
+// ------------------------------------------------------------- queue
+__device__ __forceinline__ int64_t next_photon(const ExcTraceArgs& A, int64_t& static_next, int64_t stride) {
+  if (A.queue == nullptr) {
+    const int64_t p = static_next;
+    static_next += stride;
+    return p;
+  }
+  // warp-aggregated fetch: one atomic per group of lanes arriving together
+  cg::coalesced_group g = cg::coalesced_threads();
+  unsigned long long base = 0;
+  if (g.thread_rank() == 0)
+    base = atomicAdd(reinterpret_cast<unsigned long long*>(A.queue), (unsigned long long)g.size());
+  base = g.shfl(base, 0);
+  return (int64_t)(base + g.thread_rank());
+}
+
+template <int MK, class FT, bool REC>
+__device__ __forceinline__ void write_record(const Tracer<MK, FT>& T, const ExcTraceArgs& A, Photon& P,
+                                             const double* q) {
+  if (!REC) return;
+  if (P.nrec < A.max_records) {
+    double* row = A.records + ((int64_t)P.idx * A.max_records + P.nrec) * A.record_cols;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) row[i] = P.s[i];
+    for (int i = 8; i < A.record_cols; ++i) row[i] = q ? q[i - 8] : NAN;
+  }
+  P.nrec++;
+}
+
+// Start a photon: load state, record the initial row, initialise observables.
+template <int MK, class FT, bool REC>
+__device__ __forceinline__ void photon_begin(Tracer<MK, FT>& T, const ExcTraceArgs& A, Photon& P, int64_t p) {
+  P.idx = p;
+  T.fi = A.field_index ? A.field_index[p] : 0;
+  P.bad_field = (unsigned)T.fi >= (unsigned)T.D.m.n_fields && MK == EXC_METRIC_FLRW;
+  if (P.bad_field) T.fi = 0;   // never index past the descriptor table
+  const double* src = A.state + p * 8;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) P.s[i] = src[i];
+  P.dt = A.dt_state ? A.dt_state[p] : A.dt;
+  P.steps = 0; P.it = 0; P.status = -1;
+  P.nrec = 0; P.qvalid = false;
+  write_record<MK, FT, REC>(T, A, P, nullptr);   // integrator.py:339-342 (no quantities yet)
+  if (A.obs_flags) {
+    cart_pos<MK>(T.D.m, P.s, P.p0);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) P.pprev[i] = P.p0[i];
+    cart_vel<MK>(P.s, P.v0);
+    const double nv = norm3(P.v0);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) P.e0[i] = nv > 0.0 ? P.v0[i] / nv : 0.0;
+    P.path = 0.0; P.excess = 0.0; P.isw = 0.0; P.pdot_prev = 0.0;
+    P.eta_obs = P.s[0];
+    double rel[3];
+    if (MK == EXC_METRIC_SCHWARZSCHILD) { rel[0] = P.p0[0]; rel[1] = P.p0[1]; rel[2] = P.p0[2]; }
+    else { for (int i = 0; i < 3; ++i) rel[i] = P.p0[i] - A.lens_center[i]; }
+    P.min_r = norm3(rel);
+    P.a_obs = NAN; P.phi_obs = NAN;
+    if (MK == EXC_METRIC_FLRW) {
+      double q[6];
+      if (T.quantities(P.s, q) == 0) { P.a_obs = q[0]; P.phi_obs = q[1]; P.pdot_prev = q[5]; }
+    }
+  }
+}
+
+// Per accepted step: path, stable excess, min_r, ISW.
+template <int MK, class FT>
+__device__ __forceinline__ void photon_accumulate(const Tracer<MK, FT>& T, const ExcTraceArgs& A, Photon& P,
+                                                  const double* s_old) {
+  double pc[3];
+  cart_pos<MK>(T.D.m, P.s, pc);
+  if (A.obs_flags & EXC_OBS_PATH) {
+    double d[3] = {pc[0] - P.pprev[0], pc[1] - P.pprev[1], pc[2] - P.pprev[2]};
+    P.path += norm3(d);
+    P.excess += excess_term(d, P.e0);
+  }
+  if (A.obs_flags & EXC_OBS_ENDPOINTS) {
+    double rel[3];
+    if (MK == EXC_METRIC_SCHWARZSCHILD) { rel[0] = pc[0]; rel[1] = pc[1]; rel[2] = pc[2]; }
+    else { for (int i = 0; i < 3; ++i) rel[i] = pc[i] - A.lens_center[i]; }
+    const double r = norm3(rel);
+    if (r < P.min_r) P.min_r = r;
+  }
+  if (MK == EXC_METRIC_FLRW && (A.obs_flags & EXC_OBS_ISW)) {
+    double q[6];
+    if (T.quantities(P.s, q) == 0) {
+      P.isw += 0.5 * (P.pdot_prev + q[5]) * (P.s[0] - s_old[0]);
+      P.pdot_prev = q[5];
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < 3; ++i) P.pprev[i] = pc[i];
+}
+
+template <int MK, class FT, bool REC>
+__device__ __forceinline__ void photon_finish(const Tracer<MK, FT>& T, const ExcTraceArgs& A, Photon& P) {
+  const int64_t p = P.idx;
+  const bool failed = P.status >= EXC_PH_OUTSIDE_GRID;
+  double qf[6];
+  int qst = 0;
+  // integrator.py:403 evaluates the quantities at the final state unconditionally;
+  // a failure there (e.g. outside the strict grid interior) fails the photon.
+  if (!failed) qst = T.quantities(P.s, qf);
+  if (REC) {
+    // integrator.py:403-404: quantities at the final state, then the final record
+    if (!failed && qst == 0) write_record<MK, FT, REC>(T, A, P, qf);
+    A.n_records[p] = P.nrec;
+  }
+  if (!failed && qst) P.status = qst;   // the reference raises inside state_quantities
+#pragma unroll
+  for (int i = 0; i < 8; ++i) A.state[p * 8 + i] = P.s[i];
+  A.status[p] = P.status;
+  if (A.n_steps) A.n_steps[p] = P.steps;
+  if (A.n_iter) A.n_iter[p] = P.it;
+  if (A.dt_state) A.dt_state[p] = P.dt;
+  if (A.obs && A.obs_flags) {
+    double* o = A.obs + p * EXC_OBSCOL_N;
+    for (int i = 0; i < EXC_OBSCOL_N; ++i) o[i] = NAN;
+    o[EXC_OBSCOL_ETA_OBS] = P.eta_obs;
+    o[EXC_OBSCOL_ETA_EM] = P.s[0];
+    o[EXC_OBSCOL_A_OBS] = P.a_obs;
+    o[EXC_OBSCOL_PHI_OBS] = P.phi_obs;
+    if (MK == EXC_METRIC_FLRW && !failed && qst == 0) { o[EXC_OBSCOL_A_EM] = qf[0]; o[EXC_OBSCOL_PHI_EM] = qf[1]; }
+    o[EXC_OBSCOL_ISW_INT] = P.isw;
+    if (A.obs_flags & EXC_OBS_PATH) {
+      double pc[3];
+      cart_pos<MK>(T.D.m, P.s, pc);
+      double X[3] = {pc[0] - P.p0[0], pc[1] - P.p0[1], pc[2] - P.p0[2]};
+      const double chord = norm3(X);
+      o[EXC_OBSCOL_PATH] = P.path;
+      o[EXC_OBSCOL_CHORD] = chord;
+      o[EXC_OBSCOL_EXCESS] = P.excess - excess_term(X, P.e0);
+    }
+    double v1[3];
+    cart_vel<MK>(P.s, v1);
+    o[EXC_OBSCOL_V0X] = P.v0[0]; o[EXC_OBSCOL_V0Y] = P.v0[1]; o[EXC_OBSCOL_V0Z] = P.v0[2];
+    o[EXC_OBSCOL_V1X] = v1[0]; o[EXC_OBSCOL_V1Y] = v1[1]; o[EXC_OBSCOL_V1Z] = v1[2];
+    o[EXC_OBSCOL_MIN_R] = P.min_r;
+  }
+}
+
+// One iteration of Integrator.integrate_single's loop (integrator.py:347-400)
+// plus the added box / scale-factor stops. Returns true when the photon ends.
+template <int MK, class FT, int STEPPER, bool REC>
+__device__ __forceinline__ bool photon_iterate(Tracer<MK, FT>& T, const ExcTraceArgs& A, Photon& P) {
+  if (P.bad_field) { P.status = EXC_PH_BAD_FIELD; return true; }
+  if (P.it >= A.max_iter) { P.status = EXC_PH_MAX_ITER; return true; }
+  if (P.steps >= A.max_steps) { P.status = EXC_PH_STEPS; return true; }
+  double dt = P.dt;
+  if (dt < 0.0) dt = -np_clip(-dt, A.dt_min, A.dt_max);   // integrator.py:358-364
+  else dt = np_clip(dt, A.dt_min, A.dt_max);
+  double ns[8];
+  double dt_new = dt;
+  bool accepted = true;
+  int st;
+  if (STEPPER == EXC_STEPPER_RK4) st = T.step_rk4(P.s, dt, ns);
+  else if (STEPPER == EXC_STEPPER_LEAPFROG4) st = T.step_lf4(P.s, dt, ns);
+  else st = T.step_rk45(P.s, dt, ns, dt_new, accepted);
+  if (st) { P.status = st; P.dt = dt; return true; }
+  bool stop = false;
+  if (accepted) {
+    if (A.renormalize_every && (P.steps % A.renormalize_every) == 0) {
+      st = T.renormalize(ns);
+      if (st) { P.status = st; P.dt = dt; return true; }
+    }
+    double s_old0[1] = {P.s[0]};
+#pragma unroll
+    for (int i = 0; i < 8; ++i) P.s[i] = ns[i];
+    if (REC && (A.record_every == 1 || (A.record_every > 1 && (P.steps % A.record_every) == 0))) {
+      write_record<MK, FT, REC>(T, A, P, P.qvalid ? P.q : nullptr);
+      st = T.quantities(P.s, P.q);
+      if (st) { P.status = st; P.dt = dt_new; P.steps++; P.it++; return true; }
+      P.qvalid = true;
+    }
+    if (A.obs_flags) photon_accumulate<MK, FT>(T, A, P, s_old0);
+    P.steps++;
+    if (A.stop_flags & EXC_STOP_BOX) {
+      double pc[3];
+      cart_pos<MK>(T.D.m, P.s, pc);
+      if (MK == EXC_METRIC_SCHWARZSCHILD) for (int i = 0; i < 3; ++i) pc[i] += T.D.m.center[i];
+      if (!(pc[0] >= A.box_lo[0] && pc[0] < A.box_hi[0] && pc[1] >= A.box_lo[1] && pc[1] < A.box_hi[1] &&
+            pc[2] >= A.box_lo[2] && pc[2] < A.box_hi[2])) {
+        P.status = EXC_PH_LEFT_BOX;
+        stop = true;
+      }
+    }
+    if (!stop && MK == EXC_METRIC_FLRW && (A.stop_flags & EXC_STOP_A)) {
+      double a, adot, inv_a;
+      if (scale_factor(T.D, P.s[0], a, adot, inv_a) == 0 && a <= A.a_stop) {
+        P.status = EXC_PH_A_STOP;
+        stop = true;
+      }
+    }
+  }
+  P.dt = dt_new;
+  P.it++;
+  return stop;
+}
+
+template <int MK, class FT, int STEPPER, bool REC>
+__global__ void __launch_bounds__(128) trace_kernel(const DevMetric D, const ExcTraceArgs A) {
+  Tracer<MK, FT> T(D, A);
+  Photon P;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  int64_t static_next = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long t0 = clock64();
+  int64_t p = next_photon(A, static_next, stride);
+  bool active = p < A.n_photons;
+  if (active) photon_begin<MK, FT, REC>(T, A, P, p);
+  while (active) {
+    bool done = photon_iterate<MK, FT, STEPPER, REC>(T, A, P);
+    if (!done && (P.it & 63) == 0) {
+      if (A.abort_flag && *(volatile const int32_t*)A.abort_flag) { P.status = EXC_PH_ABORTED; done = true; }
+      else if (A.deadline_cycles > 0 && clock64() - t0 > A.deadline_cycles) { P.status = EXC_PH_TIMED_OUT; done = true; }
+    }
+    if (done) {
+      photon_finish<MK, FT, REC>(T, A, P);
+      const bool stop_all = (P.status == EXC_PH_ABORTED || P.status == EXC_PH_TIMED_OUT);
+      if (stop_all) break;
+      p = next_photon(A, static_next, stride);
+      active = p < A.n_photons;
+      if (active) photon_begin<MK, FT, REC>(T, A, P, p);
+    }
+  }
+}
+
+// ------------------------------------------------------------ launchers
+struct LaunchCfg {
+  int block;          // threads per block
+  int blocks_per_sm;  // 0 = as many as fit (occupancy query)
+  int sm_count;
+};
+
+template <int MK, class FT, int STEPPER, bool REC>
+cudaError_t launch_trace_t(const DevMetric& D, const ExcTraceArgs& A, LaunchCfg lc, cudaStream_t s) {
+  auto kern = trace_kernel<MK, FT, STEPPER, REC>;
+  int per_sm = lc.blocks_per_sm;
+  if (per_sm <= 0) {
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, lc.block, 0);
+    if (e != cudaSuccess) return e;
+    if (per_sm < 1) per_sm = 1;
+  }
+  int64_t grid = (int64_t)lc.sm_count * per_sm;
+  const int64_t need = (A.n_photons + lc.block - 1) / lc.block;
+  if (grid > need) grid = need;
+  if (grid < 1) grid = 1;
+  kern<<<(int)grid, lc.block, 0, s>>>(D, A);
+  return cudaGetLastError();
+}
+
+template <int MK, class FT, int STEPPER>
+cudaError_t launch_trace_r(const DevMetric& D, const ExcTraceArgs& A, LaunchCfg lc, cudaStream_t s) {
+  if (A.records) return launch_trace_t<MK, FT, STEPPER, true>(D, A, lc, s);
+  return launch_trace_t<MK, FT, STEPPER, false>(D, A, lc, s);
+}
+
+// The dtype of field 0 selects the instantiation (all fields of a launch share it).
+template <int STEPPER>
+cudaError_t launch_trace_stepper(const DevMetric& D, const ExcTraceArgs& A, LaunchCfg lc, cudaStream_t s) {
+  if (D.m.kind == EXC_METRIC_SCHWARZSCHILD)
+    return launch_trace_r<EXC_METRIC_SCHWARZSCHILD, double, STEPPER>(D, A, lc, s);
+  if (D.m.fields[0].dtype == EXC_DTYPE_F32) return launch_trace_r<EXC_METRIC_FLRW, float, STEPPER>(D, A, lc, s);
+  return launch_trace_r<EXC_METRIC_FLRW, double, STEPPER>(D, A, lc, s);
+}
+
+// Defined in the per-stepper translation units (each compiles one stepper's kernels).
+cudaError_t trace_rk4(const DevMetric& D, const ExcTraceArgs& A, LaunchCfg lc, cudaStream_t s);
+cudaError_t trace_rk45(const DevMetric& D, const ExcTraceArgs& A, LaunchCfg lc, cudaStream_t s);
+cudaError_t trace_lf4(const DevMetric& D, const ExcTraceArgs& A, LaunchCfg lc, cudaStream_t s);
+
+inline cudaError_t launch_trace(const DevMetric& D, const ExcTraceArgs& A, LaunchCfg lc, cudaStream_t s) {
+  switch (A.stepper) {
+    case EXC_STEPPER_RK4: return trace_rk4(D, A, lc, s);
+    case EXC_STEPPER_RK45: return trace_rk45(D, A, lc, s);
+    default: return trace_lf4(D, A, lc, s);
+  }
+}
+
+}  // namespace EXC_NS

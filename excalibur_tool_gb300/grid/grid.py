@@ -1,0 +1,62 @@
+"""Potential grids (excalibur/grid/grid.py:57-112).
+
+`Grid(shape, spacing, origin)` holds named fields exactly like the reference
+(C-order [i, j, k] arrays, or [i, j, k, t] with time innermost). A field is
+uploaded to the GPU once per (device, dtype) and stays resident; the tracer
+reads it in place. POSIX shared memory (the reference's `shared=True`, used
+to feed CPU worker pools) has no role on one GPU and is accepted but ignored.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+
+class Grid:
+    def __init__(self, shape, spacing, origin=(0, 0, 0), cycle=False):
+        self.shape = np.array(shape)
+        self.spacing = np.array(spacing, dtype=float)
+        self.origin = np.array(origin, dtype=float)
+        self.fields = {}
+        self.cycle = cycle
+        self._device = {}
+
+    def add_field(self, name, data, shared=False):
+        """Register a field; `data` is a numpy array or a torch tensor of this grid's shape."""
+        if tuple(data.shape) != tuple(int(s) for s in self.shape):
+            raise ValueError("field shape does not match the grid shape")
+        self.fields[name] = data
+        for key in [k for k in self._device if k[0] == name]:
+            del self._device[key]
+
+    def get_value(self, name, i, j, k):
+        return self.fields[name][i, j, k]
+
+    def physical_position(self, indices):
+        return self.origin + indices * self.spacing
+
+    def indices_from_position(self, position):
+        relative_pos = (np.array(position) - self.origin) / self.spacing
+        indices = np.floor(relative_pos).astype(int)
+        if self.cycle:
+            indices = indices % self.shape
+        return indices
+
+    def device_field(self, name, device, dtype=None):
+        """The field as a contiguous tensor on `device` (uploaded once, then cached)."""
+        import torch
+
+        data = self.fields[name]
+        if dtype is None:
+            dtype = data.dtype if isinstance(data, torch.Tensor) else torch.from_numpy(np.asarray(data[:0])).dtype
+        key = (name, str(torch.device(device)), dtype)
+        t = self._device.get(key)
+        if t is None:
+            if isinstance(data, torch.Tensor):
+                t = data.to(device=device, dtype=dtype).contiguous()
+            else:
+                t = torch.as_tensor(np.ascontiguousarray(data)).to(device=device, dtype=dtype).contiguous()
+            self._device[key] = t
+        return t
+
+    def close_shared(self):
+        pass

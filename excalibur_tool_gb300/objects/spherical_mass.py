@@ -1,0 +1,55 @@
+"""Analytic lens potentials sampled onto grids (host-side field construction).
+
+`spherical_mass.potential` and `spherical_mass_nfw.potential` follow
+excalibur/objects/spherical_mass.py:9-49 and :125-171 (SI, m^2/s^2).
+Field construction happens once, before tracing, as in the reference runner
+(`_excalibur_runs/excalibur_run_compare_schwarzschild_vs_flrw_impact_parameter.py:462-467`).
+"""
+import numpy as np
+
+from ..core.constants import G
+
+
+class spherical_mass:
+    def __init__(self, mass, radius, center=np.array([0.5, 0.5, 0.5])):
+        self.G = G
+        self.mass = mass
+        self.radius = radius
+        self.center = center
+        self.x0, self.y0, self.z0 = self.center
+
+    def contains(self, x, y, z):
+        return (x - self.x0) ** 2 + (y - self.y0) ** 2 + (z - self.z0) ** 2 <= self.radius ** 2
+
+    def potential(self, x, y, z):
+        x, y, z = np.asarray(x), np.asarray(y), np.asarray(z)
+        if x.ndim == 1 and y.ndim == 1 and z.ndim == 1:
+            X, Y, Z = np.meshgrid(x, y, z, indexing="ij")
+        else:
+            X, Y, Z = np.broadcast_arrays(x, y, z)
+        r = np.sqrt((X - self.x0) ** 2 + (Y - self.y0) ** 2 + (Z - self.z0) ** 2)
+        r = np.where(r == 0, 1e-10, r)
+        pot = np.empty_like(r, dtype=float)
+        inside = r < self.radius
+        pot[inside] = -self.G * self.mass * (3 * self.radius ** 2 - r[inside] ** 2) / (2 * self.radius ** 3)
+        pot[~inside] = -self.G * self.mass / r[~inside]
+        return pot
+
+
+class spherical_mass_nfw:
+    def __init__(self, mass, radius, concentration, center=np.array([0.5, 0.5, 0.5])):
+        self.G = G
+        self.mass = mass
+        self.radius = radius
+        self.center = center
+        self.x0, self.y0, self.z0 = self.center
+        self.concentration = concentration
+        self.Rs = self.radius / self.concentration
+        c = concentration
+        self.rho0 = self.mass / (4 * np.pi * self.Rs ** 3 * (np.log(1 + c) - c / (1 + c)))
+
+    def potential(self, x, y, z):
+        r = np.sqrt((x - self.x0) ** 2 + (y - self.y0) ** 2 + (z - self.z0) ** 2)
+        r = np.where(r == 0, 1e-10, r)
+        xrel = r / self.Rs
+        return -4 * np.pi * self.G * self.rho0 * self.Rs ** 2 * np.log(1 + xrel) / xrel

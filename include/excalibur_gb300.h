@@ -1,0 +1,208 @@
+/*
+ * excalibur_gb300.h -- C ABI of the GB300 photon-geodesic tracer.
+ *
+ * Plain C: POD structs, raw pointers and sizes, no torch types. Every entry
+ * point takes a `void* stream` (a cudaStream_t; NULL = legacy default
+ * stream), enqueues its work on it and returns an ExcError code. Array
+ * pointers inside the structs are DEVICE pointers owned by the caller; the
+ * library never frees them. Per-photon outcomes are written to `status[]`,
+ * never raised: a photon the reference would abort with an exception gets a
+ * failure status and keeps its last accepted state.
+ *
+ * Reference interfaces replaced (lmagristella/excalibur-tool):
+ *   exc_trace            Integrator.integrate / integrate_single
+ *                        (excalibur/integration/integrator.py:218-409, :434-476)
+ *                        with RK4.step / Leapfrog4.step / RK45Adaptive.step (:9-152)
+ *   exc_geodesic_rhs     Metric.geodesic_equations
+ *                        (metrics/perturbed_flrw_metric_fast.py:227-273,
+ *                         metrics/schwarzschild_metric_fast.py:253-303)
+ *   exc_interp           InterpolatorFast.value_gradient_and_time_derivative
+ *                        (grid/interpolator_4d_fast.py:443-502; legacy strict
+ *                         grid/interpolator_fast.py:294-306)
+ *   exc_eval_cosmology   LCDM_Cosmology.a_of_eta / adot_of_eta
+ *                        (core/cosmology.py:199-206, :84-93)
+ *   exc_metric_tensor    Metric.metric_tensor (diagonal part)
+ *                        (perturbed_flrw_metric_fast.py:126-141,
+ *                         schwarzschild_metric_fast.py:190-201)
+ *   exc_null_init        Photons._solve_u0_from_null_condition
+ *                        (photon/photons.py:540-568; same formula as the
+ *                         cone generators :393-405)
+ *   exc_null_error       Photon.null_condition_relative_error
+ *                        (photon/photon.py:46-68)
+ */
+#ifndef EXCALIBUR_GB300_H
+#define EXCALIBUR_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define EXC_ABI_VERSION 1
+#define EXC_MAX_FIELDS 32
+
+/* ---- return codes of every entry point ---------------------------------- */
+typedef enum {
+  EXC_SUCCESS = 0,
+  EXC_ERR_INVALID = -1,      /* bad argument (message via exc_last_error) */
+  EXC_ERR_CUDA = -2,         /* a CUDA runtime call failed */
+  EXC_ERR_UNSUPPORTED = -3,  /* valid but not built (e.g. precision/metric combo) */
+  EXC_ERR_NO_DEVICE = -4
+} ExcError;
+
+/* ---- per-photon status written by exc_trace ----------------------------- */
+enum {
+  EXC_PH_STEPS = 0,          /* reached max_steps accepted steps ("steps" stop mode) */
+  EXC_PH_LEFT_BOX = 1,       /* position left [box_lo, box_hi) after an accepted step */
+  EXC_PH_A_STOP = 2,         /* a(eta) <= a_stop after an accepted step */
+  EXC_PH_MAX_ITER = 3,       /* iteration cap (the reference's max_iter, integrator.py:261) */
+  EXC_PH_OUTSIDE_GRID = 4,   /* interpolator error mode: point outside the strict interior */
+  EXC_PH_HORIZON = 5,        /* r <= r_s (schwarzschild_metric_fast.py:269-270) */
+  EXC_PH_NONFINITE = 6,      /* NaN/Inf state or acceleration, or overflow of r**3 */
+  EXC_PH_TIMED_OUT = 7,      /* device deadline reached */
+  EXC_PH_ABORTED = 8,        /* host abort flag seen */
+  EXC_PH_NOT_RUN = 9,        /* never dequeued (launch ended early) */
+  EXC_PH_BAD_FIELD = 10      /* field_index outside [0, n_fields) */
+};
+
+/* ---- enums -------------------------------------------------------------- */
+enum { EXC_METRIC_FLRW = 1, EXC_METRIC_SCHWARZSCHILD = 2 };
+enum { EXC_COSMO_STATIC = 0, EXC_COSMO_TABLE = 1, EXC_COSMO_TABLE_FD = 2 };
+enum { EXC_BOUNDARY_PERIODIC = 0, EXC_BOUNDARY_CLAMP = 1, EXC_BOUNDARY_ERROR = 2 };
+enum { EXC_GRAD_BASE_NODE = 0 };                 /* fast interpolators' gradient */
+enum { EXC_DTYPE_F64 = 0, EXC_DTYPE_F32 = 1 };
+enum { EXC_STEPPER_RK4 = 0, EXC_STEPPER_RK45 = 1, EXC_STEPPER_LEAPFROG4 = 2 };
+enum { EXC_TABLEAU_REFERENCE = 0, EXC_TABLEAU_FEHLBERG = 1 };
+/* EXACT: reference operation order, no FMA contraction (parity path).
+ * FAST:  same formulas, FMA contraction, reciprocal constants.
+ * MIXED: FP32 RHS + interpolation, FP64 state accumulation and step control. */
+enum { EXC_PREC_FP64_EXACT = 0, EXC_PREC_FP64_FAST = 1, EXC_PREC_MIXED = 2 };
+
+/* stop_flags bits (the "steps" stop and max_iter always apply) */
+#define EXC_STOP_BOX   1
+#define EXC_STOP_A     2
+
+/* obs_flags bits */
+#define EXC_OBS_ENDPOINTS 1   /* a, Phi at both ends; deflection; min_r */
+#define EXC_OBS_PATH      2   /* path length, chord, stable excess (time delay) */
+#define EXC_OBS_ISW       4   /* trapezoid integral of dPhi/deta along the path */
+
+/* columns of ExcTraceArgs.obs ([n_photons][EXC_OBSCOL_N], float64) */
+enum {
+  EXC_OBSCOL_A_OBS = 0, EXC_OBSCOL_A_EM = 1, EXC_OBSCOL_PHI_OBS = 2, EXC_OBSCOL_PHI_EM = 3,
+  EXC_OBSCOL_ISW_INT = 4,       /* int dPhi/deta deta (SI), trapezoid over accepted states */
+  EXC_OBSCOL_PATH = 5,          /* sum |dx| over accepted states (naive, reference definition) */
+  EXC_OBSCOL_CHORD = 6,         /* |x_N - x_0| */
+  EXC_OBSCOL_EXCESS = 7,        /* path - chord, cancellation-free form */
+  EXC_OBSCOL_V0X = 8, EXC_OBSCOL_V0Y = 9, EXC_OBSCOL_V0Z = 10,   /* first cartesian spatial velocity */
+  EXC_OBSCOL_V1X = 11, EXC_OBSCOL_V1Y = 12, EXC_OBSCOL_V1Z = 13, /* last cartesian spatial velocity */
+  EXC_OBSCOL_MIN_R = 14,        /* min |x - lens_center| over accepted states */
+  EXC_OBSCOL_ETA_OBS = 15, EXC_OBSCOL_ETA_EM = 16,
+  EXC_OBSCOL_N = 20
+};
+
+/* A potential grid. C-order [n0][n1][n2] (3-D) or [n0][n1][n2][n3] with time
+ * innermost (4-D), like the reference's field arrays (grid/grid.py:57-81,
+ * interpolator_4d_fast.py:286-298). */
+typedef struct ExcField {
+  const void* data;
+  int32_t dtype;           /* EXC_DTYPE_* */
+  int32_t ndim;            /* 3 or 4 */
+  int32_t boundary;        /* EXC_BOUNDARY_* */
+  int32_t grad_mode;       /* EXC_GRAD_* */
+  int64_t n[4];
+  double origin[4];
+  double spacing[4];
+} ExcField;
+
+/* Spacetime: metric parameters, cosmology table and potential grids. */
+typedef struct ExcMetric {
+  int32_t kind;            /* EXC_METRIC_* */
+  int32_t analytical;      /* analytical_geodesics flag */
+  int32_t free_time;       /* Schwarzschild free_time_geodesic flag */
+  int32_t cosmology;       /* EXC_COSMO_* (FLRW) */
+  double c, c2, c4;        /* float64(c), float64(c**2), float64(c**4) */
+  double two_over_c2;      /* float64 of the exact rational 2/c**2 */
+  /* Schwarzschild */
+  double mass, radius, r_s;
+  double center[3];
+  /* cosmology table (EXC_COSMO_TABLE*) */
+  const double* a_table;
+  int64_t a_table_n;
+  double eta_min, eta_step;
+  double H0, omega_m, omega_r, omega_k, omega_lambda;
+  /* potential grids (FLRW) */
+  int32_t n_fields;
+  int32_t reserved;
+  ExcField fields[EXC_MAX_FIELDS];
+} ExcMetric;
+
+typedef struct ExcTraceArgs {
+  int64_t n_photons;
+  double* state;                 /* [n][8] in/out: (x^0..x^3, u^0..u^3) */
+  int32_t* status;               /* [n] out: EXC_PH_* */
+  int32_t* n_steps;              /* [n] out: accepted steps (optional) */
+  int32_t* n_iter;               /* [n] out: iterations incl. rejected (optional) */
+  double* dt_state;              /* [n] in/out: per-photon dt (optional; NULL = use dt) */
+  const int32_t* field_index;    /* [n] grid used by each photon (optional; NULL = 0) */
+  double* obs;                   /* [n][EXC_OBSCOL_N] out (optional) */
+  double* records;               /* [n][max_records][record_cols] out (optional) */
+  int32_t* n_records;            /* [n] out (required with records) */
+  int32_t record_every;          /* reference semantics (integrator.py:271-274,387-394) */
+  int32_t max_records;
+  int32_t record_cols;           /* 14 (FLRW) or 12 (Schwarzschild) */
+  int32_t stepper;               /* EXC_STEPPER_* */
+  int32_t tableau;               /* EXC_TABLEAU_* (RK45) */
+  int32_t precision;             /* EXC_PREC_* */
+  int32_t renormalize_every;     /* 0 = off (integrator.py:376-377) */
+  int32_t stop_flags;            /* EXC_STOP_* */
+  int32_t obs_flags;             /* EXC_OBS_* bits */
+  int32_t block_size;            /* 0 = library default */
+  int32_t blocks_per_sm;         /* 0 = library default */
+  int32_t reserved0;
+  double dt, dt_min, dt_max, rtol, atol;
+  int64_t max_iter;              /* reference: 10000 */
+  int64_t max_steps;             /* "steps" stop value */
+  double box_lo[3], box_hi[3];   /* EXC_STOP_BOX: keep while lo <= x < hi */
+  double a_stop;                 /* EXC_STOP_A: stop once a <= a_stop */
+  double lens_center[3];         /* cartesian centre for min_r (FLRW) */
+  uint32_t* queue;               /* device scratch >= 2 uint32, zeroed by the call;
+                                    NULL = static per-photon assignment */
+  const int32_t* abort_flag;     /* device flag polled by the kernel (optional) */
+  int64_t deadline_cycles;       /* 0 = none; else SM clock cycles after kernel start */
+} ExcTraceArgs;
+
+/* ---- entry points ------------------------------------------------------- */
+int exc_abi_version(void);
+const char* exc_strerror(int code);
+const char* exc_last_error(void);         /* message of the last failing call (thread-local) */
+
+int exc_trace(const ExcMetric* metric, const ExcTraceArgs* args, void* stream);
+
+int exc_geodesic_rhs(const ExcMetric* metric, int32_t precision,
+                     const double* state, double* out, int32_t* status,
+                     const int32_t* field_index, int64_t n, void* stream);
+
+int exc_interp(const ExcField* field, const double* points /* [n][4]: x,y,z,t */,
+               double* out /* [n][5]: val, gx, gy, gz, dval/dt */, int32_t* status,
+               int64_t n, void* stream);
+
+int exc_eval_cosmology(const ExcMetric* metric, const double* eta, double* a,
+                       double* adot, int64_t n, void* stream);
+
+int exc_metric_tensor(const ExcMetric* metric, const double* x /* [n][4] */,
+                      double* g_diag /* [n][4] */, int32_t* status,
+                      const int32_t* field_index, int64_t n, void* stream);
+
+int exc_null_init(const ExcMetric* metric, double* state /* [n][8], u^0 written */,
+                  double sign, int32_t* status, const int32_t* field_index,
+                  int64_t n, void* stream);
+
+int exc_null_error(const ExcMetric* metric, const double* state, double* rel_err,
+                   int32_t* status, const int32_t* field_index, int64_t n, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* EXCALIBUR_GB300_H */

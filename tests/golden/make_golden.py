@@ -1,0 +1,469 @@
+"""Generate the golden vectors by running the REFERENCE implementation.
+
+Runs lmagristella/excalibur-tool's own Python code (its numba-decorated
+kernels execute as plain Python through the test-only shim in
+oracle/shim/numba) on small seeded inputs and writes the results to
+tests/golden/*.npz. Only the machine that holds the reference checkout can
+run this (default path below, or EXCALIBUR_REF=<path>); the committed .npz
+files are what the tests read.
+
+    python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import importlib.util
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+REF = os.environ.get("EXCALIBUR_REF", "/root/reference")
+sys.path[:0] = [os.path.join(REPO, "oracle", "shim"), REF, REPO]
+
+from excalibur.core.constants import c, G, one_Mpc, one_Msun, one_Gpc  # noqa: E402
+from excalibur.core.coordinates import cartesian_to_spherical, cartesian_velocity_to_spherical  # noqa: E402
+from excalibur.core.cosmology import LCDM_Cosmology, StaticCosmology  # noqa: E402
+from excalibur.grid.grid import Grid  # noqa: E402
+from excalibur.grid import interpolator_4d_fast as i4d  # noqa: E402
+from excalibur.grid import interpolator_fast as ifast  # noqa: E402
+from excalibur.integration.integrator import RK4, RK45Adaptive, Leapfrog4, Integrator  # noqa: E402
+from excalibur.metrics.perturbed_flrw_metric_fast import PerturbedFLRWMetricFast  # noqa: E402
+from excalibur.metrics.schwarzschild_metric_fast import SchwarzschildMetricFast  # noqa: E402
+from excalibur.photon.photons import Photons  # noqa: E402
+from excalibur.photon.photon import Photon  # noqa: E402
+
+from excalibur_tool_gb300.objects.fields import lens_plus_grf  # noqa: E402
+
+
+def _load_file(name, *rel):
+    """Import one reference module by path (its package __init__ pulls in matplotlib, absent here)."""
+    spec = importlib.util.spec_from_file_location(name, os.path.join(REF, *rel))
+    mod = importlib.util.module_from_spec(spec)
+    sys.modules[name] = mod
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def _load_postprocessing():
+    return _load_file("analyze_compare_trajectories", "_postprocessing", "analyze_compare_trajectories.py")
+
+
+RedshiftCalculator = _load_file("excalibur_redshift", "excalibur", "observables", "redshift.py").RedshiftCalculator
+
+
+def save(name, **arrays):
+    path = os.path.join(HERE, name)
+    np.savez_compressed(path, **arrays)
+    print(f"wrote {name}: " + ", ".join(f"{k}{np.shape(v)}" for k, v in arrays.items()))
+
+
+# ----------------------------------------------------------------- cosmology
+def gen_cosmology():
+    cz = LCDM_Cosmology(70, 0.3, 0.0, 0.7)
+    rng = np.random.default_rng(11)
+    eta_max = cz.eta_min + cz.eta_step * (cz.N_eta - 1)
+    etas = np.concatenate([rng.uniform(cz.eta_min, eta_max, 200),
+                           [cz.eta_min - 1e15, cz.eta_min, eta_max, eta_max + 1e16, cz._eta_at_a1,
+                            cz._eta_at_a1 - 5.1e13, 1e18, 1.2e18]])
+    a = np.array([cz.a_of_eta(float(e)) for e in etas])
+    adot = np.array([cz.adot_of_eta(float(e)) for e in etas])
+    save("cosmology.npz", a_grid=cz.a_grid, eta_min=cz.eta_min, eta_step=cz.eta_step, N_eta=cz.N_eta,
+         eta_at_a1=cz._eta_at_a1, H0=cz.H0, etas=etas, a=a, adot=adot)
+    return cz
+
+
+# ------------------------------------------------------------- interpolators
+def _grid_and_points(shape, spacing, origin, seed, n_pts, lo_frac=-0.3, hi_frac=1.3):
+    rng = np.random.default_rng(seed)
+    data = rng.standard_normal(shape) * 3.0e4
+    g = Grid(shape, spacing, origin)
+    g.add_field("Phi", data)
+    ext = np.array(shape[:3]) * np.array(spacing[:3])
+    pts = np.array(origin[:3]) + rng.uniform(lo_frac, hi_frac, (n_pts, 3)) * ext
+    # exact nodes, cell edges and the high corner
+    nodes = np.array(origin[:3]) + np.array([[1, 1, 1], [2, 3, 1], [shape[0] - 2, 1, 2], [0, 0, 0],
+                                             [shape[0] - 1, shape[1] - 1, shape[2] - 1]]) * np.array(spacing[:3])
+    pts = np.concatenate([pts, nodes, -nodes - 0.5 * np.array(spacing[:3])])
+    return g, data, pts
+
+
+def gen_interp():
+    out = {}
+    shape, spacing, origin = (9, 7, 8), (2.5e22, 3.0e22, 2.0e22), (1.0e22, -4.0e22, 0.0)
+    g, data, pts = _grid_and_points(shape, spacing, origin, 3, 300)
+    out.update(f3=data, f3_spacing=np.array(spacing), f3_origin=np.array(origin), pts3=pts)
+    for mode in ("periodic", "clamp", "error"):
+        ip = i4d.InterpolatorFast(g, boundary=mode)
+        vals, ok = [], []
+        for p in pts:
+            try:
+                v, gr, dt = ip.value_gradient_and_time_derivative(p, "Phi", 0.0)
+                vals.append([v, *gr, dt])
+                ok.append(1)
+            except Exception:
+                vals.append([np.nan] * 5)
+                ok.append(0)
+        out[f"out3_{mode}"] = np.array(vals)
+        out[f"ok3_{mode}"] = np.array(ok)
+    legacy = ifast.InterpolatorFast(g)
+    vals, ok = [], []
+    for p in pts:
+        try:
+            v, gr, dt = legacy.value_gradient_and_time_derivative(p, "Phi")
+            vals.append([v, *gr, dt])
+            ok.append(1)
+        except Exception:
+            vals.append([np.nan] * 5)
+            ok.append(0)
+    out["out3_legacy"] = np.array(vals)
+    out["ok3_legacy"] = np.array(ok)
+    # 4-D: three time snapshots
+    shape4, spacing4, origin4 = (8, 9, 7, 3), (2.0e22, 2.5e22, 3.0e22, 4.0e15), (0.0, 1.0e22, -2.0e22, 1.0e17)
+    rng = np.random.default_rng(5)
+    data4 = rng.standard_normal(shape4) * 3.0e4
+    g4 = Grid(shape4, spacing4, origin4)
+    g4.add_field("Phi", data4)
+    pts4 = np.concatenate([np.array(origin4[:3]) + rng.uniform(-0.2, 1.2, (200, 3)) * np.array(shape4[:3]) *
+                           np.array(spacing4[:3]),
+                           (origin4[3] + rng.uniform(-0.3, 2.3, 200) * spacing4[3])[:, None]], axis=1)
+    out.update(f4=data4, f4_spacing=np.array(spacing4), f4_origin=np.array(origin4), pts4=pts4)
+    for mode in ("periodic", "clamp", "error"):
+        ip = i4d.InterpolatorFast(g4, boundary=mode)
+        vals, ok = [], []
+        for p in pts4:
+            try:
+                v, gr, dt = ip.value_gradient_and_time_derivative(p[:3], "Phi", p[3])
+                vals.append([v, *gr, dt])
+                ok.append(1)
+            except Exception:
+                vals.append([np.nan] * 5)
+                ok.append(0)
+        out[f"out4_{mode}"] = np.array(vals)
+        out[f"ok4_{mode}"] = np.array(ok)
+    save("interp.npz", **out)
+
+
+# ----------------------------------------------------------------- RHS
+def _flrw_setup(cz, n=16, box=40 * one_Mpc, seed=7, boundary="periodic"):
+    rng = np.random.default_rng(seed)
+    data = rng.standard_normal((n, n, n)) * 1e-5 * c ** 2
+    g = Grid((n, n, n), (box / n,) * 3, (0.0, 0.0, 0.0))
+    g.add_field("Phi", data)
+    ip = i4d.InterpolatorFast(g, boundary=boundary)
+    return g, data, ip
+
+
+def gen_rhs(cz):
+    g, data, ip = _flrw_setup(cz)
+    box = 40 * one_Mpc
+    rng = np.random.default_rng(21)
+    n = 64
+    eta0 = cz._eta_at_a1
+    states = np.zeros((n, 8))
+    states[:, 0] = eta0 + rng.uniform(-3e16, 3e16, n)
+    states[:, 1:4] = rng.uniform(0.05, 0.95, (n, 3)) * box
+    d = rng.standard_normal((n, 3))
+    d /= np.linalg.norm(d, axis=1)[:, None]
+    states[:, 5:8] = d * c * rng.uniform(0.9, 1.1, (n, 1))
+    states[:, 4] = -rng.uniform(0.95, 1.05, n)
+    out = {"flrw_field": data, "flrw_box": box, "flrw_states": states}
+    static = StaticCosmology()
+    variants = {
+        "lcdm_tensorial": (cz.a_of_eta, cz.adot_of_eta, False),
+        "lcdm_analytical": (cz.a_of_eta, cz.adot_of_eta, True),
+        "lcdm_fd": (cz.a_of_eta, None, False),
+        "static_tensorial": (static.a_of_eta, static.adot_of_eta, False),
+    }
+    for name, (af, adf, analytical) in variants.items():
+        m = PerturbedFLRWMetricFast(af, g, ip, analytical_geodesics=analytical, adot_of_eta=adf)
+        out[f"flrw_{name}"] = np.array([m.geodesic_equations(s) for s in states])
+        out[f"flrw_g_{name}"] = np.array([np.diag(m.metric_tensor(s[:4])) for s in states])
+    # Schwarzschild: random spherical states away from the poles
+    M = 1e15 * one_Msun
+    rs = 2 * G * M / c ** 2
+    sst = np.zeros((n, 8))
+    sst[:, 0] = rng.uniform(0, 1e16, n)
+    sst[:, 1] = rs * np.exp(rng.uniform(np.log(1.5), np.log(1e7), n))
+    sst[:, 2] = rng.uniform(0.2, np.pi - 0.2, n)
+    sst[:, 3] = rng.uniform(-np.pi, np.pi, n)
+    sst[:, 4] = -rng.uniform(0.9, 1.2, n)
+    sst[:, 5] = c * rng.uniform(-1, 1, n)
+    sst[:, 6] = c / sst[:, 1] * rng.uniform(-1, 1, n)
+    sst[:, 7] = c / sst[:, 1] * rng.uniform(-1, 1, n)
+    out["schw_states"] = sst
+    out["schw_mass"] = M
+    for name, (an, ft) in {"analytical_free": (True, True), "analytical_null": (True, False),
+                           "tensorial": (False, True)}.items():
+        m = SchwarzschildMetricFast(M, 1.2 * rs, center=np.zeros(3), analytical_geodesics=an,
+                                    free_time_geodesic=ft, coords="spherical")
+        out[f"schw_{name}"] = np.array([m.geodesic_equations(s) for s in sst])
+        out[f"schw_g_{name}"] = np.array([np.diag(m.metric_tensor(s[:4])) for s in sst])
+    save("rhs.npz", **out)
+
+
+# ---------------------------------------------------------------- steppers
+def gen_steps(cz):
+    g, data, ip = _flrw_setup(cz, seed=8)
+    box = 40 * one_Mpc
+    rhs = np.load(os.path.join(HERE, "rhs.npz"))
+    states = rhs["flrw_states"][:24]
+    m = PerturbedFLRWMetricFast(cz.a_of_eta, g, ip, adot_of_eta=cz.adot_of_eta)
+    dt = 0.5 * one_Mpc / c
+    out = {"field": data, "box": box, "states": states, "dt": dt}
+    out["rk4"] = np.array([RK4().step(m, s, dt)[0] for s in states])
+    out["lf4"] = np.array([Leapfrog4().step(m, s, dt)[0] for s in states])
+    rk45 = RK45Adaptive()
+    res = [rk45.step(m, s, dt, 1e-9, 1e-13) for s in states]
+    out["rk45_state"] = np.array([r[0] for r in res])
+    out["rk45_dt"] = np.array([r[1] for r in res])
+    out["rk45_acc"] = np.array([r[2] for r in res])
+    res = [rk45.step(m, s, dt, 1e-3, 1e-3) for s in states]   # loose tolerances: accepted steps
+    out["rk45l_state"] = np.array([r[0] for r in res])
+    out["rk45l_dt"] = np.array([r[1] for r in res])
+    out["rk45l_acc"] = np.array([r[2] for r in res])
+    save("steps.npz", **out)
+
+
+# -------------------------------------------------- integrate_single (records)
+def gen_integrate(cz):
+    g, data, ip = _flrw_setup(cz, seed=9)
+    box = 40 * one_Mpc
+    m = PerturbedFLRWMetricFast(cz.a_of_eta, g, ip, adot_of_eta=cz.adot_of_eta)
+    dt = 0.25 * one_Mpc / c
+    eta0 = cz._eta_at_a1
+    rng = np.random.default_rng(31)
+    out = {"field": data, "box": box, "dt": dt}
+    cases = []
+    # RK4, fixed steps, record_every = 1 / 5 / 0, with and without renormalisation
+    for k, (rec, ren, nsteps) in enumerate([(1, 0, 40), (5, 0, 57), (0, 0, 40), (1, 3, 40)]):
+        d = rng.standard_normal(3)
+        d /= np.linalg.norm(d)
+        x0 = np.array([eta0, *(rng.uniform(0.3, 0.7, 3) * box)])
+        ph = Photons(m)
+        ph.photons.append(Photon(x0, np.array([0.0, *(d * c)])))
+        u0 = ph._solve_u0_from_null_condition(x0, d * c, sign=-1.0)
+        p = Photon(x0, np.array([u0, *(d * c)]))
+        integ = Integrator(m, dt=dt, integrator="rk4", dt_min=dt, dt_max=dt)
+        integ.integrate_single(p, "steps", nsteps, record_every=rec, renormalize_every=ren)
+        hist = p.history.states
+        width = max(len(h) for h in hist)
+        arr = np.full((len(hist), width), np.nan)
+        for i, h in enumerate(hist):
+            arr[i, :len(h)] = h
+        out[f"case{k}_init"] = np.concatenate([x0, [u0], d * c])
+        out[f"case{k}_final"] = np.concatenate([p.x, p.u])
+        out[f"case{k}_records"] = arr
+        cases.append((rec, ren, nsteps, "rk4"))
+    # RK45 (reference tableau) through integrate_single with the dt clip active
+    d = np.array([0.6, 0.48, 0.64])
+    x0 = np.array([eta0, 0.4 * box, 0.45 * box, 0.5 * box])
+    u0 = Photons(m)._solve_u0_from_null_condition(x0, d * c, sign=-1.0)
+    p = Photon(x0, np.array([u0, *(d * c)]))
+    integ = Integrator(m, dt=dt, integrator="rk45", rtol=1e-6, atol=1e-3, dt_min=dt / 50, dt_max=dt)
+    integ.integrate_single(p, "steps", 30, record_every=1)
+    hist = p.history.states
+    arr = np.full((len(hist), 14), np.nan)
+    for i, h in enumerate(hist):
+        arr[i, :len(h)] = h
+    out["case4_init"] = np.concatenate([x0, [u0], d * c])
+    out["case4_final"] = np.concatenate([p.x, p.u])
+    out["case4_records"] = arr
+    out["case4_tol"] = np.array([1e-6, 1e-3, dt / 50, dt])
+    cases.append((1, 0, 30, "rk45"))
+    out["cases"] = np.array([[r, e, s, 0 if n == "rk4" else 1] for r, e, s, n in cases])
+    save("integrate.npz", **out)
+
+
+# ------------------------------------------------------------- cfg1 subset
+def cfg1_initial_states():
+    """1024 photons: Schwarzschild lens (1e15 Msun at the box centre), observer at (0,500,500) Mpc,
+    32x32 polar grid theta_i = (i+1/2) 5deg/32, phi_j = 2 pi j/32, rotated onto the lens direction with
+    the reference's Rodrigues formula, spherical velocities via cartesian_velocity_to_spherical and
+    u^0 from _solve_u0_from_null_condition (sign -1)."""
+    M = 1e15 * one_Msun
+    rs = 2 * G * M / c ** 2
+    lens = np.array([500.0, 500.0, 500.0]) * one_Mpc
+    obs = np.array([0.0, 500.0, 500.0]) * one_Mpc
+    m = SchwarzschildMetricFast(M, rs * (1 + 1e-6), center=lens, coords="spherical",
+                                analytical_geodesics=True, free_time_geodesic=True)
+    ph = Photons(m)
+    origin = np.array([0.0, *cartesian_to_spherical(*(obs - lens))])
+    central = (lens - obs) / np.linalg.norm(lens - obs)
+    r0, t0, p0 = origin[1:]
+    x0 = r0 * np.sin(t0) * np.cos(p0)
+    y0 = r0 * np.sin(t0) * np.sin(p0)
+    z0 = r0 * np.cos(t0)
+    states = np.zeros((1024, 8))
+    for i in range(32):
+        th = (i + 0.5) * np.deg2rad(5.0) / 32
+        for j in range(32):
+            phi = 2 * np.pi * j / 32
+            d = np.array([np.sin(th) * np.cos(phi), np.sin(th) * np.sin(phi), np.cos(th)])
+            d3 = ph._rotate_to_direction(d, central)
+            d3 = d3 / np.linalg.norm(d3)
+            us = np.array(cartesian_velocity_to_spherical(x0, y0, z0, *(d3 * c)))
+            u0 = ph._solve_u0_from_null_condition(origin, us, sign=-1.0)
+            states[i * 32 + j] = np.concatenate([origin, [u0], us])
+    return m, states
+
+
+def gen_cfg1():
+    m, states = cfg1_initial_states()
+    dl = 0.5 * one_Mpc / c
+    rng = np.random.default_rng(101)
+    sel = np.unique(np.concatenate([[0, 1, 8, 15, 16, 17, 31, 511, 520, 1023],
+                                    rng.choice(1024, 30, replace=False)]))
+    rk = RK4()
+    finals, status, nsteps = [], [], []
+    for idx in sel:
+        s = states[idx].copy()
+        st, k = 0, 0
+        try:
+            for k in range(2000):
+                s, _, _ = rk.step(m, s, dl)
+            k = 2000
+        except Exception:
+            st = 1
+        finals.append(s)
+        status.append(st)
+        nsteps.append(k)
+    save("cfg1.npz", states=states, sel=sel, final=np.array(finals), failed=np.array(status),
+         n_steps=np.array(nsteps), dl=dl, mass=m.mass, radius=m.radius)
+
+
+# ------------------------------------------------------------- cfg2 (small)
+def gen_cfg2_small(cz):
+    """cfg2 construction on a 32^3 grid: Plummer (1e15 Msun, eps 5 Mpc) + GRF (seed 2, rms 1e-5),
+    periodic interpolation, LCDM, observer (0,500,500) Mpc at eta = _eta_at_a1, 6x6 directions in a
+    10x10 degree tangent patch, RK4 dl = 0.5 Mpc/c, stop at box exit (after each accepted step)."""
+    n, box = 32, 1000 * one_Mpc
+    lens = np.array([500.0, 500.0, 500.0]) * one_Mpc
+    phi = lens_plus_grf(n, box, 1e15 * one_Msun, 5 * one_Mpc, lens, seed=2)
+    g = Grid((n, n, n), (box / n,) * 3, (0.0, 0.0, 0.0))
+    g.add_field("Phi", phi)
+    ip = i4d.InterpolatorFast(g, boundary="periodic")
+    m = PerturbedFLRWMetricFast(cz.a_of_eta, g, ip, adot_of_eta=cz.adot_of_eta)
+    eta0 = cz._eta_at_a1
+    obs = np.array([0.0, 500.0, 500.0]) * one_Mpc
+    half = np.tan(np.deg2rad(5.0))
+    k = 6
+    t = (np.arange(k) + 0.5) / k * 2 - 1
+    states = []
+    ph = Photons(m)
+    for a in t:
+        for b in t:
+            d = np.array([1.0, a * half, b * half])
+            d /= np.linalg.norm(d)
+            x0 = np.array([eta0, *obs])
+            u0 = ph._solve_u0_from_null_condition(x0, d * c, sign=-1.0)
+            states.append(np.concatenate([x0, [u0], d * c]))
+    states = np.array(states)
+    dl = 0.5 * one_Mpc / c
+    rk = RK4()
+    finals, nsteps = [], []
+    for s0 in states:
+        s = s0.copy()
+        steps = 0
+        while steps < 10000:
+            s, _, _ = rk.step(m, s, dl)
+            steps += 1
+            if not np.all((s[1:4] >= 0.0) & (s[1:4] < box)):
+                break
+        finals.append(s)
+        nsteps.append(steps)
+    save("cfg2_small.npz", field=phi, box=box, states=states, final=np.array(finals), n_steps=np.array(nsteps),
+         dl=dl)
+
+
+# ------------------------------------------------------ photon generators
+def gen_generators(cz):
+    g, data, ip = _flrw_setup(cz, seed=12)
+    box = 40 * one_Mpc
+    m = PerturbedFLRWMetricFast(cz.a_of_eta, g, ip, adot_of_eta=cz.adot_of_eta)
+    eta0 = cz._eta_at_a1
+    origin = np.array([eta0, 0.2 * box, 0.3 * box, 0.4 * box])
+    ph = Photons(m)
+    import contextlib
+    import io
+    with contextlib.redirect_stdout(io.StringIO()):
+        ph.generate_cone_grid(n_photons=49, origin=origin, central_direction=[1.0, 0.5, -0.3],
+                              cone_angle=np.deg2rad(7), direction_basis="cartesian")
+    flrw_cone = np.array([np.concatenate([p.x, p.u]) for p in ph.photons])
+    flrw_null = np.array([p.null_condition_relative_error(m) for p in ph.photons])
+    ph2 = Photons(m)
+    ph2.generate_impact_parameter_bins(origin, [1.0, 0.2, 0.1], np.linspace(0.1, 2.0, 4) * one_Mpc, 5, seed=3)
+    flrw_bins = np.array([np.concatenate([p.x, p.u]) for p in ph2.photons])
+    M = 1e15 * one_Msun
+    rs = 2 * G * M / c ** 2
+    center = np.array([0.5, 0.5, 0.5]) * one_Gpc
+    ms = SchwarzschildMetricFast(M, 3 * one_Mpc, center=center, coords="spherical", analytical_geodesics=True)
+    obs = np.array([0.01, 0.01, 0.01]) * one_Gpc
+    o_sph = np.array([0.0, *cartesian_to_spherical(*(obs - center))])
+    ph3 = Photons(ms)
+    ph3.generate_cone_grid(n_photons=36, origin=o_sph, central_direction=center - obs, cone_angle=np.deg2rad(2),
+                           direction_basis="cartesian")
+    schw_cone = np.array([np.concatenate([p.x, p.u]) for p in ph3.photons])
+    schw_null = np.array([p.null_condition_relative_error(ms) for p in ph3.photons])
+    ph4 = Photons(ms)
+    ph4.generate_impact_parameter_bins(o_sph, center - obs, np.linspace(0.5, 10, 3) * one_Mpc, 4, seed=0)
+    schw_bins = np.array([np.concatenate([p.x, p.u]) for p in ph4.photons])
+    vecs = np.random.default_rng(4).standard_normal((20, 3))
+    targets = np.random.default_rng(5).standard_normal((20, 3))
+    targets[0] = [0, 0, 1]
+    targets[1] = [0, 0, -2]
+    rot = np.array([ph._rotate_to_direction(v, t) for v, t in zip(vecs, targets)])
+    save("generators.npz", field=data, box=box, flrw_origin=origin, flrw_cone=flrw_cone, flrw_null=flrw_null,
+         flrw_bins=flrw_bins, schw_origin=o_sph, schw_center=center, schw_cone=schw_cone, schw_null=schw_null,
+         schw_bins=schw_bins, rot_vecs=vecs, rot_targets=targets, rot_out=rot)
+
+
+# ------------------------------------------------------------ observables
+def gen_observables(cz):
+    pp = _load_postprocessing()
+    rng = np.random.default_rng(77)
+    # a smooth FLRW-like trajectory with 14 columns
+    n = 60
+    eta = cz._eta_at_a1 - np.linspace(0, 3e16, n)
+    xyz = np.cumsum(rng.normal(1.5e22, 1e19, (n, 3)), axis=0)
+    u = np.column_stack([-np.ones(n), np.tile([c * 0.6, c * 0.64, c * 0.48], (n, 1))])
+    a = np.array([cz.a_of_eta(e) for e in eta])
+    phi = rng.normal(0, 1e11, n)
+    grad = rng.normal(0, 1e-3, (n, 3))
+    phid = rng.normal(0, 1e-7, n)
+    traj = np.column_stack([eta, xyz, u, a, phi, grad, phid])
+    rc = RedshiftCalculator(traj).compute_all_components()
+    red = np.array([rc["z_H"], rc["z_SW"], rc["z_ISW"], rc["z_D"], rc["z_total"], rc["z_total_exact"]])
+    cart = pp._trajectory_stats(traj, None, is_spherical=False)
+    lens = np.array([5.0, 6.0, 7.0]) * 1e24
+    sph = np.column_stack([np.linspace(0, 1e16, n), np.linspace(1e25, 2e25, n),
+                           np.linspace(1.2, 1.3, n), np.linspace(-0.5, 0.7, n),
+                           -np.ones(n), rng.normal(c, 1e3, n), rng.normal(0, 1e-17, n), rng.normal(0, 1e-17, n)])
+    sphs = pp._trajectory_stats(sph, lens, is_spherical=True)
+    stats = lambda s: np.array([s.n_records, s.finite_fraction, s.path_length, s.min_r, s.final_r,
+                                s.bending_angle_rad, s.speed_mean, s.speed_max])
+    # compute_time_delay_map.compute_travel_time_deflected (restated: that module imports h5py/matplotlib)
+    pos = traj[:, 1:4]
+    path = 0.0
+    for i in range(len(pos) - 1):
+        path += np.linalg.norm(pos[i + 1] - pos[i])
+    delay = path / c - np.linalg.norm(pos[-1] - pos[0]) / c
+    theory = pp._deflection_theory_per_photon(np.array([1e22, 2e23, -1.0, np.nan]), 1e15 * one_Msun)
+    save("observables.npz", traj=traj, redshift=red, stats_cart=stats(cart), traj_sph=sph, lens=lens,
+         stats_sph=stats(sphs), path=path, delay=delay, theory=theory)
+
+
+if __name__ == "__main__":
+    if not os.path.isdir(REF):
+        sys.exit(f"reference checkout not found at {REF}")
+    np.seterr(all="ignore")
+    cz = gen_cosmology()
+    gen_interp()
+    gen_rhs(cz)
+    gen_steps(cz)
+    gen_integrate(cz)
+    gen_generators(cz)
+    gen_observables(cz)
+    gen_cfg2_small(cz)
+    gen_cfg1()
