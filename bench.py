@@ -1,0 +1,459 @@
+"""Benchmark: photon-steps/s of the backward ray tracer on the FLRW lensing workload.
+
+Workload (one "step" = one pass of the hot path over one batch): 65,536
+photons on a 256x256 grid of directions in a 10x10 deg patch, traced
+backward with RK4 (deta = 0.5 Mpc) through a perturbed-FLRW (LCDM) metric
+whose Phi lives on a 128^3 float64 grid over 1000 Mpc (Plummer lens + seeded
+P(k)~k^-3 random field, rms Phi/c^2 = 1e-5) until box exit or a <= 0.5.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+`--impl reference` times the CPU oracle (the C restatement of the reference's
+integrate_single loop, oracle/exc_oracle.c) on all host threads over the same
+workload instead. Under torchrun (N > 1) each rank traces its own batch (weak
+scaling, no collective on the data path); rank 0 prints one JSON line.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "rays/s & photon-steps/s on 1 GB300: plain FP64 vs mixed/surrogate at |Δz|≤1e-9"
+UNIT = "photon-steps/s"
+WORKLOAD = ("flrw_patch: 65,536 photons (256x256 directions, 10x10 deg patch) through perturbed FLRW "
+            "(LCDM Om=0.3 h=0.7), Phi on a 128^3 float64 grid over 1000 Mpc (Plummer 1e15 Msun eps 5 Mpc + "
+            "seeded k^-3 random field, rms 1e-5), RK4 deta = 0.5 Mpc, until box exit or a <= 0.5")
+L2_FLUSH_BYTES = 256 << 20
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    p.add_argument("--precision", default="fp64", choices=["fp64", "fp64_fast", "mixed"])
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-variants", action="store_true")
+    p.add_argument("--side", type=int, default=256, help="directions per side (smaller cases for profiling)")
+    return p.parse_args()
+
+
+# ------------------------------------------------------------------ dist
+def dist_setup(n):
+    rank = int(os.environ.get("RANK", 0))
+    world = int(os.environ.get("WORLD_SIZE", 1))
+    local = int(os.environ.get("LOCAL_RANK", 0))
+    if world > 1:
+        import torch.distributed as dist
+
+        backend = "nccl" if os.environ.get("BENCH_BACKEND", "nccl") == "nccl" else "gloo"
+        dist.init_process_group(backend)
+    return rank, world, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def max_over_ranks(x, world, device=None):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def sum_over_ranks(x, world, device=None):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+# ------------------------------------------------------------------ clocks
+class ClockSampler:
+    """nvidia-smi clock / throttle-reason samples during the timed region."""
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.idx = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        rows = []
+        with open(self.path) as fh:
+            for line in fh:
+                parts = [s.strip() for s in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        smax = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        power = [float(r[3]) for r in rows if r[3].replace(".", "").isdigit()]
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": reasons, "samples": len(rows), "power_w_max": max(power) if power else None}
+
+
+# ------------------------------------------------------------------ peaks
+def measured_peaks(device):
+    """HBM / bf16 from MEASURED_PEAKS.json (driver-written) plus FP64 / FP32 measured here with cuBLAS."""
+    import torch
+
+    peaks = {}
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as fh:
+            peaks.update(json.load(fh))
+    res = {}
+    old = torch.backends.cuda.matmul.allow_tf32
+    torch.backends.cuda.matmul.allow_tf32 = False
+    for name, dt, n in (("fp64_tflops", torch.float64, 4096), ("fp32_tflops", torch.float32, 8192)):
+        a = torch.randn(n, n, device=device, dtype=dt)
+        b = torch.randn(n, n, device=device, dtype=dt)
+        for _ in range(2):
+            a @ b
+        torch.cuda.synchronize(device)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        best = float("inf")
+        for _ in range(5):
+            e0.record()
+            a @ b
+            e1.record()
+            torch.cuda.synchronize(device)
+            best = min(best, e0.elapsed_time(e1))
+        res[name] = 2 * n ** 3 / (best * 1e-3) / 1e12
+        del a, b
+    torch.backends.cuda.matmul.allow_tf32 = old
+    peaks.update(res)
+    return peaks
+
+
+# ncu summary of the trace kernel on this workload (profiles/trace_fp64_flrw_patch.md):
+# DRAM bytes per launch from one capture; None until a capture exists.
+NCU_TRAFFIC_BYTES = {"fp64": None, "fp64_fast": None, "mixed": None}
+
+
+# ------------------------------------------------------------------ ours
+def run_ours(args, rank, world, local):
+    import torch
+
+    from excalibur_tool_gb300 import _native as N
+    from excalibur_tool_gb300 import roofline, workloads
+    from excalibur_tool_gb300.integration.integrator import Integrator
+    from excalibur_tool_gb300.trace import trace_batch
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    wl = workloads.flrw_patch(128, args.side, precision=args.precision, device=dev)
+    metric, states, cfg = wl.metric, wl.states, wl.cfg
+    stream = torch.cuda.current_stream(dev)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    peaks = measured_peaks(dev)
+
+    for _ in range(max(args.warmup, 1)):
+        res = trace_batch(metric, states, cfg)
+    torch.cuda.synchronize(dev)
+    steps_per_batch = int(res.n_steps.sum().item())
+    rays = states.shape[0]
+    status_counts = np.bincount(res.status.cpu().numpy(), minlength=11).tolist()
+
+    # ---- device-resident timed region ----
+    clocks = ClockSampler(local)
+    clocks.start()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    barrier(world)
+    torch.cuda.synchronize(dev)
+    t_wall = time.perf_counter()
+    for k in range(args.steps):
+        flush.fill_(float(k))                      # evict L2 between timed steps
+        evs[k][0].record(stream)
+        res = trace_batch(metric, states, cfg)
+        evs[k][1].record(stream)
+    torch.cuda.synchronize(dev)
+    barrier(world)
+    wall = time.perf_counter() - t_wall
+    clk = clocks.stop()
+    step_ms = [a.elapsed_time(b) for a, b in evs]
+    dev_s = sum(step_ms) / 1e3
+    dev_s_max = max_over_ranks(dev_s, world, dev)
+    total_steps = sum_over_ranks(float(steps_per_batch * args.steps), world, dev)
+    value = total_steps / dev_s_max
+    rays_s = sum_over_ranks(float(rays * args.steps), world, dev) / dev_s_max
+    gpu_launches = args.steps                     # one exc_trace kernel per step
+
+    # ---- end to end through the public API: host states in, host results out ----
+    integ = Integrator(metric, dt=cfg.dt, integrator="rk4", dt_min=cfg.dt_min, dt_max=cfg.dt_max,
+                       precision=args.precision, max_iter=cfg.max_iter)
+    host_states = states.cpu().pin_memory()
+    out_host = None
+    for _ in range(max(1, args.warmup)):
+        out_host = integ.integrate_batch(host_states, "box", cfg.stop_box, out_host=out_host, a_stop=0.5,
+                                         lens_center=cfg.lens_center)
+    barrier(world)
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        flush.fill_(float(k))
+        out_host = integ.integrate_batch(host_states, "box", cfg.stop_box, out_host=out_host, a_stop=0.5,
+                                         lens_center=cfg.lens_center)
+    torch.cuda.synchronize(dev)
+    barrier(world)
+    e2e_s = max_over_ranks(time.perf_counter() - t0, world, dev)
+    h2d = host_states.numel() * 8
+    d2h = sum(t.numel() * t.element_size() for t in out_host.values())
+    e2e_steps = int(out_host["n_steps"].sum())
+    e2e_value = sum_over_ranks(float(e2e_steps * args.steps), world, dev) / e2e_s
+
+    # ---- roofline of the trace kernel ----
+    mean_launch_s = dev_s / args.steps
+    flops_launch = steps_per_batch * roofline.FLOPS_PER_RK4_STEP_FLRW
+    if args.precision == "mixed":
+        bound, peak = "fp32", peaks.get("fp32_tflops")
+    else:
+        bound, peak = "fp64", peaks.get("fp64_tflops")
+    achieved = flops_launch / mean_launch_s / 1e12
+    roof = {"bound": bound, "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+            "frac": achieved / peak if peak else None, "traffic": NCU_TRAFFIC_BYTES.get(args.precision),
+            "peak_source": f"cuBLAS {'D' if bound == 'fp64' else 'S'}GEMM measured in this run",
+            "algorithmic_flops_per_launch": flops_launch, "gather_bytes_per_launch":
+                steps_per_batch * roofline.bytes_per_rk4_step(8),
+            "hbm_gbs_measured": peaks.get("hbm_gbs")}
+
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": dev_s_max * 1e3 / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": {"fp64": "f64", "fp64_fast": "f64", "mixed": "f32+f64"}[args.precision],
+            "data": "synthetic (seeded Plummer + Gaussian random field; patch of directions)",
+            "config": {"workload": WORKLOAD, "precision": args.precision, "photons": rays,
+                       "photon_steps_per_batch": steps_per_batch, "grid": "128^3 float64 (16.8 MB)",
+                       "l2": "flushed between timed steps (256 MiB write); grid itself fits in L2",
+                       "parallelism": f"replicas x{world} (independent photon batches)",
+                       "status_counts": status_counts},
+            "rays_per_s": rays_s, "wall_s_timed": wall,
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                    "api": "Integrator.integrate_batch(pinned host states) -> pinned host results"},
+            "gpu_launches": gpu_launches, "roofline": roof, "clocks": clk}
+
+    if not args.no_variants and world == 1:
+        line["variants"] = run_variants(args, wl, peaks, dev, stream)
+    if not args.no_cpu_baseline and world == 1 and rank == 0:
+        line["cpu_baseline"] = cpu_baseline(wl, steps_per_batch)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def run_variants(args, wl, peaks, dev, stream):
+    """The other precision builds on the same batch, with their error against the parity build."""
+    import dataclasses
+    import torch
+
+    from excalibur_tool_gb300 import _native as N
+    from excalibur_tool_gb300.trace import trace_batch
+
+    ref = trace_batch(wl.metric, wl.states, dataclasses.replace(wl.cfg, precision="fp64"))
+    torch.cuda.synchronize(dev)
+    out = {}
+    for prec in ("fp64", "fp64_fast", "mixed"):
+        if prec == args.precision:
+            continue
+        cfg = dataclasses.replace(wl.cfg, precision=prec)
+        try:
+            r = trace_batch(wl.metric, wl.states, cfg)
+        except N.NativeError as e:
+            out[prec] = {"unavailable": str(e).splitlines()[0][:200]}
+            continue
+        torch.cuda.synchronize(dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(3):
+            r = trace_batch(wl.metric, wl.states, cfg)
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        s = e0.elapsed_time(e1) / 3e3
+        steps = int(r.n_steps.sum())
+        out[prec] = {"photon_steps_per_s": steps / s, "rays_per_s": wl.states.shape[0] / s,
+                     "speedup_vs_fp64": None, **errors_vs(ref, r)}
+    return out
+
+
+def errors_vs(ref, r):
+    """|dz|, relative time-delay and deflection error of `r` against the parity build `ref`."""
+    from excalibur_tool_gb300.observables.lensing import deflection_angle, time_delay_excess, redshift_total
+
+    o0 = ref.obs.cpu().numpy()
+    o1 = r.obs.cpu().numpy()
+    z0, z1 = redshift_total(o0), redshift_total(o1)
+    t0, t1 = time_delay_excess(o0), time_delay_excess(o1)
+    a0, a1 = deflection_angle(o0), deflection_angle(o1)
+    return {"max_abs_dz": float(np.nanmax(np.abs(z1 - z0))),
+            "max_rel_time_delay": float(np.nanmax(np.abs(t1 - t0) / np.maximum(np.abs(t0), 1e-300))),
+            "max_abs_deflection_rad": float(np.nanmax(np.abs(a1 - a0))),
+            "max_rel_state": float(np.nanmax(np.abs(r.state.cpu().numpy() - ref.state.cpu().numpy()) /
+                                             np.maximum(np.abs(ref.state.cpu().numpy()), 1e-300)))}
+
+
+# ------------------------------------------------------------------ CPU side
+def _oracle_inputs(wl=None):
+    """Workload inputs as host arrays for the oracle (built without the GPU library)."""
+    from excalibur_tool_gb300 import workloads
+    from excalibur_tool_gb300.core.constants import c, one_Mpc
+    from excalibur_tool_gb300.objects.fields import lens_plus_grf
+    from oracle import oracle as O
+    from oracle.oracle import FieldSpec, Spacetime
+
+    cz = workloads.lcdm()
+    n = 128
+    phi = lens_plus_grf(n, workloads.BOX, workloads.LENS_MASS, 5 * one_Mpc, workloads.LENS, seed=2)
+    spec = Spacetime(kind="flrw", fields=[FieldSpec(phi, (workloads.BOX / n,) * 3, (0.0, 0.0, 0.0), "periodic")],
+                     cosmology="table", a_grid=cz.a_grid, eta_min=cz.eta_min, eta_step=cz.eta_step, H0=cz.H0,
+                     omega=(0.3, 0.0, 0.0, 0.7))
+    if wl is not None:
+        states = wl.states.cpu().numpy()
+        cfg = wl.cfg
+    else:
+        k = np.array([1.0, 0.0, 0.0])
+        e1, e2 = np.array([0.0, 1.0, 0.0]), np.array([0.0, 0.0, 1.0])
+        half = np.tan(np.deg2rad(5.0))
+        t = (np.arange(256) + 0.5) / 256 * 2 - 1
+        A, B = np.meshgrid(t, t, indexing="ij")
+        d = k[None] + (A.reshape(-1, 1) * half) * e1[None] + (B.reshape(-1, 1) * half) * e2[None]
+        d /= np.linalg.norm(d, axis=1)[:, None]
+        states = np.zeros((len(d), 8))
+        states[:, 0] = cz._eta_at_a1
+        states[:, 1:4] = workloads.OBSERVER
+        states[:, 5:8] = d * c
+        states, _ = O.null_init(spec, states, -1.0)
+        from excalibur_tool_gb300.trace import TraceConfig
+
+        B_ = workloads.BOX
+        cfg = TraceConfig(stepper="rk4", dt=workloads.DLAMBDA, dt_min=workloads.DLAMBDA, dt_max=workloads.DLAMBDA,
+                          max_steps=2 ** 62, max_iter=100_000, stop_box=((0, 0, 0), (B_, B_, B_)), a_stop=0.5,
+                          lens_center=tuple(workloads.LENS))
+    return spec, states, cfg
+
+
+def host_threads():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def time_oracle(spec, states, cfg, threads, target_s=12.0):
+    """Oracle photon-steps/s on a bounded sample (about target_s of CPU work)."""
+    from oracle import oracle as O
+
+    probe = states[:: max(1, len(states) // (threads * 8))][: threads * 8]
+    t0 = time.perf_counter()
+    r = O.trace(spec, probe, cfg, threads=threads)
+    dt = time.perf_counter() - t0
+    rate = r.n_steps.sum() / dt
+    per_photon = r.n_steps.mean()
+    n_sample = int(min(len(states), max(threads * 16, target_s * rate / max(per_photon, 1))))
+    idx = np.linspace(0, len(states) - 1, n_sample).astype(int)
+    t0 = time.perf_counter()
+    r = O.trace(spec, states[idx], cfg, threads=threads)
+    dt = time.perf_counter() - t0
+    return float(r.n_steps.sum() / dt), n_sample, float(dt), int(r.n_steps.sum())
+
+
+def cpu_baseline(wl, steps_per_batch):
+    spec, states, cfg = _oracle_inputs(wl)
+    threads = host_threads()
+    rate, n, dt, steps = time_oracle(spec, states, cfg, threads)
+    return {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{n} of {len(states)} photons of the same batch ({steps} photon-steps, {dt:.1f} s), "
+                      f"C restatement of integrate_single (oracle/exc_oracle.c), {threads} threads"}
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    spec, states, cfg = _oracle_inputs(None)
+    threads = host_threads()
+    from oracle import oracle as O
+
+    per_step = []
+    for k in range(args.warmup + args.steps):
+        rate, n, dt, steps = time_oracle(spec, states, cfg, threads, target_s=10.0)
+        if k >= args.warmup:
+            per_step.append((rate, n, dt, steps))
+    total_steps = sum(p[3] for p in per_step)
+    total_s = sum(p[2] for p in per_step)
+    value = total_steps / total_s
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total_s * 1e3 / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "impl": "reference",
+            "data": "synthetic (seeded Plummer + Gaussian random field; patch of directions)",
+            "config": {"workload": WORKLOAD, "precision": "fp64", "photons": len(states),
+                       "parallelism": f"{threads} host threads"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": f"each step: {per_step[0][1]} of {len(states)} photons "
+                                       f"(~10 s of CPU work), C restatement of integrate_single "
+                                       f"(oracle/exc_oracle.c), {threads} threads"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_setup(args.gpus)
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_ours(args, rank, world, local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

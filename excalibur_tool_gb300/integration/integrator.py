@@ -1,0 +1,232 @@
+"""Integrators and the integration driver (excalibur/integration/integrator.py).
+
+Same classes and signatures as the reference. What changes is where the work
+runs: `Integrator.integrate` traces every photon in one persistent GPU launch
+(`trace.trace_batch` -> `exc_trace`) instead of a Python loop over
+`integrate_single`; `integrate_single` is the same launch with one photon.
+The steppers' `step()` run one step through the same kernel.
+
+Differences from the reference, all deliberate:
+* `mode` ("sequential" / "parallel" / "chunked") selects nothing: one GPU
+  launch replaces the process pools (integrator.py:443-473).
+* stop modes: "steps" as in the reference; "a" stops once a(eta) <= value,
+  and "box" at the first exit from the grid box (the reference's "a",
+  "redshift" and "chi" read attributes its Photon never sets,
+  integrator.py:204-211, so they cannot work there).
+* photons that the reference would abort with an exception (outside the
+  grid, horizon, non-finite state) get a failure status instead and are
+  counted as failures by `integrate`, like the reference's chunked mode
+  (integrator.py:414-429).
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from .. import _native as N
+from ..trace import TraceConfig, trace_batch
+
+
+class _Stepper:
+    name = ""
+
+    def step(self, metric, state, dt, rtol=1e-9, atol=1e-13):
+        """One step on the GPU: returns (new_state, dt_new, accepted)."""
+        import torch
+
+        cfg = TraceConfig(stepper=self.name, dt=dt, dt_min=abs(dt), dt_max=abs(dt), rtol=rtol, atol=atol,
+                          max_iter=1, max_steps=1, observables=False, use_queue=False,
+                          tableau=getattr(self, "tableau", "reference"))
+        s = torch.as_tensor(np.asarray(state, dtype=np.float64)[None]).cuda()
+        r = trace_batch(metric, s, cfg)
+        st = int(r.status[0])
+        if st in N.FAILED_STATUSES:
+            raise ValueError(f"step failed: {N.STATUS_NAMES.get(st, st)}")
+        accepted = int(r.n_steps[0]) == 1
+        return r.state[0].cpu().numpy(), float(r.dt[0]), accepted
+
+
+class RK4(_Stepper):
+    """Classic RK4 (integrator.py:9-22)."""
+    name = "rk4"
+
+
+class Leapfrog4(_Stepper):
+    """Forest-Ruth 4th-order symplectic (integrator.py:24-90)."""
+    name = "leapfrog4"
+
+
+class RK45Adaptive(_Stepper):
+    """Embedded RK4(5) with the reference's weights (integrator.py:93-152);
+    `tableau="fehlberg"` uses Fehlberg's 6656/12825 instead of 665/1287."""
+    name = "rk45"
+
+    def __init__(self, tableau="reference"):
+        self.tableau = tableau
+
+
+class Integrator:
+    STOP_MODES = {"steps", "redshift", "a", "chi", "box"}
+    INTEGRATORS = {"rk45": RK45Adaptive, "rk4": RK4, "leapfrog4": Leapfrog4}
+
+    def __init__(self, metric, dt=1e-3, mode="sequential", integrator="rk45", rtol=1e-9, atol=1e-13,
+                 dt_min=1e14, dt_max=1e17, n_workers=None, chunk_size=50, *, precision="fp64",
+                 tableau="reference", max_iter=10_000, device=None):
+        self.metric = metric
+        self.dt = dt
+        self.mode = mode
+        self.rtol = rtol
+        self.atol = atol
+        self.dt_min = dt_min
+        self.dt_max = dt_max
+        self.chunk_size = chunk_size
+        self.n_workers = n_workers
+        if integrator.lower() not in self.INTEGRATORS:
+            raise ValueError(f"Integrator '{integrator}' not supported. Available: {list(self.INTEGRATORS.keys())}")
+        self.integrator_name = integrator.lower()
+        self.integrator = self.INTEGRATORS[self.integrator_name]()
+        self.precision = precision
+        self.tableau = tableau
+        self.max_iter = max_iter
+        self.device = device
+
+    # ------------------------------------------------------------ config
+    def config(self, stop_mode="steps", stop_value=100, *, record_every=None, renormalize_every=0,
+               observables=True, **kw) -> TraceConfig:
+        if stop_mode not in self.STOP_MODES:
+            raise ValueError(f"stop_mode must be one of {self.STOP_MODES}")
+        max_steps = int(stop_value) if stop_mode == "steps" else 2 ** 62
+        a_stop = None
+        stop_box = None
+        if stop_mode == "a":
+            a_stop = float(stop_value)
+        elif stop_mode == "box":
+            stop_box = stop_value if stop_value is not None else self._grid_box()
+        elif stop_mode in ("redshift", "chi"):
+            raise NotImplementedError(
+                f"stop_mode '{stop_mode}' is not available (the reference's Photon never defines it); "
+                "use 'a' (scale factor) or 'box'")
+        return TraceConfig(stepper=self.integrator_name, tableau=self.tableau, precision=self.precision,
+                           dt=float(self.dt), dt_min=float(self.dt_min), dt_max=float(self.dt_max),
+                           rtol=float(self.rtol), atol=float(self.atol), max_iter=int(self.max_iter),
+                           max_steps=max_steps, stop_box=stop_box, a_stop=a_stop,
+                           renormalize_every=int(renormalize_every), record_every=record_every,
+                           observables=observables, **kw)
+
+    def _grid_box(self):
+        g = getattr(self.metric, "grid", None)
+        if g is None:
+            raise ValueError("stop_mode='box' needs a metric with a grid, or an explicit ((lo), (hi)) box")
+        lo = np.asarray(g.origin[:3], dtype=float)
+        hi = lo + np.asarray(g.shape[:3], dtype=float) * np.asarray(g.spacing[:3], dtype=float)
+        return (tuple(lo), tuple(hi))
+
+    def _device(self):
+        import torch
+
+        if not torch.cuda.is_available():
+            raise N.NativeError("a CUDA device is required (the tracer has no host fallback)")
+        return torch.device(self.device) if self.device is not None else torch.device("cuda", torch.cuda.current_device())
+
+    def _prepare_state(self, state):
+        internal = getattr(self.metric, "internal_coords", None)
+        input_coords = getattr(self.metric, "input_coords", None)
+        if internal == "spherical" and input_coords == "cartesian":
+            state = self.metric.cartesian_state_to_spherical(state)
+        return state
+
+    # --------------------------------------------------- batched API
+    def trace(self, states, stop_mode="steps", stop_value=100, *, field_index=None, **cfg_kw):
+        """Trace a [N, 8] float64 CUDA tensor of states; returns a TraceResult (device tensors)."""
+        return trace_batch(self.metric, states, self.config(stop_mode, stop_value, **cfg_kw), field_index=field_index)
+
+    def integrate_batch(self, states_host, stop_mode="steps", stop_value=100, *, field_index=None,
+                        out_host=None, **cfg_kw):
+        """End-to-end batch call on HOST arrays: copy in, trace, copy results back.
+
+        `states_host` is a [N, 8] float64 array or (pinned) CPU tensor. Returns a
+        dict of host arrays: state, status, n_steps and obs (when enabled).
+        """
+        import torch
+
+        dev = self._device()
+        src = states_host if isinstance(states_host, torch.Tensor) else torch.from_numpy(
+            np.ascontiguousarray(states_host, dtype=np.float64))
+        d_states = src.to(dev, non_blocking=True)
+        res = trace_batch(self.metric, d_states, self.config(stop_mode, stop_value, **cfg_kw),
+                          field_index=field_index)
+        if out_host is None:
+            out_host = {"state": torch.empty(res.state.shape, dtype=torch.float64, pin_memory=True),
+                        "status": torch.empty(res.status.shape, dtype=torch.int32, pin_memory=True),
+                        "n_steps": torch.empty(res.n_steps.shape, dtype=torch.int32, pin_memory=True)}
+            if res.obs is not None:
+                out_host["obs"] = torch.empty(res.obs.shape, dtype=torch.float64, pin_memory=True)
+        out_host["state"].copy_(res.state, non_blocking=True)
+        out_host["status"].copy_(res.status, non_blocking=True)
+        out_host["n_steps"].copy_(res.n_steps, non_blocking=True)
+        if res.obs is not None and "obs" in out_host:
+            out_host["obs"].copy_(res.obs, non_blocking=True)
+        torch.cuda.current_stream(dev).synchronize()
+        return out_host
+
+    # ---------------------------------------------- reference-facing API
+    def integrate_single(self, photon, stop_mode="steps", stop_value=100, *, record_every: int = 1,
+                         trace_norm: bool = False, renormalize_every: int = 0):
+        """Integrator.integrate_single (integrator.py:218-409): mutates `photon`
+        (x, u, quantities, history) exactly as the reference does."""
+        import torch
+        from .._evaluate import null_error
+
+        if record_every < 0:
+            raise ValueError("record_every must be >= 0")
+        if renormalize_every < 0:
+            raise ValueError("renormalize_every must be >= 0")
+        state = self._prepare_state(np.concatenate([photon.x, photon.u]))
+        dev = self._device()
+        if trace_norm and not hasattr(photon, "norm_history"):
+            photon.norm_history = []
+        s = torch.as_tensor(np.asarray(state, dtype=np.float64)[None], device=dev)
+        res = self.trace(s, stop_mode, stop_value, record_every=record_every,
+                         renormalize_every=renormalize_every, observables=False)
+        st = int(res.status[0])
+        nrec = int(res.n_records[0])
+        rows = res.records[0, :min(nrec, res.records.shape[1])].cpu().numpy()
+        final = res.state[0].cpu().numpy()
+        for i, row in enumerate(rows):
+            # the first record (and any recorded before quantities exist) has 8 columns
+            photon.history.append(row if not np.isnan(row[8:]).all() else row[:8])
+        photon.x = final[:4]
+        photon.u = final[4:]
+        if st in N.FAILED_STATUSES:
+            raise ValueError(f"integration failed: {N.STATUS_NAMES.get(st, st)}")
+        photon.quantities = rows[-1][8:] if len(rows) else np.array([])
+        if trace_norm:
+            rel, _ = null_error(self.metric, np.stack([rows[0][:8], final]))
+            photon.norm_history.extend(rel.cpu().numpy().tolist())
+        return photon
+
+    def integrate(self, photons, stop_mode="steps", stop_value=100, verbose=True):
+        """Integrator.integrate (integrator.py:434-476): all photons in one GPU launch.
+
+        Final states are written back into the Photon objects; returns the
+        number of photons that finished without a failure status."""
+        import torch
+
+        if stop_mode not in self.STOP_MODES:
+            raise ValueError(f"stop_mode must be one of {self.STOP_MODES}")
+        plist = list(photons)
+        if not plist:
+            return 0
+        states = np.stack([self._prepare_state(np.concatenate([p.x, p.u])) for p in plist])
+        out = self.integrate_batch(torch.from_numpy(states).pin_memory(), stop_mode, stop_value, observables=False)
+        final = out["state"].numpy()
+        status = out["status"].numpy()
+        ok = 0
+        for p, s, st in zip(plist, final, status):
+            p.x = s[:4].copy()
+            p.u = s[4:].copy()
+            p.history.append(s.copy())
+            if st not in N.FAILED_STATUSES:
+                ok += 1
+        if verbose:
+            print(f"GPU integration of {len(plist)} photons: {ok} succeeded")
+        return ok

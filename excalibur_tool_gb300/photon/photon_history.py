@@ -1,0 +1,20 @@
+"""Photon history (excalibur/photon/photon_history.py:19-44)."""
+import numpy as np
+
+
+class PhotonHistory:
+    def __init__(self):
+        self.states = []
+
+    def append(self, state):
+        self.states.append(np.array(state, copy=True))
+
+    def as_array(self):
+        """History padded with NaN to a [n_records, max_cols] array (runner layout)."""
+        if not self.states:
+            return np.zeros((0, 0))
+        w = max(len(s) for s in self.states)
+        out = np.full((len(self.states), w), np.nan)
+        for i, s in enumerate(self.states):
+            out[i, :len(s)] = s
+        return out

@@ -1,0 +1,287 @@
+"""Photon collections and generators (excalibur/photon/photons.py).
+
+The generators keep the reference's direction sampling (cone grid with the
+theta = 0 de-duplication, random cone, impact-parameter bins, Rodrigues
+rotation `_rotate_to_direction`); the null-normalised u^0 is solved on the
+GPU by `exc_null_init` (`_solve_u0_from_null_condition`, photons.py:540-568).
+Photons are held as one [N, 8] float64 batch; `Photon` objects are made on
+demand for code that iterates over `photons.photons`.
+
+New generators for the batched workloads: `generate_polar_grid`
+(theta_i = (i + 1/2) alpha / n_theta, no on-axis ray), `generate_patch_grid`
+(pixel centres of a square tangent-plane patch) and `generate_full_sky`
+(uniform random directions on the sphere).
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from ..core.constants import c
+from ..core.coordinates import cartesian_velocity_to_spherical
+from .photon import Photon
+
+
+def rotate_to_direction(vectors, target_direction):
+    """Rodrigues rotation taking +z onto `target_direction` (photons.py:426-459), batched."""
+    v = np.atleast_2d(np.asarray(vectors, dtype=float))
+    t = np.asarray(target_direction, dtype=float)
+    t = t / np.linalg.norm(t)
+    z = np.array([0, 0, 1])
+    if np.allclose(t, z):
+        return v.copy()
+    if np.allclose(t, -z):
+        return v @ np.array([[1, 0, 0], [0, -1, 0], [0, 0, -1]]).T
+    k = np.cross(z, t)
+    k = k / np.linalg.norm(k)
+    cos_a = np.dot(z, t)
+    sin_a = np.linalg.norm(np.cross(z, t))
+    return v * cos_a + np.cross(k, v) * sin_a + k[None, :] * (v @ k)[:, None] * (1 - cos_a)
+
+
+class Photons:
+    def __init__(self, metric):
+        self.metric = metric
+        self._batch = []          # list of [n, 8] arrays (host) or tensors (device)
+        self._photons = None
+        self.field_index = None
+
+    # ---- storage ---------------------------------------------------------
+    @property
+    def photons(self):
+        if self._photons is None:
+            st = self.states_numpy()
+            self._photons = [Photon(s[:4].copy(), s[4:].copy()) for s in st]
+        return self._photons
+
+    def states_numpy(self):
+        import torch
+
+        if self._photons is not None:
+            return np.array([np.concatenate([p.x, p.u]) for p in self._photons]).reshape(-1, 8)
+        if not self._batch:
+            return np.zeros((0, 8))
+        parts = [b.cpu().numpy() if isinstance(b, torch.Tensor) else b for b in self._batch]
+        return np.concatenate(parts, axis=0)
+
+    def states(self, device="cuda"):
+        """All photons as one [N, 8] float64 tensor on `device`."""
+        import torch
+
+        return torch.as_tensor(self.states_numpy(), dtype=torch.float64, device=device).contiguous()
+
+    def _append_batch(self, arr):
+        self._batch.append(arr)
+        self._photons = None
+
+    def add_photon(self, photon):
+        self.photons.append(photon)
+
+    def positions(self):
+        return self.states_numpy()[:, :4]
+
+    def directions(self):
+        return self.states_numpy()[:, 4:]
+
+    def __len__(self):
+        return len(self.photons) if self._photons is not None else sum(len(b) for b in self._batch)
+
+    @property
+    def n_photons(self):
+        return len(self)
+
+    def __getitem__(self, i):
+        return self.photons[i]
+
+    def __iter__(self):
+        return iter(self.photons)
+
+    def record_all(self):
+        for p in self.photons:
+            p.record()
+
+    # ---- u^0 on the device ------------------------------------------------
+    def _finish(self, origins, u_spatial, sign=-1.0):
+        import torch
+        from .._evaluate import null_init
+
+        n = len(u_spatial)
+        st = np.zeros((n, 8))
+        st[:, :4] = origins
+        st[:, 5:8] = u_spatial
+        t = torch.as_tensor(st, dtype=torch.float64, device="cuda")
+        status = null_init(self.metric, t, sign)
+        if int((status != 0).sum()) != 0:
+            raise ValueError("metric evaluation failed at a photon origin (outside the grid?)")
+        self._append_batch(t.cpu().numpy())
+        return t
+
+    @staticmethod
+    def _origin_looks_spherical(origin) -> bool:
+        """Spherical-like [t, r, theta, phi] vs cartesian [eta, x, y, z] (photons.py:461-487)."""
+        origin = np.asarray(origin, dtype=float)
+        if origin.shape[0] < 4:
+            return False
+        r0, t0, p0 = float(origin[1]), float(origin[2]), float(origin[3])
+        if not (np.isfinite(r0) and np.isfinite(t0) and np.isfinite(p0)) or r0 <= 0:
+            return False
+        if not (-1e-12 <= t0 <= np.pi + 1e-12):
+            return False
+        return -2 * np.pi - 1e-12 <= p0 <= 2 * np.pi + 1e-12
+
+    def _spatial_from_directions(self, origin, dirs, direction_basis):
+        """c * n-hat in the coordinate basis the metric integrates in."""
+        u_cart = dirs * c
+        if direction_basis == "coordinates":
+            return u_cart
+        if direction_basis != "cartesian":
+            raise ValueError("direction_basis must be 'coordinates' or 'cartesian'")
+        if self._origin_looks_spherical(origin):
+            r0, t0, p0 = float(origin[1]), float(origin[2]), float(origin[3])
+            x0 = r0 * np.sin(t0) * np.cos(p0)
+            y0 = r0 * np.sin(t0) * np.sin(p0)
+            z0 = r0 * np.cos(t0)
+            vr, vt, vp = cartesian_velocity_to_spherical(x0, y0, z0, u_cart[:, 0], u_cart[:, 1], u_cart[:, 2])
+            return np.stack([vr, vt, vp], axis=1)
+        return u_cart
+
+    @staticmethod
+    def _basis_alias(direction_basis, direction_coords):
+        if direction_coords is None:
+            return direction_basis
+        if direction_coords == "metric":
+            return "coordinates"
+        if direction_coords == "cartesian":
+            return "cartesian"
+        raise ValueError("direction_coords must be 'metric' or 'cartesian'")
+
+    def _rotate_to_direction(self, vector, target_direction):
+        return rotate_to_direction(vector, target_direction)[0]
+
+    # ---- reference generators ---------------------------------------------
+    def generate_cone_grid(self, n_photons, origin, central_direction, cone_angle, direction_basis="coordinates",
+                           *, direction_coords=None):
+        """Regular (theta, phi) grid in a cone (photons.py:295-424), skipping duplicate theta = 0 points."""
+        direction_basis = self._basis_alias(direction_basis, direction_coords)
+        if type(n_photons) == int:
+            n_phi = n_theta = int(np.floor(np.sqrt(n_photons)))
+        else:
+            n_theta, n_phi = n_photons[0], n_photons[1]
+        origin = np.asarray(origin, dtype=float)
+        central = np.asarray(central_direction, dtype=float)
+        central = central / np.linalg.norm(central)
+        thetas = np.linspace(0, cone_angle, n_theta)
+        phis = np.linspace(0, 2 * np.pi, n_phi, endpoint=False)
+        dirs = []
+        for th in thetas:
+            for ph in phis:
+                if th == 0 and ph != phis[0]:
+                    continue
+                dirs.append([np.sin(th) * np.cos(ph), np.sin(th) * np.sin(ph), np.cos(th)])
+        d = rotate_to_direction(np.array(dirs), central)
+        d = d / np.linalg.norm(d, axis=1)[:, None]
+        u_sp = self._spatial_from_directions(origin, d, direction_basis)
+        return self._finish(np.tile(origin, (len(d), 1)), u_sp, -1.0)
+
+    def generate_cone_random(self, n_photons, origin, central_direction, cone_angle,
+                             direction_basis="coordinates", *, direction_coords=None, seed=None):
+        """Random directions in a cone (photons.py:33-156); u^0 > 0 as in the reference."""
+        direction_basis = self._basis_alias(direction_basis, direction_coords)
+        rng = np.random.default_rng(seed)
+        origin = np.asarray(origin, dtype=float)
+        th = rng.uniform(0, cone_angle, n_photons)
+        ph = rng.uniform(0, 2 * np.pi, n_photons)
+        d = np.stack([np.sin(th) * np.cos(ph), np.sin(th) * np.sin(ph), np.cos(th)], axis=1)
+        d = rotate_to_direction(d, central_direction)
+        d = d / np.linalg.norm(d, axis=1)[:, None]
+        u_sp = self._spatial_from_directions(origin, d, direction_basis)
+        return self._finish(np.tile(origin, (n_photons, 1)), u_sp, +1.0)
+
+    def generate_impact_parameter_bins(self, origin, central_direction, b_edges, n_per_bin, *,
+                                       direction_basis="cartesian", direction_coords=None, random_phi=True,
+                                       seed=None, u0_sign=-1.0):
+        """Screen sampling in impact-parameter annuli (photons.py:570-701)."""
+        direction_basis = self._basis_alias(direction_basis, direction_coords)
+        origin = np.asarray(origin, dtype=float)
+        b_edges = np.asarray(b_edges, dtype=float)
+        if b_edges.ndim != 1 or b_edges.size < 2:
+            raise ValueError("b_edges must be a 1D array of length >= 2")
+        if np.any(b_edges[1:] <= b_edges[:-1]):
+            raise ValueError("b_edges must be strictly increasing")
+        if b_edges[0] < 0:
+            raise ValueError("b_edges must be >= 0")
+        nbins = b_edges.size - 1
+        n_list = [int(n_per_bin)] * nbins if isinstance(n_per_bin, (int, np.integer)) else [int(x) for x in n_per_bin]
+        spherical = self._origin_looks_spherical(origin)
+        if spherical and direction_basis != "cartesian":
+            raise ValueError("For spherical-like origins [t,r,theta,phi], use direction_basis='cartesian'.")
+        rng = np.random.default_rng(seed)
+        k = np.asarray(central_direction, dtype=float).reshape(3)
+        k = k / np.linalg.norm(k)
+        up = np.array([0.0, 0.0, 1.0]) if abs(np.dot(k, [0, 0, 1.0])) <= 0.95 else np.array([0.0, 1.0, 0.0])
+        e1 = np.cross(up, k)
+        e1 /= np.linalg.norm(e1)
+        e2 = np.cross(k, e1)
+        t0 = float(origin[0])
+        if spherical:
+            r0, th0, ph0 = float(origin[1]), float(origin[2]), float(origin[3])
+            oxyz = np.array([r0 * np.sin(th0) * np.cos(ph0), r0 * np.sin(th0) * np.sin(ph0), r0 * np.cos(th0)])
+        else:
+            oxyz = origin[1:4].astype(float)
+        u_cart = k * c
+        origins, u_sp = [], []
+        for ib in range(nbins):
+            b1, b2, nph = float(b_edges[ib]), float(b_edges[ib + 1]), n_list[ib]
+            if nph == 0:
+                continue
+            phis = rng.uniform(0.0, 2.0 * np.pi, size=nph) if random_phi else np.linspace(0, 2 * np.pi, nph,
+                                                                                          endpoint=False)
+            us = rng.uniform(0.0, 1.0, size=nph)
+            bs = np.sqrt(us * (b2 * b2 - b1 * b1) + b1 * b1)
+            for b, ph in zip(bs, phis):
+                xyz = oxyz + float(b) * (np.cos(ph) * e1 + np.sin(ph) * e2)
+                if spherical:
+                    r = np.sqrt(xyz @ xyz)
+                    origins.append([t0, r, np.arccos(np.clip(xyz[2] / r, -1.0, 1.0)), np.arctan2(xyz[1], xyz[0])])
+                    u_sp.append(cartesian_velocity_to_spherical(xyz[0], xyz[1], xyz[2], *u_cart))
+                else:
+                    origins.append([t0, *xyz])
+                    u_sp.append(u_cart)
+        return self._finish(np.array(origins), np.array(u_sp, dtype=float), u0_sign)
+
+    # ---- batched-workload generators --------------------------------------
+    def generate_polar_grid(self, n_theta, n_phi, origin, central_direction, cone_angle,
+                            direction_basis="cartesian", sign=-1.0):
+        """theta_i = (i + 1/2) alpha / n_theta, phi_j = 2 pi j / n_phi: no on-axis ray, no duplicates."""
+        origin = np.asarray(origin, dtype=float)
+        th = (np.arange(n_theta) + 0.5) * cone_angle / n_theta
+        ph = 2 * np.pi * np.arange(n_phi) / n_phi
+        T, P = np.meshgrid(th, ph, indexing="ij")
+        d = np.stack([np.sin(T) * np.cos(P), np.sin(T) * np.sin(P), np.cos(T)], -1).reshape(-1, 3)
+        d = rotate_to_direction(d, np.asarray(central_direction, dtype=float) / np.linalg.norm(central_direction))
+        d = d / np.linalg.norm(d, axis=1)[:, None]
+        u_sp = self._spatial_from_directions(origin, d, direction_basis)
+        return self._finish(np.tile(origin, (len(d), 1)), u_sp, sign)
+
+    def generate_patch_grid(self, n_side, origin, central_direction, patch_deg, sign=-1.0, device="cuda"):
+        """n_side^2 pixel centres of a patch_deg x patch_deg tangent-plane patch around the axis."""
+        import torch
+
+        k = np.asarray(central_direction, dtype=float)
+        k = k / np.linalg.norm(k)
+        up = np.array([0.0, 0.0, 1.0]) if abs(k[2]) < 0.9 else np.array([0.0, 1.0, 0.0])
+        e1 = np.cross(up, k)
+        e1 /= np.linalg.norm(e1)
+        e2 = np.cross(k, e1)
+        half = np.tan(np.deg2rad(patch_deg / 2.0))
+        t = (np.arange(n_side) + 0.5) / n_side * 2 - 1
+        A, B = np.meshgrid(t, t, indexing="ij")
+        d = k[None] + (A.reshape(-1, 1) * half) * e1[None] + (B.reshape(-1, 1) * half) * e2[None]
+        d /= np.linalg.norm(d, axis=1)[:, None]
+        return self._finish(np.tile(np.asarray(origin, dtype=float), (len(d), 1)), d * c, sign)
+
+    def generate_full_sky(self, n_photons, origin, seed, sign=-1.0):
+        """Uniform random directions on the sphere (numpy default_rng(seed))."""
+        rng = np.random.default_rng(seed)
+        v = rng.standard_normal((n_photons, 3))
+        v /= np.linalg.norm(v, axis=1)[:, None]
+        return self._finish(np.tile(np.asarray(origin, dtype=float), (n_photons, 1)), v * c, sign)

@@ -1,0 +1,19 @@
+"""Algorithmic work per photon-step, for roofline reporting.
+
+Counted by executing the reference's formulas on a counting float
+(oracle/opcount.py; tests/test_roofline_counts.py keeps these in sync):
+one RK4 step of the FLRW-fast tracer = 4 RHS evaluations (periodic trilinear
+Phi + base-node gradient, LCDM a(eta) and adot, tensorial Christoffel
+contraction) + the RK4 combination.
+"""
+
+# floating-point add/sub/mul/div (+ the periodic wrap's fmod) per RK4 photon-step
+FLOPS_PER_RK4_STEP_FLRW = 1009
+SQRT_PER_RK4_STEP_FLRW = 4
+# bytes gathered per RK4 photon-step: 4 RHS x (11 distinct grid nodes + 2 a(eta) table entries)
+NODES_PER_RHS = 11
+TABLE_ENTRIES_PER_RHS = 2
+
+
+def bytes_per_rk4_step(field_itemsize: int) -> int:
+    return 4 * (NODES_PER_RHS * field_itemsize + TABLE_ENTRIES_PER_RHS * 8)

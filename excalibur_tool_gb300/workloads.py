@@ -1,0 +1,92 @@
+"""The benchmark workloads, built from seeded synthetic inputs.
+
+* lens_cone (1,024 rays): Schwarzschild point mass 1e15 Msun at the centre
+  (500, 500, 500) Mpc of a 1000 Mpc box, observer at (0, 500, 500) Mpc, 32x32
+  polar grid of directions in a 5 deg half-angle cone, RK4 with
+  dlambda = 0.5 Mpc / c, 2,000 steps.
+* flrw_patch (65,536 rays): perturbed FLRW (LCDM, Omega_m = 0.3, h = 0.7) with
+  Phi on a 128^3 float64 grid over 1000 Mpc = Plummer sphere (1e15 Msun,
+  softening 5 Mpc) + Gaussian random field (P(k) ~ k^-3, rms Phi/c^2 = 1e-5,
+  seed 2); 256x256 directions in a 10 x 10 deg patch; RK4 with
+  deta = 0.5 Mpc, until box exit or a <= 0.5.
+* flrw_patch_fp32grid: the same construction on a 512^3 float32 grid,
+  2048 x 2048 directions in a 20 x 20 deg patch (seed 4).
+* multi_field: one main field plus 16 random-field realisations (seeds 1..16,
+  grids cycling 64^3/128^3/256^3) traced in one launch.
+
+Inputs are resident on the GPU when the builders return.
+"""
+from __future__ import annotations
+
+import dataclasses
+
+import numpy as np
+
+from .core.constants import c, one_Mpc, one_Msun, G
+from .core.cosmology import LCDM_Cosmology
+from .grid.grid import Grid
+from .grid.interpolator_4d_fast import InterpolatorFast
+from .metrics.perturbed_flrw_metric_fast import PerturbedFLRWMetricFast
+from .metrics.schwarzschild_metric_fast import SchwarzschildMetricFast
+from .objects.fields import lens_plus_grf
+from .photon.photons import Photons
+from .trace import TraceConfig
+
+BOX = 1000 * one_Mpc
+LENS = np.array([500.0, 500.0, 500.0]) * one_Mpc
+OBSERVER = np.array([0.0, 500.0, 500.0]) * one_Mpc
+LENS_MASS = 1e15 * one_Msun
+DLAMBDA = 0.5 * one_Mpc / c
+
+_COSMO = None
+
+
+def lcdm():
+    global _COSMO
+    if _COSMO is None:
+        _COSMO = LCDM_Cosmology(70, 0.3, 0.0, 0.7)
+    return _COSMO
+
+
+@dataclasses.dataclass
+class Workload:
+    name: str
+    metric: object
+    states: "torch.Tensor"
+    cfg: TraceConfig
+    info: dict
+    field_index: "torch.Tensor" = None
+
+
+def flrw_patch(n_grid=128, n_side=256, patch_deg=10.0, seed=2, field_dtype=np.float64, precision="fp64",
+               device="cuda", with_grf=True):
+    import torch
+
+    cz = lcdm()
+    phi = lens_plus_grf(n_grid, BOX, LENS_MASS, 5 * one_Mpc, LENS, seed=seed, dtype=field_dtype, with_grf=with_grf)
+    grid = Grid((n_grid,) * 3, (BOX / n_grid,) * 3, (0.0, 0.0, 0.0))
+    grid.add_field("Phi", phi)
+    interp = InterpolatorFast(grid, boundary="periodic")
+    metric = PerturbedFLRWMetricFast(cz.a_of_eta, grid, interp, adot_of_eta=cz.adot_of_eta)
+    ph = Photons(metric)
+    states = ph.generate_patch_grid(n_side, [cz._eta_at_a1, *OBSERVER], LENS - OBSERVER, patch_deg)
+    cfg = TraceConfig(stepper="rk4", precision=precision, dt=DLAMBDA, dt_min=DLAMBDA, dt_max=DLAMBDA,
+                      max_steps=2 ** 62, max_iter=100_000, stop_box=((0, 0, 0), (BOX, BOX, BOX)), a_stop=0.5,
+                      lens_center=tuple(LENS))
+    info = {"grid": f"{n_grid}^3 {np.dtype(field_dtype).name}", "photons": n_side * n_side,
+            "patch_deg": patch_deg, "seed": seed, "grid_bytes": int(phi.nbytes)}
+    return Workload(f"flrw_patch_{n_grid}", metric, states.to(device), cfg, info)
+
+
+def lens_cone(n_theta=32, n_phi=32, cone_deg=5.0, n_steps=2000, precision="fp64", device="cuda"):
+    from .core.coordinates import cartesian_to_spherical
+
+    rs = 2 * G * LENS_MASS / c ** 2
+    metric = SchwarzschildMetricFast(LENS_MASS, rs * (1 + 1e-6), center=LENS, coords="spherical",
+                                     analytical_geodesics=True, free_time_geodesic=True)
+    origin = np.array([0.0, *cartesian_to_spherical(*(OBSERVER - LENS))])
+    ph = Photons(metric)
+    states = ph.generate_polar_grid(n_theta, n_phi, origin, LENS - OBSERVER, np.deg2rad(cone_deg))
+    cfg = TraceConfig(stepper="rk4", precision=precision, dt=DLAMBDA, dt_min=DLAMBDA, dt_max=DLAMBDA,
+                      max_steps=n_steps, max_iter=n_steps)
+    return Workload("lens_cone", metric, states.to(device), cfg, {"photons": n_theta * n_phi})

@@ -66,7 +66,8 @@ def test_cosmology_matches_reference(cuda):
     a = lc.a_of_eta(cz["etas"])
     adot = lc.adot_of_eta(cz["etas"])
     assert np.array_equal(a, cz["a"])
-    assert rel_err(adot, cz["adot"]).max() <= 2.3e-16
+    # adot = a^2 H0 E(z): E sums Omega_m (1+z)^3 (libm pow in the reference) -> <= 2 ulp
+    assert rel_err(adot, cz["adot"]).max() <= 4.5e-16
 
 
 @pytest.mark.parametrize("variant,cosmo,analytical", [("lcdm_tensorial", "table", False),
