@@ -109,6 +109,10 @@ __device__ __forceinline__ double trilinear(double c000, double c100, double c01
 
 // One spatial snapshot `it` (of nt, innermost index) of a 3-D/4-D field.
 // Returns an EXC_PH_* failure code, or 0 with `o` filled (o.dtd = 0).
+// The cell coordinate rel = (x - origin) / spacing is an IEEE division in
+// every build: the base-node gradient is discontinuous across cell faces, and
+// positions that sit exactly on a node plane (an observer placed on a grid
+// node, as the reference runner does) must select the reference's cell.
 template <class FT>
 __device__ __forceinline__ int interp_snapshot(const ExcField& f, const double* fi, const FT* __restrict__ d,
                                                int64_t nt, int64_t it, double x, double y, double z,
@@ -123,7 +127,7 @@ __device__ __forceinline__ int interp_snapshot(const ExcField& f, const double* 
     x = ox + py_fmod(x - ox, Lx);
     y = oy + py_fmod(y - oy, Ly);
     z = oz + py_fmod(z - oz, Lz);
-    const double rx = div_c(x - ox, sx, fi[0]), ry = div_c(y - oy, sy, fi[1]), rz = div_c(z - oz, sz, fi[2]);
+    const double rx = (x - ox) / sx, ry = (y - oy) / sy, rz = (z - oz) / sz;
     if (!isfinite(rx) || !isfinite(ry) || !isfinite(rz)) return EXC_PH_NONFINITE;
     int64_t i0 = (int64_t)floor(rx), j0 = (int64_t)floor(ry), k0 = (int64_t)floor(rz);
     const double dx = rx - (double)i0, dy = ry - (double)j0, dz = rz - (double)k0;
@@ -150,7 +154,7 @@ __device__ __forceinline__ int interp_snapshot(const ExcField& f, const double* 
     if (x < ox) x = ox; else if (x > hx) x = hx;
     if (y < oy) y = oy; else if (y > hy) y = hy;
     if (z < oz) z = oz; else if (z > hz) z = hz;
-    const double rx = div_c(x - ox, sx, fi[0]), ry = div_c(y - oy, sy, fi[1]), rz = div_c(z - oz, sz, fi[2]);
+    const double rx = (x - ox) / sx, ry = (y - oy) / sy, rz = (z - oz) / sz;
     if (!isfinite(rx) || !isfinite(ry) || !isfinite(rz)) return EXC_PH_NONFINITE;
     int64_t i0 = (int64_t)floor(rx), j0 = (int64_t)floor(ry), k0 = (int64_t)floor(rz);
     if (i0 < 0) i0 = 0;
@@ -175,7 +179,7 @@ __device__ __forceinline__ int interp_snapshot(const ExcField& f, const double* 
   // EXC_BOUNDARY_ERROR: fused_interpolation_gradient_3d_error,
   // interpolator_4d_fast.py:50-91 (same arithmetic as the legacy strict
   // interpolator, grid/interpolator_fast.py:119-192)
-  const double rx = div_c(x - ox, sx, fi[0]), ry = div_c(y - oy, sy, fi[1]), rz = div_c(z - oz, sz, fi[2]);
+  const double rx = (x - ox) / sx, ry = (y - oy) / sy, rz = (z - oz) / sz;
   if (rx < 1.0 || rx >= (double)nx - 2.0 || ry < 1.0 || ry >= (double)ny - 2.0 ||
       rz < 1.0 || rz >= (double)nz - 2.0)
     return EXC_PH_OUTSIDE_GRID;
@@ -215,9 +219,9 @@ __device__ __forceinline__ int interp_field(const ExcField& f, const double* fi,
     const double et = 1e-12 * stp;
     const double ht = ot + (double)(nt - 1) * stp - et;
     if (t < ot) t = ot; else if (t > ht) t = ht;
-    rt = div_c(t - ot, stp, fi[3]);
+    rt = (t - ot) / stp;
   } else {
-    rt = div_c(t - ot, stp, fi[3]);
+    rt = (t - ot) / stp;
     if (rt < 0.0 || rt >= (double)nt - 1.0) return EXC_PH_OUTSIDE_GRID;
   }
   if (!isfinite(rt)) return EXC_PH_NONFINITE;

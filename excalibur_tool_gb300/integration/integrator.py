@@ -95,8 +95,8 @@ class Integrator:
         if stop_mode not in self.STOP_MODES:
             raise ValueError(f"stop_mode must be one of {self.STOP_MODES}")
         max_steps = int(stop_value) if stop_mode == "steps" else 2 ** 62
-        a_stop = None
-        stop_box = None
+        a_stop = kw.pop("a_stop", None)
+        stop_box = kw.pop("stop_box", None)
         if stop_mode == "a":
             a_stop = float(stop_value)
         elif stop_mode == "box":

@@ -89,8 +89,11 @@ def test_flrw_rhs_matches_reference(cuda, variant, cosmo, analytical, precision)
         # the analytic adot uses x**3 (libm pow in the reference): <= 1 ulp in rare cases
         assert rel_err(out, want).max() <= (0.0 if cosmo != "table" else 4.5e-16)
     else:
+        # reciprocal constants + FMA: ulp-level; the finite-difference adot
+        # (a(eta+h) - a(eta-h)) / 2h with h = 1e-6 eta amplifies a's ulps by ~1e6
         scale = np.abs(want).max(axis=0, keepdims=True)
-        assert (np.abs(out - want) / np.maximum(scale, 1e-300)).max() <= 1e-13
+        tol = 1e-10 if cosmo == "table_fd" else 1e-13
+        assert (np.abs(out - want) / np.maximum(scale, 1e-300)).max() <= tol
 
 
 @pytest.mark.parametrize("variant,analytical,free", [("analytical_free", True, True),
