@@ -1,0 +1,77 @@
+"""The C ABI: the built library exports every entry point the header declares,
+and the ctypes mirrors of the structs have the C layout (no GPU needed)."""
+import ctypes as C
+import os
+import re
+import subprocess
+import tempfile
+
+import pytest
+
+from conftest import ROOT
+from excalibur_tool_gb300 import _native as N
+
+HEADER = os.path.join(ROOT, "include", "excalibur_gb300.h")
+
+
+def declared_functions():
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(exc_[a-z0-9_]+)\s*\(", text)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    if not os.path.exists(N.LIB_PATH):
+        from excalibur_tool_gb300 import build
+
+        build.build()
+    return C.CDLL(N.LIB_PATH)
+
+
+def test_every_declared_symbol_is_exported(lib):
+    names = declared_functions()
+    assert len(names) >= 10
+    for name in names:
+        assert hasattr(lib, name), name
+
+
+def test_version_and_errors_without_a_device(lib):
+    lib.exc_abi_version.restype = C.c_int
+    assert lib.exc_abi_version() == N.EXC_ABI_VERSION
+    lib.exc_strerror.restype = C.c_char_p
+    assert lib.exc_strerror(N.EXC_ERR_INVALID) == b"invalid argument"
+
+
+def test_invalid_arguments_rejected_before_any_launch(lib):
+    L = N.load()
+    m = N.ExcMetric()
+    m.kind = 99
+    a = N.ExcTraceArgs()
+    rc = L.exc_trace(C.byref(m), C.byref(a), None)
+    assert rc == N.EXC_ERR_INVALID
+    assert b"metric kind" in L.exc_last_error()
+    assert L.exc_trace(None, C.byref(a), None) == N.EXC_ERR_INVALID
+
+
+def test_struct_layout_matches_c():
+    src = r'''
+#include <stdio.h>
+#include <stddef.h>
+#include "excalibur_gb300.h"
+int main(void) {
+  printf("%zu %zu %zu %zu %zu %zu %zu\n", sizeof(ExcField), sizeof(ExcMetric), sizeof(ExcTraceArgs),
+         offsetof(ExcMetric, fields), offsetof(ExcTraceArgs, dt), offsetof(ExcTraceArgs, queue),
+         offsetof(ExcTraceArgs, deadline_cycles));
+  return 0;
+}
+'''
+    with tempfile.TemporaryDirectory() as d:
+        c = os.path.join(d, "sz.c")
+        open(c, "w").write(src)
+        exe = os.path.join(d, "sz")
+        subprocess.run(["gcc", "-I", os.path.dirname(HEADER), c, "-o", exe], check=True)
+        got = [int(v) for v in subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split()]
+    want = [C.sizeof(N.ExcField), C.sizeof(N.ExcMetric), C.sizeof(N.ExcTraceArgs), N.ExcMetric.fields.offset,
+            N.ExcTraceArgs.dt.offset, N.ExcTraceArgs.queue.offset, N.ExcTraceArgs.deadline_cycles.offset]
+    assert got == want

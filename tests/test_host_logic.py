@@ -1,0 +1,96 @@
+"""Host-side logic that needs no GPU: configuration validation, generators'
+direction math, the cosmology table build, observables post-processing."""
+import numpy as np
+import pytest
+
+from conftest import golden
+from excalibur_tool_gb300.trace import TraceConfig
+
+
+def test_trace_config_validation():
+    TraceConfig().validate()
+    with pytest.raises(ValueError):
+        TraceConfig(stepper="euler").validate()
+    with pytest.raises(ValueError):
+        TraceConfig(record_every=-1).validate()
+    with pytest.raises(ValueError):
+        TraceConfig(dt=float("nan")).validate()
+    with pytest.raises(ValueError):
+        TraceConfig(precision="fp16").validate()
+
+
+def test_lcdm_table_matches_reference():
+    from excalibur_tool_gb300.core.cosmology import LCDM_Cosmology
+
+    cz = golden("cosmology.npz")
+    lc = LCDM_Cosmology(70, 0.3, 0.0, 0.7)
+    assert lc.eta_min == float(cz["eta_min"])
+    assert lc.eta_step == float(cz["eta_step"])
+    assert np.array_equal(lc.a_grid, cz["a_grid"])
+    assert lc._eta_at_a1 == float(cz["eta_at_a1"])
+
+
+def test_rotation_matches_reference():
+    from excalibur_tool_gb300.photon.photons import rotate_to_direction
+
+    g = golden("generators.npz")
+    for v, t, want in zip(g["rot_vecs"], g["rot_targets"], g["rot_out"]):
+        got = rotate_to_direction(v, t)[0]
+        assert np.allclose(got, want, rtol=0, atol=1e-15 * max(1.0, np.abs(want).max()))
+
+
+def test_cosmology_resolution_rejects_foreign_callables():
+    from excalibur_tool_gb300.core.cosmology import StaticCosmology, resolve_cosmology
+
+    s = StaticCosmology()
+    assert resolve_cosmology(s.a_of_eta, s.adot_of_eta)[1] == 0
+    with pytest.raises(NotImplementedError):
+        resolve_cosmology(lambda e: 1.0, None)
+
+
+def test_redshift_calculator_matches_reference():
+    from excalibur_tool_gb300.observables.redshift import RedshiftCalculator
+
+    g = golden("observables.npz")
+    r = RedshiftCalculator(g["traj"]).compute_all_components()
+    got = np.array([r["z_H"], r["z_SW"], r["z_ISW"], r["z_D"], r["z_total"], r["z_total_exact"]])
+    assert np.allclose(got, g["redshift"], rtol=1e-14, atol=0)
+
+
+def test_observables_from_accumulators():
+    from excalibur_tool_gb300 import _native as N
+    from excalibur_tool_gb300.observables import lensing as L
+
+    obs = np.full((2, N.OBS_N), np.nan)
+    i = {n: k for k, n in enumerate(N.OBS_COLS)}
+    obs[:, i["a_obs"]] = [1.0, 1.0]
+    obs[:, i["a_em"]] = [0.5, 0.8]
+    obs[:, i["phi_obs"]] = [0.0, 1e11]
+    obs[:, i["phi_em"]] = [0.0, 0.0]
+    obs[:, i["isw_int"]] = [0.0, 0.0]
+    obs[:, [i["v0x"], i["v0y"], i["v0z"]]] = [[1, 0, 0], [1, 0, 0]]
+    obs[:, [i["v1x"], i["v1y"], i["v1z"]]] = [[1, 1e-6, 0], [0, 1, 0]]
+    z = L.redshift_components(obs)
+    assert np.allclose(z["z_H"], [1.0, 0.25])
+    assert np.isclose(z["z_SW"][1], 1e11 / 299792458.0 ** 2)
+    a = L.deflection_angle(obs)
+    assert np.isclose(a[0], 1e-6, rtol=1e-9) and np.isclose(a[1], np.pi / 2)
+    # the naive arccos loses most digits at 1e-6; the stable form keeps them
+    assert abs(L.deflection_angle_naive(obs)[0] - 1e-6) > abs(a[0] - 1e-6)
+
+
+def test_integrator_config_mapping():
+    from excalibur_tool_gb300.integration.integrator import Integrator
+
+    class M:
+        grid = None
+
+    it = Integrator(M(), dt=2.0, integrator="rk4", dt_min=1.0, dt_max=3.0)
+    cfg = it.config("steps", 17)
+    assert cfg.max_steps == 17 and cfg.stepper == "rk4" and cfg.stop_box is None
+    cfg = it.config("a", 0.5)
+    assert cfg.a_stop == 0.5
+    with pytest.raises(NotImplementedError):
+        it.config("redshift", 1.0)
+    with pytest.raises(ValueError):
+        Integrator(M(), integrator="euler")
