@@ -90,6 +90,7 @@ EXPORTS = {
                                 C.c_int64, C.c_void_p]),
     "exc_null_error": (C.c_int, [C.POINTER(ExcMetric), C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                  C.c_int64, C.c_void_p]),
+    "exc_trace_noalloc": (C.c_int, [C.POINTER(ExcMetric), C.POINTER(ExcTraceArgs), C.c_void_p]),
 }
 
 _lib = None

@@ -25,6 +25,7 @@ UNITS = {
     **{f"exc_fast_{s}.cu": ["--fmad=true"] for s in ("rk4", "rk45", "lf4", "aux")},
     "exc_mixed.cu": ["--fmad=true"],
     "exc_capi.cu": [],
+    "exc_noalloc.cu": [],
 }
 
 

@@ -107,6 +107,11 @@ int check_fidx(const ExcMetric* m, const int32_t* fidx) {
 
 }  // namespace
 
+namespace exc {
+// Lets the other boundary unit (exc_noalloc.cu) report through exc_last_error().
+void set_last_error(const char* msg) { snprintf(g_err, sizeof(g_err), "%s", msg); }
+}  // namespace exc
+
 extern "C" {
 
 int exc_abi_version(void) { return EXC_ABI_VERSION; }

@@ -202,6 +202,24 @@ int exc_null_init(const ExcMetric* metric, double* state /* [n][8], u^0 written 
 int exc_null_error(const ExcMetric* metric, const double* state, double* rel_err,
                    int32_t* status, const int32_t* field_index, int64_t n, void* stream);
 
+/* ---- no-allocation variant ----------------------------------------------
+ * No counterpart in the reference. exc_trace_noalloc runs exc_trace with its
+ * work-queue scratch taken from a fixed array inside the library instead of
+ * ExcTraceArgs.queue (which must be NULL), for callers that cannot allocate
+ * device memory themselves -- e.g. an application that owns every device buffer
+ * and forbids allocation in its processing loop, or a latency-bound loop that
+ * cannot afford the implicit device synchronisation of cudaMalloc/cudaFree.
+ * Inputs and outputs are still the caller's. Limits: the array is
+ * EXC_NOALLOC_SCRATCH_BYTES per GPU, held until the process exits; a launch
+ * uses 8 bytes of it (the queue head), on devices 0..EXC_NOALLOC_MAX_DEVICES-1.
+ * The first call on a device looks up the array's address (with that device
+ * current); make that first call before any stream capture. All calls share
+ * the one array, so calls that overlap on the GPU (e.g. concurrent streams)
+ * race on the queue: serialise them. Nothing here calls cudaMalloc/cudaFree. */
+#define EXC_NOALLOC_SCRATCH_BYTES 256
+#define EXC_NOALLOC_MAX_DEVICES 64
+int exc_trace_noalloc(const ExcMetric* metric, const ExcTraceArgs* args, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
