@@ -21,20 +21,20 @@ EXC_SUCCESS, EXC_ERR_INVALID, EXC_ERR_CUDA, EXC_ERR_UNSUPPORTED, EXC_ERR_NO_DEVI
 
 # per-photon status
 PH_STEPS, PH_LEFT_BOX, PH_A_STOP, PH_MAX_ITER, PH_OUTSIDE_GRID, PH_HORIZON, PH_NONFINITE, \
-    PH_TIMED_OUT, PH_ABORTED, PH_NOT_RUN, PH_BAD_FIELD = range(11)
+    PH_TIMED_OUT, PH_ABORTED, PH_NOT_RUN, PH_BAD_FIELD, PH_RETRACE = range(12)
 STATUS_NAMES = {PH_STEPS: "steps", PH_LEFT_BOX: "left_box", PH_A_STOP: "a_stop",
                 PH_MAX_ITER: "max_iter", PH_OUTSIDE_GRID: "outside_grid", PH_HORIZON: "horizon",
                 PH_NONFINITE: "nonfinite", PH_TIMED_OUT: "timed_out", PH_ABORTED: "aborted",
-                PH_NOT_RUN: "not_run", PH_BAD_FIELD: "bad_field"}
+                PH_NOT_RUN: "not_run", PH_BAD_FIELD: "bad_field", PH_RETRACE: "retrace"}
 FAILED_STATUSES = (PH_OUTSIDE_GRID, PH_HORIZON, PH_NONFINITE, PH_TIMED_OUT, PH_ABORTED, PH_NOT_RUN, PH_BAD_FIELD)
 
 METRIC_FLRW, METRIC_SCHWARZSCHILD = 1, 2
 COSMO_STATIC, COSMO_TABLE, COSMO_TABLE_FD = 0, 1, 2
 BOUNDARY = {"periodic": 0, "clamp": 1, "error": 2}
-DTYPE_F64, DTYPE_F32 = 0, 1
+DTYPE_F64, DTYPE_F32, DTYPE_F32X2 = 0, 1, 2
 STEPPER = {"rk4": 0, "rk45": 1, "leapfrog4": 2}
 TABLEAU = {"reference": 0, "fehlberg": 1}
-PRECISION = {"fp64": 0, "fp64_fast": 1, "mixed": 2}
+PRECISION = {"fp64": 0, "fp64_fast": 1, "mixed": 2, "mixed_raw": 3}
 STOP_BOX, STOP_A = 1, 2
 OBS_ENDPOINTS, OBS_PATH, OBS_ISW = 1, 2, 4
 OBS_COLS = ["a_obs", "a_em", "phi_obs", "phi_em", "isw_int", "path", "chord", "excess",

@@ -47,7 +47,7 @@ int sm_count_current() {
 int check_field(const ExcField& f, int idx) {
   if (!f.data) return fail(EXC_ERR_INVALID, "field %d: data is NULL", idx);
   if (f.ndim != 3 && f.ndim != 4) return fail(EXC_ERR_INVALID, "field %d: ndim must be 3 or 4", idx);
-  if (f.dtype != EXC_DTYPE_F64 && f.dtype != EXC_DTYPE_F32)
+  if (f.dtype != EXC_DTYPE_F64 && f.dtype != EXC_DTYPE_F32 && f.dtype != EXC_DTYPE_F32X2)
     return fail(EXC_ERR_INVALID, "field %d: unknown dtype %d", idx, f.dtype);
   if (f.boundary < EXC_BOUNDARY_PERIODIC || f.boundary > EXC_BOUNDARY_ERROR)
     return fail(EXC_ERR_INVALID, "field %d: unknown boundary %d", idx, f.boundary);
@@ -99,6 +99,14 @@ int build_dev_metric(const ExcMetric* m, exc::DevMetric& D) {
   return 0;
 }
 
+// Split float32x2 grids are read by the mixed-precision tracer alone; every
+// FP64 evaluator rejects them (all fields of a call share one dtype).
+int reject_split(const ExcMetric* m) {
+  if (m->kind == EXC_METRIC_FLRW && m->fields[0].dtype == EXC_DTYPE_F32X2)
+    return fail(EXC_ERR_UNSUPPORTED, "split float32x2 grids are read by the mixed-precision tracer only");
+  return 0;
+}
+
 int check_fidx(const ExcMetric* m, const int32_t* fidx) {
   if (fidx && m->kind != EXC_METRIC_FLRW)
     return fail(EXC_ERR_INVALID, "field_index given for a metric without fields");
@@ -143,8 +151,14 @@ int exc_trace(const ExcMetric* metric, const ExcTraceArgs* a, void* stream) {
     return fail(EXC_ERR_INVALID, "unknown stepper %d", a->stepper);
   if (a->tableau != EXC_TABLEAU_REFERENCE && a->tableau != EXC_TABLEAU_FEHLBERG)
     return fail(EXC_ERR_INVALID, "unknown tableau %d", a->tableau);
-  if (a->precision < EXC_PREC_FP64_EXACT || a->precision > EXC_PREC_MIXED)
+  if (a->precision < EXC_PREC_FP64_EXACT || a->precision > EXC_PREC_MIXED_RAW)
     return fail(EXC_ERR_INVALID, "unknown precision %d", a->precision);
+  const bool mixed = a->precision == EXC_PREC_MIXED || a->precision == EXC_PREC_MIXED_RAW;
+  if (!mixed && (e = reject_split(metric))) return e;
+  if (mixed) {
+    const int me = exc_mixed::check(D, *a);
+    if (me) return fail(EXC_ERR_UNSUPPORTED, "%s", exc_mixed::why(me));
+  }
   if (a->max_iter < 0 || a->max_steps < 0) return fail(EXC_ERR_INVALID, "max_iter/max_steps must be >= 0");
   if (!std::isfinite(a->dt)) return fail(EXC_ERR_INVALID, "dt must be finite");
   if (a->record_every < 0) return fail(EXC_ERR_INVALID, "record_every must be >= 0");
@@ -176,9 +190,20 @@ int exc_trace(const ExcMetric* metric, const ExcTraceArgs* a, void* stream) {
   else if (a->precision == EXC_PREC_FP64_FAST)
     ce = exc_fast::trace(D, *a, block, a->blocks_per_sm, sms, s);
   else {
-    int me = exc_mixed::check(D, *a);
-    if (me) return fail(EXC_ERR_UNSUPPORTED, "%s", exc_mixed::why(me));
     ce = exc_mixed::trace(D, *a, block, a->blocks_per_sm, sms, s);
+    if (ce != cudaSuccess) return cuda_fail(ce, "mixed trace launch");
+    if (a->precision == EXC_PREC_MIXED) {
+      // second launch on the same stream: the parity tracer takes the rays the
+      // mixed one handed back (status EXC_PH_RETRACE, state untouched)
+      if (a->queue) {
+        ce = cudaMemsetAsync(a->queue, 0, 2 * sizeof(uint32_t), s);
+        if (ce != cudaSuccess) return cuda_fail(ce, "queue reset");
+      }
+      D.retrace_only = 1;
+      ce = exc_exact::trace(D, *a, block, a->blocks_per_sm, sms, s);
+      if (ce != cudaSuccess) return cuda_fail(ce, "re-trace launch");
+    }
+    return EXC_SUCCESS;
   }
   if (ce != cudaSuccess) return cuda_fail(ce, "trace launch");
   return EXC_SUCCESS;
@@ -193,6 +218,7 @@ int exc_geodesic_rhs(const ExcMetric* metric, int32_t precision, const double* s
   if (n < 0) return fail(EXC_ERR_INVALID, "n < 0");
   if (n > 0 && (!state || !out)) return fail(EXC_ERR_INVALID, "state/out are required");
   if ((e = check_fidx(metric, field_index))) return e;
+  if ((e = reject_split(metric))) return e;
   cudaStream_t s = (cudaStream_t)stream;
   cudaError_t ce;
   if (precision == EXC_PREC_FP64_EXACT) ce = exc_exact::rhs(D, state, out, status, field_index, n, s);
@@ -208,6 +234,8 @@ int exc_interp(const ExcField* field, const double* points, double* out, int32_t
   if (!field) return fail(EXC_ERR_INVALID, "field is NULL");
   int e = check_field(*field, 0);
   if (e) return e;
+  if (field->dtype == EXC_DTYPE_F32X2)
+    return fail(EXC_ERR_UNSUPPORTED, "exc_interp reads float64 or float32 grids");
   if (n < 0) return fail(EXC_ERR_INVALID, "n < 0");
   if (n > 0 && (!points || !out)) return fail(EXC_ERR_INVALID, "points/out are required");
   cudaError_t ce = exc_exact::interp(*field, points, out, status, n, (cudaStream_t)stream);
@@ -241,6 +269,7 @@ int exc_metric_tensor(const ExcMetric* metric, const double* x, double* g_diag, 
   if (n < 0) return fail(EXC_ERR_INVALID, "n < 0");
   if (n > 0 && (!x || !g_diag)) return fail(EXC_ERR_INVALID, "x/g_diag are required");
   if ((e = check_fidx(metric, field_index))) return e;
+  if ((e = reject_split(metric))) return e;
   cudaError_t ce = exc_exact::metric(D, x, g_diag, status, field_index, n, (cudaStream_t)stream);
   if (ce != cudaSuccess) return cuda_fail(ce, "metric launch");
   return EXC_SUCCESS;
@@ -255,6 +284,7 @@ int exc_null_init(const ExcMetric* metric, double* state, double sign, int32_t* 
   if (n < 0) return fail(EXC_ERR_INVALID, "n < 0");
   if (n > 0 && !state) return fail(EXC_ERR_INVALID, "state is required");
   if ((e = check_fidx(metric, field_index))) return e;
+  if ((e = reject_split(metric))) return e;
   cudaError_t ce = exc_exact::null_init(D, state, sign, status, field_index, n, (cudaStream_t)stream);
   if (ce != cudaSuccess) return cuda_fail(ce, "null_init launch");
   return EXC_SUCCESS;
@@ -269,6 +299,7 @@ int exc_null_error(const ExcMetric* metric, const double* state, double* rel_err
   if (n < 0) return fail(EXC_ERR_INVALID, "n < 0");
   if (n > 0 && (!state || !rel_err)) return fail(EXC_ERR_INVALID, "state/rel_err are required");
   if ((e = check_fidx(metric, field_index))) return e;
+  if ((e = reject_split(metric))) return e;
   cudaError_t ce = exc_exact::null_error(D, state, rel_err, status, field_index, n, (cudaStream_t)stream);
   if (ce != cudaSuccess) return cuda_fail(ce, "null_error launch");
   return EXC_SUCCESS;

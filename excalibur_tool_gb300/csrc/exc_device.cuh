@@ -77,6 +77,12 @@ template <class FT>
 __device__ __forceinline__ double ldf(const FT* p, int64_t i) {
   return (double)__ldg(p + i);
 }
+// split grid (EXC_DTYPE_F32X2): interleaved (hi, lo) pairs; hi + lo is exact in FP64
+template <>
+__device__ __forceinline__ double ldf<float2>(const float2* p, int64_t i) {
+  const float2 v = __ldg(p + i);
+  return (double)v.x + (double)v.y;
+}
 
 struct InterpOut {
   double val, gx, gy, gz, dtd;

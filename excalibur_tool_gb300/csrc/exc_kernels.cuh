@@ -458,6 +458,15 @@ __device__ __forceinline__ bool photon_iterate(Tracer<MK, FT>& T, const ExcTrace
   return stop;
 }
 
+// Next photon to trace; in a re-trace pass only those the mixed tracer handed back.
+__device__ __forceinline__ int64_t next_work(const DevMetric& D, const ExcTraceArgs& A, int64_t& static_next,
+                                             int64_t stride) {
+  int64_t p = next_photon(A, static_next, stride);
+  if (D.retrace_only)
+    while (p < A.n_photons && A.status[p] != EXC_PH_RETRACE) p = next_photon(A, static_next, stride);
+  return p;
+}
+
 template <int MK, class FT, int STEPPER, bool REC>
 __global__ void __launch_bounds__(128) trace_kernel(const DevMetric D, const ExcTraceArgs A) {
   Tracer<MK, FT> T(D, A);
@@ -465,7 +474,7 @@ __global__ void __launch_bounds__(128) trace_kernel(const DevMetric D, const Exc
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   int64_t static_next = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const long long t0 = clock64();
-  int64_t p = next_photon(A, static_next, stride);
+  int64_t p = next_work(D, A, static_next, stride);
   bool active = p < A.n_photons;
   if (active) photon_begin<MK, FT, REC>(T, A, P, p);
   while (active) {
@@ -478,7 +487,7 @@ __global__ void __launch_bounds__(128) trace_kernel(const DevMetric D, const Exc
       photon_finish<MK, FT, REC>(T, A, P);
       const bool stop_all = (P.status == EXC_PH_ABORTED || P.status == EXC_PH_TIMED_OUT);
       if (stop_all) break;
-      p = next_photon(A, static_next, stride);
+      p = next_work(D, A, static_next, stride);
       active = p < A.n_photons;
       if (active) photon_begin<MK, FT, REC>(T, A, P, p);
     }
@@ -521,6 +530,13 @@ cudaError_t launch_trace_stepper(const DevMetric& D, const ExcTraceArgs& A, Laun
   if (D.m.kind == EXC_METRIC_SCHWARZSCHILD)
     return launch_trace_r<EXC_METRIC_SCHWARZSCHILD, double, STEPPER>(D, A, lc, s);
   if (D.m.fields[0].dtype == EXC_DTYPE_F32) return launch_trace_r<EXC_METRIC_FLRW, float, STEPPER>(D, A, lc, s);
+  if (D.m.fields[0].dtype == EXC_DTYPE_F32X2) {
+    // split grids reach the FP64 tracer only as the mixed tracer's RK4 re-trace pass
+    if constexpr (STEPPER == EXC_STEPPER_RK4 && !EXC_FAST) {
+      if (!A.records) return launch_trace_t<EXC_METRIC_FLRW, float2, STEPPER, false>(D, A, lc, s);
+    }
+    return cudaErrorInvalidValue;
+  }
   return launch_trace_r<EXC_METRIC_FLRW, double, STEPPER>(D, A, lc, s);
 }
 

@@ -48,6 +48,8 @@ class Grid:
         data = self.fields[name]
         if dtype is None:
             dtype = data.dtype if isinstance(data, torch.Tensor) else torch.from_numpy(np.asarray(data[:0])).dtype
+        elif not isinstance(dtype, torch.dtype):          # numpy dtype or "float32"-style name
+            dtype = torch.from_numpy(np.zeros(0, dtype=np.dtype(dtype))).dtype
         key = (name, str(torch.device(device)), dtype)
         t = self._device.get(key)
         if t is None:
@@ -55,6 +57,21 @@ class Grid:
                 t = data.to(device=device, dtype=dtype).contiguous()
             else:
                 t = torch.as_tensor(np.ascontiguousarray(data)).to(device=device, dtype=dtype).contiguous()
+            self._device[key] = t
+        return t
+
+    def device_field_split(self, name, device):
+        """A float64 field as interleaved float32 pairs (hi, lo) per node, hi =
+        float32(x) and lo = float32(x - hi), flattened, cached on `device`."""
+        import torch
+
+        key = (name, str(torch.device(device)), "f32x2")
+        t = self._device.get(key)
+        if t is None:
+            d = self.device_field(name, device, torch.float64)
+            hi = d.to(torch.float32)
+            lo = (d - hi.to(torch.float64)).to(torch.float32)
+            t = torch.stack([hi.reshape(-1), lo.reshape(-1)], dim=1).reshape(-1).contiguous()
             self._device[key] = t
         return t
 

@@ -34,11 +34,18 @@ class InterpolatorFast:
                 raise ValueError("3D grid requires origin/spacing/shape of length >= 3")
 
     # ---- descriptor used by the tracer and exc_interp --------------------
-    def field_struct(self, field, device):
+    def field_struct(self, field, device, split=False):
+        """ExcField for `field` on `device`. With `split`, a float64 grid is passed
+        as two float32 planes (hi, lo) for the mixed-precision tracer."""
         from ..trace import field_struct
 
         t = self.grid.device_field(field, device, self.field_dtype)
         nd = 4 if self.is_4d else 3
+        if split and str(t.dtype) == "torch.float64":
+            planes = self.grid.device_field_split(field, device)
+            f = field_struct(planes, self.shape[:nd], self.spacing[:nd], self.origin[:nd], self.boundary,
+                             split=True)
+            return f, planes
         return field_struct(t, self.shape[:nd], self.spacing[:nd], self.origin[:nd], self.boundary), t
 
     # ---- batched evaluation ----------------------------------------------

@@ -20,5 +20,5 @@ class Metric(ABC):
         """Quantities recorded with each trajectory row."""
 
     @abstractmethod
-    def descriptor(self, device):
+    def descriptor(self, device, split=False):
         """The C ABI ExcMetric for this spacetime (see trace.MetricDescriptor)."""

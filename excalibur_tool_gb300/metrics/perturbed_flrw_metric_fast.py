@@ -37,11 +37,13 @@ class PerturbedFLRWMetricFast(Metric):
         self._desc = {}
 
     # ---- device descriptor ----------------------------------------------
-    def descriptor(self, device):
+    def descriptor(self, device, split=False):
+        """ExcMetric for `device`; `split` passes float64 grids as float32 hi/lo planes
+        (what the mixed-precision tracer reads)."""
         import torch
         from ..trace import MetricDescriptor, base_metric_struct
 
-        key = str(torch.device(device))
+        key = (str(torch.device(device)), bool(split))
         d = self._desc.get(key)
         if d is not None:
             return d
@@ -63,7 +65,7 @@ class PerturbedFLRWMetricFast(Metric):
         if len(interps) > N.EXC_MAX_FIELDS:
             raise ValueError(f"at most {N.EXC_MAX_FIELDS} potential fields per launch")
         for i, ip in enumerate(interps):
-            f, t = ip.field_struct(self.field, device)
+            f, t = ip.field_struct(self.field, device, split=split)
             m.fields[i] = f
             keep.append(t)
         m.n_fields = len(interps)

@@ -34,7 +34,7 @@ class SchwarzschildMetricFast(Metric):
         self.internal_coords = "spherical"
         self._desc = {}
 
-    def descriptor(self, device):
+    def descriptor(self, device, split=False):
         import torch
         from ..trace import MetricDescriptor, base_metric_struct
 

@@ -39,7 +39,7 @@ def gaussian_random_field(n, box, seed, rms=1e-5, spectral_index=-3.0, dtype=np.
     amp = np.zeros_like(k2)
     nz = k2 > 0
     amp[nz] = k2[nz] ** (spectral_index / 4.0)      # sqrt(P) = |k|^(index/2)
-    field = np.fft.irfftn(wk * amp, s=(n, n, n))
+    field = np.fft.irfftn(wk * amp, s=(n, n, n), axes=(0, 1, 2))
     field *= rms / field.std()
     return field.astype(dtype)
 

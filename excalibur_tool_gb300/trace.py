@@ -29,7 +29,7 @@ class TraceConfig:
 
     stepper: str = "rk45"            # "rk4" | "rk45" | "leapfrog4"
     tableau: str = "reference"       # RK45 weights: "reference" (665/1287) | "fehlberg"
-    precision: str = "fp64"          # "fp64" (reference order) | "fp64_fast" | "mixed"
+    precision: str = "fp64"          # "fp64" (reference order) | "fp64_fast" | "mixed" | "mixed_raw"
     dt: float = 1e-3
     dt_min: float = 1e14
     dt_max: float = 1e17
@@ -104,11 +104,15 @@ def base_metric_struct(kind: int) -> N.ExcMetric:
     return m
 
 
-def field_struct(data, shape, spacing, origin, boundary: str) -> N.ExcField:
+def field_struct(data, shape, spacing, origin, boundary: str, split: bool = False) -> N.ExcField:
     import torch
 
     f = N.ExcField()
-    if data.dtype == torch.float64:
+    if split:
+        if data.dtype != torch.float32:
+            raise TypeError("split planes must be float32")
+        f.dtype = N.DTYPE_F32X2
+    elif data.dtype == torch.float64:
         f.dtype = N.DTYPE_F64
     elif data.dtype == torch.float32:
         f.dtype = N.DTYPE_F32
@@ -156,7 +160,7 @@ def trace_batch(metric, states, cfg: TraceConfig, *, field_index=None, dt=None, 
     _check_device_tensor(states, torch.float64, (8,), "states")
     dev = states.device
     n = states.shape[0]
-    desc = metric.descriptor(dev)
+    desc = metric.descriptor(dev, split=cfg.precision in ("mixed", "mixed_raw"))
     if out is None:
         st = states.clone()
         status = torch.empty(n, dtype=torch.int32, device=dev)

@@ -63,7 +63,12 @@ enum {
   EXC_PH_TIMED_OUT = 7,      /* device deadline reached */
   EXC_PH_ABORTED = 8,        /* host abort flag seen */
   EXC_PH_NOT_RUN = 9,        /* never dequeued (launch ended early) */
-  EXC_PH_BAD_FIELD = 10      /* field_index outside [0, n_fields) */
+  EXC_PH_BAD_FIELD = 10,     /* field_index outside [0, n_fields) */
+  EXC_PH_RETRACE = 11        /* EXC_PREC_MIXED_RAW only: a stage point or a stop decision came
+                                within the mixed tracer's error window of a discontinuity of the
+                                reference's RHS (a cell face of the base-node gradient, a stop
+                                threshold); the photon's state, dt and outputs are left untouched
+                                for the FP64 tracer (EXC_PREC_MIXED does that re-trace itself) */
 };
 
 /* ---- enums -------------------------------------------------------------- */
@@ -71,13 +76,22 @@ enum { EXC_METRIC_FLRW = 1, EXC_METRIC_SCHWARZSCHILD = 2 };
 enum { EXC_COSMO_STATIC = 0, EXC_COSMO_TABLE = 1, EXC_COSMO_TABLE_FD = 2 };
 enum { EXC_BOUNDARY_PERIODIC = 0, EXC_BOUNDARY_CLAMP = 1, EXC_BOUNDARY_ERROR = 2 };
 enum { EXC_GRAD_BASE_NODE = 0 };                 /* fast interpolators' gradient */
-enum { EXC_DTYPE_F64 = 0, EXC_DTYPE_F32 = 1 };
+/* EXC_DTYPE_F32X2: a float64 grid stored as interleaved float32 pairs, node i
+ * at data[2i] = hi = (float)x_i and data[2i + 1] = lo = (float)(x_i - hi);
+ * read by the mixed-precision tracer, whose FP32 arithmetic then takes grid
+ * differences without cancellation (hi differences are exact), and by its
+ * FP64 re-trace pass as hi + lo (x_i to 2^-48 relative). */
+enum { EXC_DTYPE_F64 = 0, EXC_DTYPE_F32 = 1, EXC_DTYPE_F32X2 = 2 };
 enum { EXC_STEPPER_RK4 = 0, EXC_STEPPER_RK45 = 1, EXC_STEPPER_LEAPFROG4 = 2 };
 enum { EXC_TABLEAU_REFERENCE = 0, EXC_TABLEAU_FEHLBERG = 1 };
-/* EXACT: reference operation order, no FMA contraction (parity path).
- * FAST:  same formulas, FMA contraction, reciprocal constants.
- * MIXED: FP32 RHS + interpolation, FP64 state accumulation and step control. */
-enum { EXC_PREC_FP64_EXACT = 0, EXC_PREC_FP64_FAST = 1, EXC_PREC_MIXED = 2 };
+/* EXACT:     reference operation order, no FMA contraction (parity path).
+ * FAST:      same formulas, FMA contraction, reciprocal constants.
+ * MIXED:     FP32 RHS + interpolation, double-float (hi + lo FP32) state; rays
+ *            that come within the error window of a discontinuity of the
+ *            reference's RHS are re-traced by the EXACT tracer in a second
+ *            launch on the same stream (FLRW, RK4, no records).
+ * MIXED_RAW: the mixed launch alone; such rays end with EXC_PH_RETRACE. */
+enum { EXC_PREC_FP64_EXACT = 0, EXC_PREC_FP64_FAST = 1, EXC_PREC_MIXED = 2, EXC_PREC_MIXED_RAW = 3 };
 
 /* stop_flags bits (the "steps" stop and max_iter always apply) */
 #define EXC_STOP_BOX   1

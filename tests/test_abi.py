@@ -54,6 +54,58 @@ def test_invalid_arguments_rejected_before_any_launch(lib):
     assert L.exc_trace(None, C.byref(a), None) == N.EXC_ERR_INVALID
 
 
+def _split_flrw_metric():
+    m = N.ExcMetric()
+    m.kind = N.METRIC_FLRW
+    m.c, m.c2, m.c4 = 299792458.0, 299792458.0 ** 2, 299792458.0 ** 4
+    m.n_fields = 1
+    f = m.fields[0]
+    f.data = 4096                      # never dereferenced: every case fails validation first
+    f.dtype = N.DTYPE_F32X2
+    f.ndim = 3
+    for d in range(3):
+        f.n[d], f.spacing[d] = 8, 1.0
+    return m
+
+
+def _args(**kw):
+    a = N.ExcTraceArgs()
+    a.n_photons = 1
+    a.state = a.status = 4096
+    a.dt = a.dt_min = a.dt_max = 1.0
+    for k, v in kw.items():
+        setattr(a, k, v)
+    return a
+
+
+def test_split_grids_only_for_the_mixed_tracer(lib):
+    """float32x2 planes are rejected by every FP64 entry point before any device work."""
+    L = N.load()
+    m = _split_flrw_metric()
+    for prec in (N.PRECISION["fp64"], N.PRECISION["fp64_fast"]):
+        assert L.exc_trace(C.byref(m), C.byref(_args(precision=prec)), None) == N.EXC_ERR_UNSUPPORTED
+        assert b"mixed-precision" in L.exc_last_error()
+    x = C.c_void_p(4096)
+    assert L.exc_geodesic_rhs(C.byref(m), 0, x, x, None, None, 1, None) == N.EXC_ERR_UNSUPPORTED
+    assert L.exc_metric_tensor(C.byref(m), x, x, None, None, 1, None) == N.EXC_ERR_UNSUPPORTED
+    assert L.exc_null_init(C.byref(m), x, C.c_double(-1.0), None, None, 1, None) == N.EXC_ERR_UNSUPPORTED
+    assert L.exc_null_error(C.byref(m), x, x, None, None, 1, None) == N.EXC_ERR_UNSUPPORTED
+
+
+@pytest.mark.parametrize("kw,msg", [
+    (dict(stepper=N.STEPPER["rk45"]), b"RK4 stepper only"),
+    (dict(records=4096, n_records=4096, max_records=2, record_cols=14), b"record"),
+    (dict(renormalize_every=3), b"renormalise"),
+    (dict(obs=4096, obs_flags=N.OBS_ISW), b"ISW"),
+])
+def test_mixed_rejects_what_it_does_not_implement(lib, kw, msg):
+    L = N.load()
+    m = _split_flrw_metric()
+    a = _args(precision=N.PRECISION["mixed"], **kw)
+    assert L.exc_trace(C.byref(m), C.byref(a), None) == N.EXC_ERR_UNSUPPORTED
+    assert msg in L.exc_last_error()
+
+
 def test_struct_layout_matches_c():
     src = r'''
 #include <stdio.h>

@@ -1,0 +1,145 @@
+"""Mixed-precision tracer (FP32 right-hand side, double-float state) against the
+FP64 oracle on the 1000 Mpc lens-plus-random-field patch.
+
+The mixed tracer is not bit-faithful to the reference; it is held to error
+bounds on the observables that come out of a trace (stated here and in the
+assertions):
+
+* redshift:            |dz| <= 1e-9
+* time-delay excess:   relative <= 1e-6
+* deflection angle:    |d alpha| <= 1e-5 * alpha + 5e-11 rad
+* accepted steps and final status: identical (same box-exit step)
+
+Rays whose mixed trajectory comes within its error window of a cell face of
+the reference's base-node gradient (or of a stop threshold) are re-traced by
+the FP64 parity tracer inside the same `exc_trace` call; `mixed_raw` exposes
+the mixed launch alone, with those rays marked EXC_PH_RETRACE.
+"""
+import dataclasses
+import os
+
+import numpy as np
+import pytest
+
+from helpers import gpu_trace, rel_err
+from test_gpu_parity import _cfg2_like
+from excalibur_tool_gb300 import _native as N
+from excalibur_tool_gb300.observables import lensing as L
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+DZ_MAX = 1e-9
+TAU_REL_MAX = 1e-6
+DEFL_REL, DEFL_ABS = 1e-5, 5e-11
+
+
+def _check_observables(r, o):
+    assert np.array_equal(r["status"], o.status)
+    assert np.array_equal(r["n_steps"], o.n_steps)
+    z_gpu, z_ref = L.redshift_total(r["obs"]), L.redshift_total(o.obs)
+    assert np.abs(z_gpu - z_ref).max() <= DZ_MAX
+    t_gpu, t_ref = L.time_delay_excess(r["obs"]), L.time_delay_excess(o.obs)
+    assert (np.abs(t_gpu - t_ref) / np.abs(t_ref)).max() <= TAU_REL_MAX
+    a_gpu, a_ref = L.deflection_angle(r["obs"]), L.deflection_angle(o.obs)
+    assert (np.abs(a_gpu - a_ref) <= DEFL_REL * np.abs(a_ref) + DEFL_ABS).all()
+    # trajectory end point and path length: FP32-RHS-limited, far below a grid cell
+    assert rel_err(r["state"][:, :4], o.state[:, :4]).max() <= 1e-8
+    i = N.OBS_COLS.index("path")
+    assert rel_err(r["obs"][:, i], o.obs[:, i]).max() <= 1e-7
+
+
+@pytest.mark.parametrize("n_grid,side", [(128, 24), (32, 16)])
+def test_mixed_matches_fp64_oracle(cuda, n_grid, side):
+    spec, st, cfg = _cfg2_like(n_grid, side)
+    cfg = dataclasses.replace(cfg, precision="mixed")
+    r = gpu_trace(spec, st, cfg)
+    o = O.trace(spec, st, cfg, threads=8)
+    _check_observables(r, o)
+
+
+@pytest.mark.parametrize("a_stop,max_steps,want", [(0.93, 10000, "A_STOP"), (None, 300, "STEPS")])
+def test_mixed_a_stop_and_step_cap(cuda, a_stop, max_steps, want):
+    """The a(eta) stop and the step cap end photons where the FP64 tracer does."""
+    spec, st, cfg = _cfg2_like(32, 8)
+    cfg = dataclasses.replace(cfg, precision="mixed", a_stop=a_stop, max_steps=max_steps)
+    r = gpu_trace(spec, st, cfg)
+    o = O.trace(spec, st, cfg, threads=8)
+    assert (o.status == getattr(N, "PH_" + want)).all()
+    _check_observables(r, o)
+
+
+def test_mixed_queue_and_static_schedules_agree(cuda):
+    spec, st, cfg = _cfg2_like(32, 12)
+    cfg = dataclasses.replace(cfg, precision="mixed")
+    a = gpu_trace(spec, st, dataclasses.replace(cfg, use_queue=True))
+    b = gpu_trace(spec, st, dataclasses.replace(cfg, use_queue=False))
+    for k in ("state", "status", "n_steps", "obs"):
+        assert np.array_equal(a[k], b[k], equal_nan=True)
+
+
+def test_mixed_float32_grid(cuda):
+    """A float32 grid (one plane) traces against the oracle run on the same rounded grid."""
+    import torch
+    from helpers import gpu_metric
+    from excalibur_tool_gb300.trace import trace_batch
+
+    spec, st, cfg = _cfg2_like(32, 8)
+    spec.fields[0].data = spec.fields[0].data.astype(np.float32).astype(np.float64)
+    cfg = dataclasses.replace(cfg, precision="mixed")
+    m = gpu_metric(spec, field_dtype=np.float32)
+    res = trace_batch(m, torch.as_tensor(st).cuda(), cfg)
+    torch.cuda.synchronize()
+    r = {k: getattr(res, a).cpu().numpy() for k, a in
+         (("state", "state"), ("status", "status"), ("n_steps", "n_steps"), ("obs", "obs"))}
+    o = O.trace(spec, st, cfg, threads=8)
+    _check_observables(r, o)
+
+
+@pytest.fixture(scope="module")
+def patch(cuda):
+    """The 65,536-ray 1000 Mpc lens patch (128^3 float64 grid) and its oracle trace."""
+    from excalibur_tool_gb300 import workloads
+    from oracle.oracle import FieldSpec, Spacetime
+
+    wl = workloads.flrw_patch(128, 256, device=cuda)
+    cz = workloads.lcdm()
+    phi = np.asarray(wl.metric.interp.grid.fields["Phi"])
+    spec = Spacetime(kind="flrw", fields=[FieldSpec(phi, (workloads.BOX / 128,) * 3, (0.0, 0.0, 0.0), "periodic")],
+                     cosmology="table", a_grid=cz.a_grid, eta_min=cz.eta_min, eta_step=cz.eta_step, H0=cz.H0,
+                     omega=(0.3, 0.0, 0.0, 0.7))
+    states = wl.states.cpu().numpy()
+    o = O.trace(spec, states, wl.cfg, threads=os.cpu_count() or 1)
+    return wl, states, o
+
+
+def _run(wl, precision):
+    import torch
+    from excalibur_tool_gb300.trace import trace_batch
+
+    res = trace_batch(wl.metric, wl.states, dataclasses.replace(wl.cfg, precision=precision))
+    torch.cuda.synchronize()
+    return {k: getattr(res, k).cpu().numpy() for k in ("state", "status", "n_steps", "obs")}
+
+
+def test_mixed_full_patch_every_ray_within_bounds(patch):
+    """All 65,536 rays of the lens patch meet the bounds against the FP64 oracle."""
+    wl, states, o = patch
+    _check_observables(_run(wl, "mixed"), o)
+
+
+def test_mixed_raw_hands_back_untouched_rays(patch):
+    """mixed_raw marks the guarded rays and leaves their state as it came in;
+    mixed = mixed_raw elsewhere and = the FP64 parity tracer on those rays."""
+    wl, states, o = patch
+    raw = _run(wl, "mixed_raw")
+    mixed = _run(wl, "mixed")
+    back = raw["status"] == N.PH_RETRACE
+    assert 0 < back.sum() < 0.05 * len(back)          # a small fraction (about 1.5 % here)
+    assert np.array_equal(raw["state"][back], states[back])
+    keep = ~back
+    for k in ("state", "status", "n_steps", "obs"):
+        assert np.array_equal(raw[k][keep], mixed[k][keep], equal_nan=True), k
+    assert not (mixed["status"] == N.PH_RETRACE).any()
+    assert np.array_equal(mixed["n_steps"][back], o.n_steps[back])
+    assert rel_err(mixed["state"][back], o.state[back]).max() <= 1e-12
