@@ -8,6 +8,11 @@ P(k)~k^-3 random field, rms Phi/c^2 = 1e-5) until box exit or a <= 0.5.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
+The line also carries `precision`: the guarded mixed-precision tracer on the
+precision workload (4,194,304 photons, 2048x2048 directions in a 20x20 deg
+patch, Phi on a 512^3 float32 grid, seed 4) against the FP64 tracer on a
+seeded 65,536-ray subset (numpy default_rng(40)).
+
 `--impl reference` times the CPU oracle (the C restatement of the reference's
 integrate_single loop, oracle/exc_oracle.c) on all host threads over the same
 workload instead. Under torchrun (N > 1) each rank traces its own batch (weak
@@ -48,6 +53,8 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-variants", action="store_true")
     p.add_argument("--side", type=int, default=256, help="directions per side (smaller cases for profiling)")
+    p.add_argument("--no-precision", action="store_true", help="skip the 512^3 / 4M-ray precision workload")
+    p.add_argument("--precision-side", type=int, default=2048)
     return p.parse_args()
 
 
@@ -285,6 +292,10 @@ def run_ours(args, rank, world, local):
         line["variants"] = run_variants(args, wl, peaks, dev, stream, value)
     if not args.no_cpu_baseline and world == 1 and rank == 0:
         line["cpu_baseline"] = cpu_baseline(wl, steps_per_batch)
+    if not args.no_precision and world == 1:
+        del wl, metric, states, res
+        torch.cuda.empty_cache()
+        line["precision"] = run_precision(args, dev, stream, flush, value)
     if rank == 0:
         print(json.dumps(line), flush=True)
 
@@ -320,6 +331,22 @@ def run_variants(args, wl, peaks, dev, stream, main_value):
         steps = int(r.n_steps[r.status != N.PH_RETRACE].sum())
         out[prec] = {"photon_steps_per_s": steps / s, "rays_per_s": wl.states.shape[0] / s,
                      f"speedup_vs_{args.precision}": steps / s / main_value}
+        if prec == "mixed":
+            # a stream of batches: each batch's FP64 re-traces overlap the next batches' mixed launches
+            from excalibur_tool_gb300.trace import trace_pipelined
+
+            nb = 8
+            trace_pipelined(wl.metric, [wl.states] * 2, cfg)
+            torch.cuda.synchronize(dev)
+            e0.record(stream)
+            rs = trace_pipelined(wl.metric, [wl.states] * nb, cfg)
+            e1.record(stream)
+            torch.cuda.synchronize(dev)
+            sp = e0.elapsed_time(e1) / 1e3
+            out[prec]["pipelined"] = {"batches": nb, "photon_steps_per_s": nb * steps / sp,
+                                      "rays_per_s": nb * wl.states.shape[0] / sp,
+                                      f"speedup_vs_{args.precision}": nb * steps / sp / main_value,
+                                      "note": "re-trace of batch k on a side stream, overlapping batches k+1.."}
         if prec == "mixed_raw":
             # the mixed launch alone: rays handed back for the FP64 re-trace carry no result
             back = r.status == N.PH_RETRACE
@@ -329,6 +356,74 @@ def run_variants(args, wl, peaks, dev, stream, main_value):
         else:
             out[prec].update(errors_vs(ref, r))
     return out
+
+
+def run_precision(args, dev, stream, flush, fp64_value):
+    """Guarded mixed tracer on the 512^3 float32 / 4M-ray workload; errors against the
+    FP64 parity tracer on a seeded 65,536-ray subset of the same rays."""
+    import dataclasses
+    import torch
+
+    from excalibur_tool_gb300 import _native as N
+    from excalibur_tool_gb300 import workloads
+    from excalibur_tool_gb300.trace import trace_batch
+
+    t0 = time.perf_counter()
+    side = args.precision_side
+    wl = workloads.flrw_patch(512, side, 20.0, seed=4, field_dtype=np.float32, device=dev)
+    build_s = time.perf_counter() - t0
+    n = wl.states.shape[0]
+    cfg = dataclasses.replace(wl.cfg, precision="mixed")
+    r = trace_batch(wl.metric, wl.states, cfg)
+    torch.cuda.synchronize(dev)
+    steps = int(r.n_steps.sum())
+    k = max(2, min(args.steps, 3))
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(k)]
+    for i in range(k):
+        flush.fill_(float(i))
+        evs[i][0].record(stream)
+        r = trace_batch(wl.metric, wl.states, cfg)
+        evs[i][1].record(stream)
+    torch.cuda.synchronize(dev)
+    sec = sum(a.elapsed_time(b) for a, b in evs) / 1e3 / k
+    raw = trace_batch(wl.metric, wl.states, dataclasses.replace(cfg, precision="mixed_raw"))
+    torch.cuda.synchronize(dev)
+    back = float((raw.status == N.PH_RETRACE).float().mean())
+    del raw
+    # FP64 parity tracer on the seeded subset
+    idx = np.sort(np.random.default_rng(40).choice(n, min(65536, n), replace=False))
+    sub = wl.states[torch.as_tensor(idx, device=dev)].contiguous()
+    c64 = dataclasses.replace(wl.cfg, precision="fp64")
+    r64 = trace_batch(wl.metric, sub, c64)
+    torch.cuda.synchronize(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    r64 = trace_batch(wl.metric, sub, c64)
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    s64 = e0.elapsed_time(e1) / 1e3
+    steps64 = int(r64.n_steps.sum())
+
+    class _Sub:
+        pass
+
+    rs = _Sub()
+    ti = torch.as_tensor(idx, device=dev)
+    rs.obs, rs.state, rs.status = r.obs[ti], r.state[ti], r.status[ti]
+    err = errors_vs(r64, rs)
+    err["status_equal"] = bool(torch.equal(rs.status, r64.status))
+    err["steps_equal"] = bool(torch.equal(r.n_steps[ti], r64.n_steps))
+    mixed_ps = steps / sec
+    fp64_ps = steps64 / s64
+    return {"workload": f"flrw_patch_512: {n:,} photons ({side}x{side} directions, 20x20 deg patch), Phi on a "
+                        "512^3 float32 grid (512 MB, Plummer + seeded random field, seed 4), RK4 deta = 0.5 Mpc",
+            "precision": "mixed (FP32 RHS, double-float state, FP64 re-trace of guarded rays)",
+            "photon_steps_per_s": mixed_ps, "rays_per_s": n / sec, "ms_per_batch": sec * 1e3,
+            "timed_batches": k, "retrace_fraction": back,
+            "fp64_subset_photon_steps_per_s": fp64_ps, "speedup_vs_fp64": mixed_ps / fp64_ps,
+            "speedup_vs_fp64_patch_value": mixed_ps / fp64_value,
+            "errors_vs_fp64_on_subset": {**err, "subset": "65,536 rays, numpy default_rng(40)"},
+            "host_field_build_s": build_s}
 
 
 def errors_vs(ref, r, mask=None):

@@ -34,7 +34,7 @@ BOUNDARY = {"periodic": 0, "clamp": 1, "error": 2}
 DTYPE_F64, DTYPE_F32, DTYPE_F32X2 = 0, 1, 2
 STEPPER = {"rk4": 0, "rk45": 1, "leapfrog4": 2}
 TABLEAU = {"reference": 0, "fehlberg": 1}
-PRECISION = {"fp64": 0, "fp64_fast": 1, "mixed": 2, "mixed_raw": 3}
+PRECISION = {"fp64": 0, "fp64_fast": 1, "mixed": 2, "mixed_raw": 3, "retrace": 4}
 STOP_BOX, STOP_A = 1, 2
 OBS_ENDPOINTS, OBS_PATH, OBS_ISW = 1, 2, 4
 OBS_COLS = ["a_obs", "a_em", "phi_obs", "phi_em", "isw_int", "path", "chord", "excess",

@@ -151,9 +151,9 @@ int exc_trace(const ExcMetric* metric, const ExcTraceArgs* a, void* stream) {
     return fail(EXC_ERR_INVALID, "unknown stepper %d", a->stepper);
   if (a->tableau != EXC_TABLEAU_REFERENCE && a->tableau != EXC_TABLEAU_FEHLBERG)
     return fail(EXC_ERR_INVALID, "unknown tableau %d", a->tableau);
-  if (a->precision < EXC_PREC_FP64_EXACT || a->precision > EXC_PREC_MIXED_RAW)
+  if (a->precision < EXC_PREC_FP64_EXACT || a->precision > EXC_PREC_RETRACE)
     return fail(EXC_ERR_INVALID, "unknown precision %d", a->precision);
-  const bool mixed = a->precision == EXC_PREC_MIXED || a->precision == EXC_PREC_MIXED_RAW;
+  const bool mixed = a->precision >= EXC_PREC_MIXED;
   if (!mixed && (e = reject_split(metric))) return e;
   if (mixed) {
     const int me = exc_mixed::check(D, *a);
@@ -176,7 +176,7 @@ int exc_trace(const ExcMetric* metric, const ExcTraceArgs* a, void* stream) {
   if (sms <= 0) return fail(EXC_ERR_NO_DEVICE, "no CUDA device");
   cudaStream_t s = (cudaStream_t)stream;
   cudaError_t ce;
-  if (a->abort_flag || a->deadline_cycles > 0) {
+  if ((a->abort_flag || a->deadline_cycles > 0) && a->precision != EXC_PREC_RETRACE) {
     // photons the launch never reaches keep EXC_PH_NOT_RUN
     ce = exc_fast::fill_status(a->status, a->n_photons, EXC_PH_NOT_RUN, s);
     if (ce != cudaSuccess) return cuda_fail(ce, "fill_status");
@@ -190,17 +190,19 @@ int exc_trace(const ExcMetric* metric, const ExcTraceArgs* a, void* stream) {
   else if (a->precision == EXC_PREC_FP64_FAST)
     ce = exc_fast::trace(D, *a, block, a->blocks_per_sm, sms, s);
   else {
-    ce = exc_mixed::trace(D, *a, block, a->blocks_per_sm, sms, s);
-    if (ce != cudaSuccess) return cuda_fail(ce, "mixed trace launch");
-    if (a->precision == EXC_PREC_MIXED) {
-      // second launch on the same stream: the parity tracer takes the rays the
-      // mixed one handed back (status EXC_PH_RETRACE, state untouched)
-      if (a->queue) {
+    if (a->precision != EXC_PREC_RETRACE) {
+      ce = exc_mixed::trace(D, *a, block, a->blocks_per_sm, sms, s);
+      if (ce != cudaSuccess) return cuda_fail(ce, "mixed trace launch");
+    }
+    if (a->precision == EXC_PREC_MIXED || a->precision == EXC_PREC_RETRACE) {
+      // the FP64 tracer takes the rays the mixed one handed back (status
+      // EXC_PH_RETRACE, state and dt untouched); same stream, so in order
+      if (a->queue && a->precision == EXC_PREC_MIXED) {
         ce = cudaMemsetAsync(a->queue, 0, 2 * sizeof(uint32_t), s);
         if (ce != cudaSuccess) return cuda_fail(ce, "queue reset");
       }
       D.retrace_only = 1;
-      ce = exc_exact::trace(D, *a, block, a->blocks_per_sm, sms, s);
+      ce = exc_fast::trace(D, *a, block, a->blocks_per_sm, sms, s);
       if (ce != cudaSuccess) return cuda_fail(ce, "re-trace launch");
     }
     return EXC_SUCCESS;

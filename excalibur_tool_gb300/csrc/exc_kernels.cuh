@@ -531,8 +531,8 @@ cudaError_t launch_trace_stepper(const DevMetric& D, const ExcTraceArgs& A, Laun
     return launch_trace_r<EXC_METRIC_SCHWARZSCHILD, double, STEPPER>(D, A, lc, s);
   if (D.m.fields[0].dtype == EXC_DTYPE_F32) return launch_trace_r<EXC_METRIC_FLRW, float, STEPPER>(D, A, lc, s);
   if (D.m.fields[0].dtype == EXC_DTYPE_F32X2) {
-    // split grids reach the FP64 tracer only as the mixed tracer's RK4 re-trace pass
-    if constexpr (STEPPER == EXC_STEPPER_RK4 && !EXC_FAST) {
+    // split grids reach the FP64 tracer only as the mixed tracer's RK4 re-trace pass (fast build)
+    if constexpr (STEPPER == EXC_STEPPER_RK4 && EXC_FAST) {
       if (!A.records) return launch_trace_t<EXC_METRIC_FLRW, float2, STEPPER, false>(D, A, lc, s);
     }
     return cudaErrorInvalidValue;

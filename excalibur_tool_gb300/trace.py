@@ -29,7 +29,7 @@ class TraceConfig:
 
     stepper: str = "rk45"            # "rk4" | "rk45" | "leapfrog4"
     tableau: str = "reference"       # RK45 weights: "reference" (665/1287) | "fehlberg"
-    precision: str = "fp64"          # "fp64" (reference order) | "fp64_fast" | "mixed" | "mixed_raw"
+    precision: str = "fp64"          # "fp64" (reference order) | "fp64_fast" | "mixed" | "mixed_raw" | "retrace"
     dt: float = 1e-3
     dt_min: float = 1e14
     dt_max: float = 1e17
@@ -160,7 +160,7 @@ def trace_batch(metric, states, cfg: TraceConfig, *, field_index=None, dt=None, 
     _check_device_tensor(states, torch.float64, (8,), "states")
     dev = states.device
     n = states.shape[0]
-    desc = metric.descriptor(dev, split=cfg.precision in ("mixed", "mixed_raw"))
+    desc = metric.descriptor(dev, split=cfg.precision in ("mixed", "mixed_raw", "retrace"))
     if out is None:
         st = states.clone()
         status = torch.empty(n, dtype=torch.int32, device=dev)
@@ -186,8 +186,25 @@ def trace_batch(metric, states, cfg: TraceConfig, *, field_index=None, dt=None, 
         nf = desc.struct.n_fields
         if n and (int(field_index.min()) < 0 or int(field_index.max()) >= nf):
             raise ValueError(f"field_index values must lie in [0, {nf})")
+    res = TraceResult(st, status, nsteps, niter, dts, obs, records, nrec)
+    res.field_index = field_index
+    _launch(desc, res, cfg, queue=queue, abort_flag=abort_flag, stream=stream)
+    return res
+
+
+def _launch(desc, res, cfg: TraceConfig, *, queue=None, abort_flag=None, stream=None):
+    """Fill ExcTraceArgs from `res`'s tensors and call exc_trace on `stream`."""
+    import torch
+
+    dev = res.state.device
+    n = res.state.shape[0]
+    s = torch.cuda.current_stream(dev) if stream is None else stream
     if queue is None and cfg.use_queue:
-        queue = torch.zeros(2, dtype=torch.int64, device=dev)
+        with torch.cuda.stream(s):
+            queue = torch.zeros(2, dtype=torch.int64, device=dev)
+    st, status, nsteps, niter, dts, obs = res.state, res.status, res.n_steps, res.n_iter, res.dt, res.obs
+    records, nrec = res.records, res.n_records
+    field_index = getattr(res, "field_index", None)
 
     a = N.ExcTraceArgs()
     a.n_photons = n
@@ -235,12 +252,51 @@ def trace_batch(metric, states, cfg: TraceConfig, *, field_index=None, dt=None, 
     a.deadline_cycles = int(cfg.deadline_cycles)
 
     lib = N.load()
-    s = C.c_void_p(stream.cuda_stream) if stream is not None else N.stream_handle(dev)
     with torch.cuda.device(dev):
-        N.check(lib.exc_trace(C.byref(desc.struct), C.byref(a), s), "exc_trace")
-    res = TraceResult(st, status, nsteps, niter, dts, obs, records, nrec)
+        N.check(lib.exc_trace(C.byref(desc.struct), C.byref(a), C.c_void_p(s.cuda_stream)), "exc_trace")
     res._keepalive = (desc, queue)
     return res
+
+
+def retrace(metric, res: TraceResult, cfg: TraceConfig, *, stream=None) -> TraceResult:
+    """The FP64 pass of the guarded mixed tracer over `res` in place: photons that a
+    "mixed_raw" trace handed back (status "retrace") are traced by the FP64 tracer;
+    every other photon's outputs are left as they are."""
+    cfg = dataclasses.replace(cfg, precision="retrace").validate()
+    desc = metric.descriptor(res.state.device, split=True)
+    return _launch(desc, res, cfg, stream=stream)
+
+
+def trace_pipelined(metric, batches: Sequence, cfg: TraceConfig, *, side_stream=None) -> list:
+    """Guarded mixed tracing of several batches with the re-traces overlapped.
+
+    Each batch's mixed launch runs on the current stream; its FP64 re-trace of the
+    handed-back rays (a few percent, each as long as a full FP64 trajectory) runs on
+    `side_stream` after an event, so it overlaps the next batches' mixed launches.
+    The current stream waits for the side stream before returning; results are
+    those of precision "mixed" (identical per photon)."""
+    import torch
+
+    if cfg.precision not in ("mixed", "mixed_raw"):
+        raise ValueError("trace_pipelined runs the mixed tracer")
+    raw = dataclasses.replace(cfg, precision="mixed_raw")
+    main = torch.cuda.current_stream(batches[0].device)
+    side = side_stream or torch.cuda.Stream(batches[0].device)
+    out = []
+    for b in batches:
+        r = trace_batch(metric, b, raw)
+        ev = torch.cuda.Event()
+        ev.record(main)
+        side.wait_event(ev)
+        for t in (r.state, r.status, r.n_steps, r.n_iter, r.dt, r.obs):
+            if t is not None:
+                t.record_stream(side)
+        retrace(metric, r, cfg, stream=side)
+        out.append(r)
+    done = torch.cuda.Event()
+    done.record(side)
+    main.wait_event(done)
+    return out
 
 
 def _default_max_records(cfg: TraceConfig) -> int:

@@ -88,10 +88,15 @@ enum { EXC_TABLEAU_REFERENCE = 0, EXC_TABLEAU_FEHLBERG = 1 };
  * FAST:      same formulas, FMA contraction, reciprocal constants.
  * MIXED:     FP32 RHS + interpolation, double-float (hi + lo FP32) state; rays
  *            that come within the error window of a discontinuity of the
- *            reference's RHS are re-traced by the EXACT tracer in a second
+ *            reference's RHS are re-traced by the FAST FP64 tracer in a second
  *            launch on the same stream (FLRW, RK4, no records).
- * MIXED_RAW: the mixed launch alone; such rays end with EXC_PH_RETRACE. */
-enum { EXC_PREC_FP64_EXACT = 0, EXC_PREC_FP64_FAST = 1, EXC_PREC_MIXED = 2, EXC_PREC_MIXED_RAW = 3 };
+ * MIXED_RAW: the mixed launch alone; such rays end with EXC_PH_RETRACE.
+ * RETRACE:   the second launch alone: the FAST FP64 tracer over the photons
+ *            whose status is EXC_PH_RETRACE (the others are not touched), so a
+ *            caller can overlap one batch's re-trace with the next batch's
+ *            MIXED_RAW launch on another stream. */
+enum { EXC_PREC_FP64_EXACT = 0, EXC_PREC_FP64_FAST = 1, EXC_PREC_MIXED = 2, EXC_PREC_MIXED_RAW = 3,
+       EXC_PREC_RETRACE = 4 };
 
 /* stop_flags bits (the "steps" stop and max_iter always apply) */
 #define EXC_STOP_BOX   1

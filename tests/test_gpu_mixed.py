@@ -143,3 +143,19 @@ def test_mixed_raw_hands_back_untouched_rays(patch):
     assert not (mixed["status"] == N.PH_RETRACE).any()
     assert np.array_equal(mixed["n_steps"][back], o.n_steps[back])
     assert rel_err(mixed["state"][back], o.state[back]).max() <= 1e-12
+
+
+def test_pipelined_batches_match_single_launches(patch):
+    """Re-traces overlapped on a side stream give the same photons as precision "mixed"."""
+    import torch
+    from excalibur_tool_gb300.trace import trace_pipelined
+
+    wl, states, o = patch
+    parts = [wl.states[i * 16384:(i + 1) * 16384].contiguous() for i in range(4)]
+    res = trace_pipelined(wl.metric, parts, dataclasses.replace(wl.cfg, precision="mixed"))
+    torch.cuda.synchronize()
+    whole = _run(wl, "mixed")
+    got = np.concatenate([r.state.cpu().numpy() for r in res])
+    assert np.array_equal(got, whole["state"])
+    assert np.array_equal(np.concatenate([r.status.cpu().numpy() for r in res]), whole["status"])
+    assert np.array_equal(np.concatenate([r.obs.cpu().numpy() for r in res]), whole["obs"], equal_nan=True)
