@@ -74,6 +74,17 @@ class ExcTraceArgs(C.Structure):
                 ("queue", C.c_void_p), ("abort_flag", C.c_void_p), ("deadline_cycles", C.c_int64)]
 
 
+class ExcGemm(C.Structure):
+    _fields_ = [("a", C.c_void_p), ("b", C.c_void_p), ("m", C.c_int64), ("n", C.c_int32), ("k", C.c_int32),
+                ("stride_a", C.c_int64), ("stride_b", C.c_int64), ("n_batch", C.c_int32),
+                ("epilogue", C.c_int32), ("k_splits", C.c_int32), ("reserved", C.c_int32),
+                ("bias", C.c_void_p), ("z_in", C.c_void_p), ("c", C.c_void_p), ("c2", C.c_void_p),
+                ("ct", C.c_void_p), ("stride_c", C.c_int64), ("ldt", C.c_int64), ("stride_ct", C.c_int64)]
+
+
+EPI_F32, EPI_BIAS_SILU, EPI_DSILU, EPI_SPLITK = 0, 1, 2, 3
+
+_V = C.c_void_p
 EXPORTS = {
     "exc_abi_version": (C.c_int, []),
     "exc_strerror": (C.c_char_p, [C.c_int]),
@@ -91,6 +102,17 @@ EXPORTS = {
     "exc_null_error": (C.c_int, [C.POINTER(ExcMetric), C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                  C.c_int64, C.c_void_p]),
     "exc_trace_noalloc": (C.c_int, [C.POINTER(ExcMetric), C.POINTER(ExcTraceArgs), C.c_void_p]),
+    # surrogate kernels (include/excalibur_mlp.h)
+    "exc_gemm_bf16": (C.c_int, [C.POINTER(ExcGemm), _V]),
+    "exc_mlp_features": (C.c_int, [_V, C.c_int64, C.c_int64, C.c_int32, C.POINTER(C.c_double),
+                                   C.POINTER(C.c_double), _V, _V]),
+    "exc_mlp_head": (C.c_int, [_V, C.c_int64, C.c_int32, C.c_int32, C.c_int32, _V, _V, _V, _V, _V, _V, _V,
+                               C.c_int64, _V, _V, _V, _V]),
+    "exc_mlp_reduce_splits": (C.c_int, [_V, C.c_int32, C.c_int32, C.c_int64, _V, _V]),
+    "exc_mlp_row_sums": (C.c_int, [_V, C.c_int64, C.c_int64, C.c_int64, _V, _V]),
+    "exc_mlp_adam": (C.c_int, [_V, _V, _V, _V, C.c_int64, C.c_float, C.c_float, C.c_float, C.c_float, C.c_int32,
+                               _V, _V, C.c_int32, C.c_int32, _V]),
+    "exc_mlp_error_count": (C.c_int, [C.POINTER(C.c_uint32)]),
 }
 
 _lib = None

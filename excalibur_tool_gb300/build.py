@@ -26,6 +26,7 @@ UNITS = {
     "exc_mixed.cu": ["--fmad=true"],
     "exc_capi.cu": [],
     "exc_noalloc.cu": [],
+    "exc_mlp.cu": [],
 }
 
 

@@ -1,0 +1,110 @@
+"""Thin ctypes wrappers over the surrogate's CUDA kernels (include/excalibur_mlp.h).
+
+Every function takes device tensors (torch is only the allocator and the
+stream) and launches on the current CUDA stream; nothing here computes on the
+host. BF16 tensors are torch.bfloat16.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+from .. import _native as N
+
+EPI = {"f32": N.EPI_F32, "bias_silu": N.EPI_BIAS_SILU, "dsilu": N.EPI_DSILU, "splitk": N.EPI_SPLITK}
+
+
+def _p(t):
+    return None if t is None else C.c_void_p(t.data_ptr())
+
+
+def _stream(t):
+    import torch
+
+    return C.c_void_p(torch.cuda.current_stream(t.device).cuda_stream)
+
+
+def _as3(t):
+    return t if t.dim() == 3 else t.unsqueeze(0)
+
+
+def gemm(a, b, *, epilogue="f32", bias=None, z_in=None, c=None, c2=None, ct=None, k_splits=1):
+    """epilogue(A . B^T): a [E, M, K] (or [M, K]) bf16, b [E, N, K] bf16, outputs preallocated.
+
+    c:  f32 [E, M, N] ("f32"), f32 [E, splits, M, N] ("splitk"), bf16 [E, M, N] (others);
+    c2: bf16 [E, M, N] (silu output); ct: bf16 [E, N, ldt] transposed output."""
+    import torch
+
+    a3, b3 = _as3(a), _as3(b)
+    E, M, K = a3.shape
+    Eb, Nn, Kb = b3.shape
+    if Eb != E or Kb != K:
+        raise ValueError("gemm: a [E,M,K] and b [E,N,K] must agree")
+    for t in (a3, b3):
+        if t.dtype != torch.bfloat16 or not t.is_contiguous():
+            raise TypeError("gemm: a and b must be contiguous bfloat16")
+    g = N.ExcGemm()
+    g.a, g.b = a3.data_ptr(), b3.data_ptr()
+    g.m, g.n, g.k = M, Nn, K
+    g.stride_a, g.stride_b = M * K, Nn * K
+    g.n_batch = E
+    g.epilogue = EPI[epilogue]
+    g.k_splits = int(k_splits)
+    g.bias = bias.data_ptr() if bias is not None else None
+    g.z_in = z_in.data_ptr() if z_in is not None else None
+    g.c = c.data_ptr() if c is not None else None
+    g.c2 = c2.data_ptr() if c2 is not None else None
+    g.ct = ct.data_ptr() if ct is not None else None
+    g.stride_c = M * Nn
+    if ct is not None:
+        ct3 = _as3(ct)
+        g.ldt = ct3.shape[2]
+        g.stride_ct = ct3.shape[1] * ct3.shape[2]
+    lib = N.load()
+    N.check(lib.exc_gemm_bf16(C.byref(g), _stream(a3)), "exc_gemm_bf16")
+
+
+def features(dirs, n_pad, n_freq, center, scale, out):
+    """Fourier features of [n, 2] float64 (theta, phi) directions into out [n_pad, 4 n_freq] bf16."""
+    lib = N.load()
+    c2 = (C.c_double * 2)(*[float(v) for v in center])
+    s2 = (C.c_double * 2)(*[float(v) for v in scale])
+    N.check(lib.exc_mlp_features(_p(dirs), dirs.shape[0], n_pad, n_freq, c2, s2, _p(out), _stream(out)),
+            "exc_mlp_features")
+
+
+def head(h, w, b, *, y=None, targets=None, z=None, dh=None, dht=None, dw=None, db=None, loss=None):
+    """Linear head over h [E, M, 256] bf16 with w [E, n_out, 256] f32, b [E, n_out] f32."""
+    E, M, width = h.shape
+    n_out = w.shape[1]
+    ldt = dht.shape[2] if dht is not None else 0
+    lib = N.load()
+    N.check(lib.exc_mlp_head(_p(h), M, width, n_out, E, _p(w), _p(b), _p(y), _p(targets), _p(z), _p(dh), _p(dht),
+                             ldt, _p(dw), _p(db), _p(loss), _stream(h)), "exc_mlp_head")
+
+
+def reduce_splits(part, out):
+    """part [E, S, R, C] f32 -> out [E, R, C] (sum over S)."""
+    E, S = part.shape[0], part.shape[1]
+    rc = part[0, 0].numel()
+    lib = N.load()
+    N.check(lib.exc_mlp_reduce_splits(_p(part), E, S, rc, _p(out), _stream(part)), "exc_mlp_reduce_splits")
+
+
+def row_sums(x, m, out):
+    """Row sums of x [R, ld] bf16 over the first m columns -> out [R] f32."""
+    rows, ld = x.shape[-2] * (x.shape[0] if x.dim() == 3 else 1), x.shape[-1]
+    lib = N.load()
+    N.check(lib.exc_mlp_row_sums(_p(x), rows, m, ld, _p(out), _stream(x)), "exc_mlp_row_sums")
+
+
+def adam(p, g, m1, m2, *, lr, beta1, beta2, eps, t, p_bf16=None, pt_bf16=None, shape=None):
+    rows, cols = shape if shape is not None else (0, 0)
+    lib = N.load()
+    N.check(lib.exc_mlp_adam(_p(p), _p(g), _p(m1), _p(m2), p.numel(), lr, beta1, beta2, eps, t, _p(p_bf16),
+                             _p(pt_bf16), rows, cols, _stream(p)), "exc_mlp_adam")
+
+
+def error_count() -> int:
+    v = C.c_uint32(0)
+    N.check(N.load().exc_mlp_error_count(C.byref(v)), "exc_mlp_error_count")
+    return int(v.value)

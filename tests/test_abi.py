@@ -12,12 +12,15 @@ from conftest import ROOT
 from excalibur_tool_gb300 import _native as N
 
 HEADER = os.path.join(ROOT, "include", "excalibur_gb300.h")
+HEADERS = [os.path.join(ROOT, "include", h) for h in ("excalibur_gb300.h", "excalibur_mlp.h")]
 
 
 def declared_functions():
-    text = open(HEADER).read()
-    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
-    return sorted(set(re.findall(r"\b(exc_[a-z0-9_]+)\s*\(", text)))
+    names = set()
+    for h in HEADERS:
+        text = re.sub(r"/\*.*?\*/", "", open(h).read(), flags=re.S)
+        names.update(re.findall(r"\b(exc_[a-z0-9_]+)\s*\(", text))
+    return sorted(names)
 
 
 @pytest.fixture(scope="module")
@@ -111,10 +114,12 @@ def test_struct_layout_matches_c():
 #include <stdio.h>
 #include <stddef.h>
 #include "excalibur_gb300.h"
+#include "excalibur_mlp.h"
 int main(void) {
-  printf("%zu %zu %zu %zu %zu %zu %zu\n", sizeof(ExcField), sizeof(ExcMetric), sizeof(ExcTraceArgs),
+  printf("%zu %zu %zu %zu %zu %zu %zu %zu %zu %zu\n", sizeof(ExcField), sizeof(ExcMetric), sizeof(ExcTraceArgs),
          offsetof(ExcMetric, fields), offsetof(ExcTraceArgs, dt), offsetof(ExcTraceArgs, queue),
-         offsetof(ExcTraceArgs, deadline_cycles));
+         offsetof(ExcTraceArgs, deadline_cycles), sizeof(ExcGemm), offsetof(ExcGemm, bias),
+         offsetof(ExcGemm, stride_ct));
   return 0;
 }
 '''
@@ -125,5 +130,6 @@ int main(void) {
         subprocess.run(["gcc", "-I", os.path.dirname(HEADER), c, "-o", exe], check=True)
         got = [int(v) for v in subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split()]
     want = [C.sizeof(N.ExcField), C.sizeof(N.ExcMetric), C.sizeof(N.ExcTraceArgs), N.ExcMetric.fields.offset,
-            N.ExcTraceArgs.dt.offset, N.ExcTraceArgs.queue.offset, N.ExcTraceArgs.deadline_cycles.offset]
+            N.ExcTraceArgs.dt.offset, N.ExcTraceArgs.queue.offset, N.ExcTraceArgs.deadline_cycles.offset,
+            C.sizeof(N.ExcGemm), N.ExcGemm.bias.offset, N.ExcGemm.stride_ct.offset]
     assert got == want
