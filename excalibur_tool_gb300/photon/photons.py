@@ -262,22 +262,32 @@ class Photons:
         u_sp = self._spatial_from_directions(origin, d, direction_basis)
         return self._finish(np.tile(origin, (len(d), 1)), u_sp, sign)
 
-    def generate_patch_grid(self, n_side, origin, central_direction, patch_deg, sign=-1.0, device="cuda"):
-        """n_side^2 pixel centres of a patch_deg x patch_deg tangent-plane patch around the axis."""
-        import torch
-
+    @staticmethod
+    def patch_basis(central_direction):
+        """Unit axis k and tangent-plane basis (e1, e2) of a patch around `central_direction`."""
         k = np.asarray(central_direction, dtype=float)
         k = k / np.linalg.norm(k)
         up = np.array([0.0, 0.0, 1.0]) if abs(k[2]) < 0.9 else np.array([0.0, 1.0, 0.0])
         e1 = np.cross(up, k)
         e1 /= np.linalg.norm(e1)
         e2 = np.cross(k, e1)
+        return k, e1, e2
+
+    def generate_patch_points(self, uv, origin, central_direction, patch_deg, sign=-1.0):
+        """Directions at tangent-plane coordinates uv [n, 2] in [-1, 1]^2 of a patch_deg x patch_deg patch."""
+        k, e1, e2 = self.patch_basis(central_direction)
         half = np.tan(np.deg2rad(patch_deg / 2.0))
-        t = (np.arange(n_side) + 0.5) / n_side * 2 - 1
-        A, B = np.meshgrid(t, t, indexing="ij")
-        d = k[None] + (A.reshape(-1, 1) * half) * e1[None] + (B.reshape(-1, 1) * half) * e2[None]
+        uv = np.asarray(uv, dtype=float)
+        d = k[None] + (uv[:, :1] * half) * e1[None] + (uv[:, 1:2] * half) * e2[None]
         d /= np.linalg.norm(d, axis=1)[:, None]
         return self._finish(np.tile(np.asarray(origin, dtype=float), (len(d), 1)), d * c, sign)
+
+    def generate_patch_grid(self, n_side, origin, central_direction, patch_deg, sign=-1.0, device="cuda"):
+        """n_side^2 pixel centres of a patch_deg x patch_deg tangent-plane patch around the axis."""
+        t = (np.arange(n_side) + 0.5) / n_side * 2 - 1
+        A, B = np.meshgrid(t, t, indexing="ij")
+        return self.generate_patch_points(np.stack([A.reshape(-1), B.reshape(-1)], 1), origin, central_direction,
+                                          patch_deg, sign)
 
     def generate_full_sky(self, n_photons, origin, seed, sign=-1.0):
         """Uniform random directions on the sphere (numpy default_rng(seed))."""

@@ -28,24 +28,28 @@ def _as3(t):
 
 
 def gemm(a, b, *, epilogue="f32", bias=None, z_in=None, c=None, c2=None, ct=None, k_splits=1):
-    """epilogue(A . B^T): a [E, M, K] (or [M, K]) bf16, b [E, N, K] bf16, outputs preallocated.
+    """epilogue(A . B^T): a [E, M, K] bf16, b [E, N, K] bf16 (a 2-D operand is shared by
+    every member: batch stride 0); outputs preallocated and contiguous:
 
     c:  f32 [E, M, N] ("f32"), f32 [E, splits, M, N] ("splitk"), bf16 [E, M, N] (others);
     c2: bf16 [E, M, N] (silu output); ct: bf16 [E, N, ldt] transposed output."""
     import torch
 
-    a3, b3 = _as3(a), _as3(b)
-    E, M, K = a3.shape
-    Eb, Nn, Kb = b3.shape
-    if Eb != E or Kb != K:
+    M, K = a.shape[-2:]
+    Nn, Kb = b.shape[-2:]
+    E = max(a.shape[0] if a.dim() == 3 else 1, b.shape[0] if b.dim() == 3 else 1)
+    if Kb != K or (a.dim() == 3 and a.shape[0] != E) or (b.dim() == 3 and b.shape[0] != E):
         raise ValueError("gemm: a [E,M,K] and b [E,N,K] must agree")
-    for t in (a3, b3):
-        if t.dtype != torch.bfloat16 or not t.is_contiguous():
-            raise TypeError("gemm: a and b must be contiguous bfloat16")
+    for t in (a, b, c, c2, ct, z_in):
+        if t is not None and not t.is_contiguous():
+            raise ValueError("gemm: operands and outputs must be contiguous")
+    if a.dtype != torch.bfloat16 or b.dtype != torch.bfloat16:
+        raise TypeError("gemm: a and b must be bfloat16")
     g = N.ExcGemm()
-    g.a, g.b = a3.data_ptr(), b3.data_ptr()
+    g.a, g.b = a.data_ptr(), b.data_ptr()
     g.m, g.n, g.k = M, Nn, K
-    g.stride_a, g.stride_b = M * K, Nn * K
+    g.stride_a = M * K if a.dim() == 3 else 0
+    g.stride_b = Nn * K if b.dim() == 3 else 0
     g.n_batch = E
     g.epilogue = EPI[epilogue]
     g.k_splits = int(k_splits)
@@ -56,11 +60,10 @@ def gemm(a, b, *, epilogue="f32", bias=None, z_in=None, c=None, c2=None, ct=None
     g.ct = ct.data_ptr() if ct is not None else None
     g.stride_c = M * Nn
     if ct is not None:
-        ct3 = _as3(ct)
-        g.ldt = ct3.shape[2]
-        g.stride_ct = ct3.shape[1] * ct3.shape[2]
+        g.ldt = ct.shape[-1]
+        g.stride_ct = ct.shape[-2] * ct.shape[-1]
     lib = N.load()
-    N.check(lib.exc_gemm_bf16(C.byref(g), _stream(a3)), "exc_gemm_bf16")
+    N.check(lib.exc_gemm_bf16(C.byref(g), _stream(a)), "exc_gemm_bf16")
 
 
 def features(dirs, n_pad, n_freq, center, scale, out):

@@ -94,3 +94,19 @@ def test_integrator_config_mapping():
         it.config("redshift", 1.0)
     with pytest.raises(ValueError):
         Integrator(M(), integrator="euler")
+
+
+def test_exit_geometry_crossing():
+    """The straight-line exit and the back-extrapolated crossing of a box face."""
+    from excalibur_tool_gb300.surrogate.sky import ExitGeometry, Patch
+
+    patch = Patch((1.0, 0.0, 5.0, 5.0), (1.0, 0.0, 0.0), 20.0)
+    geo = ExitGeometry(patch, ((0.0, 0.0, 0.0), (10.0, 10.0, 10.0)))
+    ax, t, p = geo.straight(np.array([[0.0, 0.0], [0.5, -0.5]]))
+    assert list(ax) == [0, 0] and np.allclose(p[:, 0], 10.0) and np.isclose(t[0], 10.0)
+    # a state 0.3 past the x = 10 face, moving along (2, 1, 0) with u0 = 4: back by 0.15 in lambda
+    st = np.array([[7.0, 10.3, 6.0, 5.0, 4.0, 2.0, 1.0, 0.0]])
+    axc, eta_c, x_c = geo.crossing(st)
+    assert axc[0] == 0 and np.isclose(eta_c[0], 7.0 - 0.15 * 4.0)
+    assert np.allclose(x_c[0], [10.0, 5.85, 5.0])
+    assert ExitGeometry.in_face(np.array([0, 1, 2])).tolist() == [[1, 2], [2, 0], [0, 1]]
