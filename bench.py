@@ -56,6 +56,8 @@ def parse():
     p.add_argument("--no-precision", action="store_true", help="skip the 512^3 / 4M-ray precision workload")
     p.add_argument("--precision-side", type=int, default=2048)
     p.add_argument("--no-surrogate", action="store_true", help="skip the learned sky-map leg")
+    p.add_argument("--no-batching", action="store_true", help="skip the multi-field RK45 batching leg")
+    p.add_argument("--batching-scale", type=int, default=4, help="run 1/scale of the batching configuration")
     p.add_argument("--map-side", type=int, default=4096)
     p.add_argument("--train-steps", type=int, default=8000)
     return p.parse_args()
@@ -299,6 +301,9 @@ def run_ours(args, rank, world, local):
         del wl, metric, states, res
         torch.cuda.empty_cache()
         line["precision"] = run_precision(args, dev, stream, flush, value)
+    if not args.no_batching and world == 1:
+        torch.cuda.empty_cache()
+        line["batching"] = run_batching(args, dev, stream)
     if not args.no_surrogate and world == 1:
         torch.cuda.empty_cache()
         line["surrogate"] = run_surrogate(args, dev, stream, peaks, rays_s)
@@ -430,6 +435,70 @@ def run_precision(args, dev, stream, flush, fp64_value):
             "speedup_vs_fp64_patch_value": mixed_ps / fp64_value,
             "errors_vs_fp64_on_subset": {**err, "subset": "65,536 rays, numpy default_rng(40)"},
             "host_field_build_s": build_s}
+
+
+def run_batching(args, dev, stream):
+    """The lens grid (256^3) with 1,048,576 full-sky rays plus 16 random fields (64^3..256^3) with
+    65,536 patch rays each: one persistent adaptive-RK45 launch, autotuned, captured in a CUDA graph."""
+    import torch
+
+    from excalibur_tool_gb300 import workloads
+    from excalibur_tool_gb300.trace import CapturedTrace, autotune, trace_batch, tune_report
+
+    t0 = time.perf_counter()
+    scale = args.batching_scale
+    wl = workloads.multi_field(n_sky=(1 << 20) // scale, n_side=256 // int(round(scale ** 0.5)), device=dev)
+    build_s = time.perf_counter() - t0
+    t1 = time.perf_counter()
+    tuned = autotune(wl.metric, wl.states, wl.cfg, field_index=wl.field_index, use_cache=False)
+    tune_s = time.perf_counter() - t1
+    plan = next(iter(tune_report().values()))
+    # one eager launch with the default schedule for comparison
+    r = trace_batch(wl.metric, wl.states, wl.cfg, field_index=wl.field_index)
+    torch.cuda.synchronize(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    r = trace_batch(wl.metric, wl.states, wl.cfg, field_index=wl.field_index)
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    default_s = e0.elapsed_time(e1) / 1e3
+    cap = CapturedTrace(wl.metric, wl.states, tuned, field_index=wl.field_index)
+    cap.run()
+    torch.cuda.synchronize(dev)
+    k = 3
+    e0.record(stream)
+    for _ in range(k):
+        out = cap.run()
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    graph_s = e0.elapsed_time(e1) / 1e3 / k
+    n = wl.states.shape[0]
+    steps = out.n_steps.cpu().numpy()
+    iters = out.n_iter.cpu().numpy()
+    status = out.status.cpu().numpy()
+    fidx = wl.field_index.cpu().numpy()
+    sky = fidx == 0
+    long = steps[sky][steps[sky] > 1]
+    return {"workload": f"lens alone on a 256^3 float64 grid with {(1 << 20) // scale:,} full-sky rays "
+                        f"(default_rng(3)) + 16 random fields (seeds 1-16; 64^3/128^3/256^3) x "
+                        f"{wl.info['patch_photons']:,} patch rays, adaptive RK45 (Fehlberg weights, rtol 1e-8, "
+                        "atol 1e-12, dt in [1e10, 1e17] s) to box exit; one launch"
+                        + (f"; 1/{scale} of the 1,048,576 + 16 x 65,536 configuration" if scale > 1 else ""),
+            "photons": n, "fields": wl.info["fields"], "host_build_s": build_s,
+            "autotune": {"block_size": plan["block_size"], "blocks_per_sm": plan["blocks_per_sm"],
+                         "best_steps_tried_per_s": plan["best_rate"], "trials": len(plan["trials"]),
+                         "seconds": tune_s, "sample": plan["sample"], "time_box": "1e8 SM cycles per trial",
+                         "all_trials": [{"block": t[0], "per_sm": t[1], "rate": t[3]} for t in plan["trials"]]},
+            "default_schedule_s": default_s, "graph_replay_s": graph_s,
+            "rays_per_s": n / graph_s, "accepted_steps_per_s": float(steps.sum()) / graph_s,
+            "rk45_trials_per_s": float(iters.sum()) / graph_s,
+            "steps_sky_rays_leaving_forward": {"p05": float(np.percentile(long, 5)), "median": float(np.median(long)),
+                                               "p95": float(np.percentile(long, 95)), "max": int(long.max())}
+            if len(long) else None,
+            "steps_patch_rays_median": float(np.median(steps[~sky])),
+            "rejected_fraction": float(1 - steps.sum() / max(1, iters.sum())),
+            "status_counts": np.bincount(status, minlength=12).tolist(),
+            "gpu_launches_per_replay": 1}
 
 
 def gemm_tflops(dev, stream, m=1 << 20, members=4):

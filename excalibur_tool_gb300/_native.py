@@ -74,6 +74,16 @@ class ExcTraceArgs(C.Structure):
                 ("queue", C.c_void_p), ("abort_flag", C.c_void_p), ("deadline_cycles", C.c_int64)]
 
 
+EXC_TUNE_MAX_TRIALS = 32
+
+
+class ExcLaunchPlan(C.Structure):
+    _fields_ = [("block_size", C.c_int32), ("blocks_per_sm", C.c_int32), ("best_ms", C.c_float),
+                ("best_rate", C.c_float), ("n_trials", C.c_int32), ("trial_block", C.c_int32 * EXC_TUNE_MAX_TRIALS),
+                ("trial_blocks_per_sm", C.c_int32 * EXC_TUNE_MAX_TRIALS),
+                ("trial_ms", C.c_float * EXC_TUNE_MAX_TRIALS), ("trial_rate", C.c_float * EXC_TUNE_MAX_TRIALS)]
+
+
 class ExcGemm(C.Structure):
     _fields_ = [("a", C.c_void_p), ("b", C.c_void_p), ("m", C.c_int64), ("n", C.c_int32), ("k", C.c_int32),
                 ("stride_a", C.c_int64), ("stride_b", C.c_int64), ("n_batch", C.c_int32),
@@ -102,6 +112,8 @@ EXPORTS = {
     "exc_null_error": (C.c_int, [C.POINTER(ExcMetric), C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                  C.c_int64, C.c_void_p]),
     "exc_trace_noalloc": (C.c_int, [C.POINTER(ExcMetric), C.POINTER(ExcTraceArgs), C.c_void_p]),
+    "exc_autotune": (C.c_int, [C.POINTER(ExcMetric), C.POINTER(ExcTraceArgs), C.c_void_p,
+                               C.POINTER(ExcLaunchPlan), C.c_void_p]),
     # surrogate kernels (include/excalibur_mlp.h)
     "exc_gemm_bf16": (C.c_int, [C.POINTER(ExcGemm), _V]),
     "exc_mlp_features": (C.c_int, [_V, C.c_int64, C.c_int64, C.c_int32, C.POINTER(C.c_double),

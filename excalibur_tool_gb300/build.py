@@ -27,6 +27,7 @@ UNITS = {
     "exc_capi.cu": [],
     "exc_noalloc.cu": [],
     "exc_mlp.cu": [],
+    "exc_tune.cu": [],
 }
 
 

@@ -192,16 +192,9 @@ def trace_batch(metric, states, cfg: TraceConfig, *, field_index=None, dt=None, 
     return res
 
 
-def _launch(desc, res, cfg: TraceConfig, *, queue=None, abort_flag=None, stream=None):
-    """Fill ExcTraceArgs from `res`'s tensors and call exc_trace on `stream`."""
-    import torch
-
-    dev = res.state.device
+def _make_args(desc, res, cfg: TraceConfig, queue=None, abort_flag=None) -> N.ExcTraceArgs:
+    """ExcTraceArgs pointing at `res`'s tensors."""
     n = res.state.shape[0]
-    s = torch.cuda.current_stream(dev) if stream is None else stream
-    if queue is None and cfg.use_queue:
-        with torch.cuda.stream(s):
-            queue = torch.zeros(2, dtype=torch.int64, device=dev)
     st, status, nsteps, niter, dts, obs = res.state, res.status, res.n_steps, res.n_iter, res.dt, res.obs
     records, nrec = res.records, res.n_records
     field_index = getattr(res, "field_index", None)
@@ -250,7 +243,19 @@ def _launch(desc, res, cfg: TraceConfig, *, queue=None, abort_flag=None, stream=
     a.queue = queue.data_ptr() if queue is not None else None
     a.abort_flag = abort_flag.data_ptr() if abort_flag is not None else None
     a.deadline_cycles = int(cfg.deadline_cycles)
+    return a
 
+
+def _launch(desc, res, cfg: TraceConfig, *, queue=None, abort_flag=None, stream=None):
+    """Call exc_trace on `res`'s tensors on `stream`."""
+    import torch
+
+    dev = res.state.device
+    s = torch.cuda.current_stream(dev) if stream is None else stream
+    if queue is None and cfg.use_queue:
+        with torch.cuda.stream(s):
+            queue = torch.zeros(2, dtype=torch.int64, device=dev)
+    a = _make_args(desc, res, cfg, queue, abort_flag)
     lib = N.load()
     with torch.cuda.device(dev):
         N.check(lib.exc_trace(C.byref(desc.struct), C.byref(a), C.c_void_p(s.cuda_stream)), "exc_trace")
@@ -297,6 +302,106 @@ def trace_pipelined(metric, batches: Sequence, cfg: TraceConfig, *, side_stream=
     done.record(side)
     main.wait_event(done)
     return out
+
+
+_TUNE_CACHE: dict = {}
+
+
+def autotune(metric, states, cfg: TraceConfig, *, field_index=None, sample: int = 131072, seed: int = 0,
+             time_box_cycles: int = 100_000_000, use_cache: bool = True) -> TraceConfig:
+    """`cfg` with the (block_size, blocks_per_sm) that exc_autotune measured fastest.
+
+    The sample is a seeded random subset of `states` (and `field_index`) in shuffled
+    order, and each trial is time-boxed (`time_box_cycles` SM clock cycles, ~50 ms):
+    the score is steps tried per second over the box, i.e. the steady-state rate of
+    the mix, not the time of the longest trajectory. Plans are cached per device,
+    metric kind, stepper, tableau, precision, grid dtype and number of fields."""
+    import torch
+
+    dev = states.device
+    desc = metric.descriptor(dev, split=cfg.precision in ("mixed", "mixed_raw", "retrace"))
+    key = (torch.cuda.get_device_name(dev), desc.kind, cfg.stepper, cfg.tableau, cfg.precision,
+           int(desc.struct.fields[0].dtype), int(desc.struct.n_fields))
+    if use_cache and key in _TUNE_CACHE:
+        b, p = _TUNE_CACHE[key][:2]
+        return dataclasses.replace(cfg, block_size=b, blocks_per_sm=p)
+    n = states.shape[0]
+    g = torch.Generator(device="cpu").manual_seed(seed)
+    idx = torch.randperm(n, generator=g)[:min(sample, n)].to(dev)
+    pristine = states[idx].contiguous()
+    fidx = field_index[idx].contiguous() if field_index is not None else None
+    m = pristine.shape[0]
+    res = TraceResult(pristine.clone(), torch.empty(m, dtype=torch.int32, device=dev),
+                      torch.empty(m, dtype=torch.int32, device=dev), torch.empty(m, dtype=torch.int32, device=dev),
+                      torch.empty(m, dtype=torch.float64, device=dev),
+                      torch.empty((m, N.OBS_N), dtype=torch.float64, device=dev) if cfg.observables else None)
+    res.field_index = fidx
+    queue = torch.zeros(2, dtype=torch.int64, device=dev) if cfg.use_queue else None
+    a = _make_args(desc, res, dataclasses.replace(cfg, deadline_cycles=int(time_box_cycles)), queue)
+    a.dt_state = None
+    plan = N.ExcLaunchPlan()
+    lib = N.load()
+    with torch.cuda.device(dev):
+        N.check(lib.exc_autotune(C.byref(desc.struct), C.byref(a), C.c_void_p(pristine.data_ptr()), C.byref(plan),
+                                 N.stream_handle(dev)), "exc_autotune")
+    trials = [(plan.trial_block[i], plan.trial_blocks_per_sm[i], plan.trial_ms[i], plan.trial_rate[i])
+              for i in range(plan.n_trials)]
+    _TUNE_CACHE[key] = (plan.block_size, plan.blocks_per_sm, plan.best_ms, trials, plan.best_rate, m)
+    return dataclasses.replace(cfg, block_size=plan.block_size, blocks_per_sm=plan.blocks_per_sm)
+
+
+def tune_report() -> dict:
+    return {str(k): {"block_size": v[0], "blocks_per_sm": v[1], "best_ms": v[2], "trials": v[3],
+                     "best_rate": v[4], "sample": v[5]} for k, v in _TUNE_CACHE.items()}
+
+
+class CapturedTrace:
+    """A trace of a fixed-size batch captured once in a CUDA graph and replayed.
+
+    The graph holds the copy of the input states into the result buffer, the dt
+    reset, the work-queue reset and the exc_trace launch(es) (two for the guarded
+    mixed tracer), so one replay is one graph launch with no host work between
+    kernels. `run(states)` copies new inputs into the static input buffer first."""
+
+    def __init__(self, metric, states, cfg: TraceConfig, *, field_index=None):
+        import torch
+
+        cfg.validate()
+        if cfg.record_every is not None:
+            raise ValueError("records are not captured")
+        dev = states.device
+        n = states.shape[0]
+        self.cfg = cfg
+        self.desc = metric.descriptor(dev, split=cfg.precision in ("mixed", "mixed_raw", "retrace"))
+        self.inputs = states.clone()
+        self.field_index = field_index.clone() if field_index is not None else None
+        self.res = TraceResult(states.clone(), torch.empty(n, dtype=torch.int32, device=dev),
+                               torch.empty(n, dtype=torch.int32, device=dev),
+                               torch.empty(n, dtype=torch.int32, device=dev),
+                               torch.empty(n, dtype=torch.float64, device=dev),
+                               torch.empty((n, N.OBS_N), dtype=torch.float64, device=dev) if cfg.observables else None)
+        self.res.field_index = self.field_index
+        self.queue = torch.zeros(2, dtype=torch.int64, device=dev) if cfg.use_queue else None
+        side = torch.cuda.Stream(dev)
+        side.wait_stream(torch.cuda.current_stream(dev))
+        with torch.cuda.stream(side):              # eager run: loads the kernels before capture
+            self._body()
+        torch.cuda.current_stream(dev).wait_stream(side)
+        torch.cuda.synchronize(dev)
+        self.graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(self.graph):
+            self._body()
+
+    def _body(self):
+        self.res.state.copy_(self.inputs)
+        self.res.dt.fill_(float(self.cfg.dt))
+        _launch(self.desc, self.res, self.cfg, queue=self.queue)
+
+    def run(self, states=None) -> TraceResult:
+        if states is not None:
+            self.inputs.copy_(states)
+        self.graph.replay()
+        return self.res
 
 
 def _default_max_records(cfg: TraceConfig) -> int:

@@ -11,8 +11,12 @@
   deta = 0.5 Mpc, until box exit or a <= 0.5.
 * flrw_patch_fp32grid: the same construction on a 512^3 float32 grid,
   2048 x 2048 directions in a 20 x 20 deg patch (seed 4).
-* multi_field: one main field plus 16 random-field realisations (seeds 1..16,
-  grids cycling 64^3/128^3/256^3) traced in one launch.
+* multi_field: the lens alone (Plummer, no random field) on a 256^3 float64 grid
+  with 1,048,576 full-sky directions (numpy default_rng(3)), plus 16 random-field
+  realisations (seeds 1..16, grid 64^3 / 128^3 / 256^3 for seed mod 3 = 0 / 1 / 2)
+  with the 65,536-ray patch each, all traced in one launch with adaptive RK45
+  (Fehlberg weights, rtol 1e-8, atol 1e-12, dt clipped to [1e10, 1e17] s, at most
+  20,000 tried steps per ray).
 
 Inputs are resident on the GPU when the builders return.
 """
@@ -28,7 +32,7 @@ from .grid.grid import Grid
 from .grid.interpolator_4d_fast import InterpolatorFast
 from .metrics.perturbed_flrw_metric_fast import PerturbedFLRWMetricFast
 from .metrics.schwarzschild_metric_fast import SchwarzschildMetricFast
-from .objects.fields import lens_plus_grf
+from .objects.fields import gaussian_random_field, lens_plus_grf, plummer_potential
 from .photon.photons import Photons
 from .trace import TraceConfig
 
@@ -90,3 +94,41 @@ def lens_cone(n_theta=32, n_phi=32, cone_deg=5.0, n_steps=2000, precision="fp64"
     cfg = TraceConfig(stepper="rk4", precision=precision, dt=DLAMBDA, dt_min=DLAMBDA, dt_max=DLAMBDA,
                       max_steps=n_steps, max_iter=n_steps)
     return Workload("lens_cone", metric, states.to(device), cfg, {"photons": n_theta * n_phi})
+
+
+def multi_field(main_n=256, n_sky=1 << 20, n_side=256, seeds=tuple(range(1, 17)), sizes=(64, 128, 256),
+                tableau="fehlberg", rtol=1e-8, atol=1e-12, precision="fp64", device="cuda"):
+    import torch
+
+    from ._evaluate import null_init
+
+    cz = lcdm()
+    grids, interps = [], []
+    g0 = Grid((main_n,) * 3, (BOX / main_n,) * 3, (0.0, 0.0, 0.0))
+    g0.add_field("Phi", plummer_potential(main_n, BOX, LENS_MASS, 5 * one_Mpc, LENS))
+    interps.append(InterpolatorFast(g0, boundary="periodic"))
+    for sd in seeds:
+        n = sizes[sd % 3]
+        g = Grid((n,) * 3, (BOX / n,) * 3, (0.0, 0.0, 0.0))
+        g.add_field("Phi", float(c) ** 2 * gaussian_random_field(n, BOX, sd, 1e-5))
+        interps.append(InterpolatorFast(g, boundary="periodic"))
+    metric = PerturbedFLRWMetricFast(cz.a_of_eta, g0, interps[0], adot_of_eta=cz.adot_of_eta,
+                                     extra_interpolators=interps[1:])
+    ph = Photons(metric)
+    origin = [cz._eta_at_a1, *OBSERVER]
+    sky = ph.generate_full_sky(n_sky, origin, seed=3)
+    patch = ph.generate_patch_grid(n_side, origin, LENS - OBSERVER, 10.0)
+    states = torch.cat([sky] + [patch] * len(seeds)).to(device).contiguous()
+    fidx = torch.cat([torch.zeros(n_sky, dtype=torch.int32)] +
+                     [torch.full((patch.shape[0],), i + 1, dtype=torch.int32) for i in range(len(seeds))]).to(device)
+    st = null_init(metric, states, -1.0, field_index=fidx)        # u^0 from each photon's own field
+    if int((st != 0).sum()):
+        raise ValueError("null initialisation failed")
+    # dt floor 1e10 s: the reference's 1e14 s floor (0.97 Mpc) would pin rejected steps at the floor, where a
+    # step that straddles a cell face (base-node gradient jump) never meets rtol, until max_iter
+    cfg = TraceConfig(stepper="rk45", tableau=tableau, precision=precision, dt=DLAMBDA, dt_min=1e10, dt_max=1e17,
+                      rtol=rtol, atol=atol, max_steps=2 ** 62, max_iter=20_000,
+                      stop_box=((0, 0, 0), (BOX, BOX, BOX)), a_stop=0.5, lens_center=tuple(LENS))
+    info = {"photons": int(states.shape[0]), "sky_photons": n_sky, "patch_photons": int(patch.shape[0]),
+            "fields": 1 + len(seeds), "grids": [main_n] + [sizes[sd % 3] for sd in seeds]}
+    return Workload("multi_field", metric, states, cfg, info, field_index=fidx)

@@ -239,6 +239,34 @@ int exc_null_error(const ExcMetric* metric, const double* state, double* rel_err
 #define EXC_NOALLOC_MAX_DEVICES 64
 int exc_trace_noalloc(const ExcMetric* metric, const ExcTraceArgs* args, void* stream);
 
+/* ---- launch-schedule autotuner (no reference counterpart: the reference has no
+ * GPU schedule). Runs exc_trace on a sample batch for each candidate (block size
+ * 32, 64, 96, 128) x (blocks per SM 1, 2, 3, 4, 6, 8 within 2048 threads per SM, and
+ * 0 = the occupancy limit) and returns the one with the highest rate. The sample's
+ * buffers are scratch: before every trial the library copies pristine_state
+ * ([n][8] float64, device) into args->state; args->dt_state must be NULL (trials
+ * start from args->dt); args->block_size / blocks_per_sm are ignored. With
+ * args->n_iter given, the rate is the sum of n_iter (steps tried) per second, so a
+ * trial may be cut short by args->deadline_cycles (a time box over a large,
+ * shuffled sample measures the steady state rather than the longest trajectory);
+ * without it the rate is 1 / elapsed time. One untimed warm-up trial precedes the
+ * timed ones. Synchronous on `stream`; allocates no device memory. */
+#define EXC_TUNE_MAX_TRIALS 32
+typedef struct ExcLaunchPlan {
+  int32_t block_size;
+  int32_t blocks_per_sm;
+  float best_ms;
+  float best_rate;          /* steps tried per second (or 1/s) of the chosen candidate */
+  int32_t n_trials;
+  int32_t trial_block[EXC_TUNE_MAX_TRIALS];
+  int32_t trial_blocks_per_sm[EXC_TUNE_MAX_TRIALS];
+  float trial_ms[EXC_TUNE_MAX_TRIALS];
+  float trial_rate[EXC_TUNE_MAX_TRIALS];
+} ExcLaunchPlan;
+
+int exc_autotune(const ExcMetric* metric, const ExcTraceArgs* args, const double* pristine_state,
+                 ExcLaunchPlan* plan, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
