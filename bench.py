@@ -58,6 +58,8 @@ def parse():
     p.add_argument("--no-surrogate", action="store_true", help="skip the learned sky-map leg")
     p.add_argument("--no-batching", action="store_true", help="skip the multi-field RK45 batching leg")
     p.add_argument("--batching-scale", type=int, default=4, help="run 1/scale of the batching configuration")
+    p.add_argument("--profile-gemm", type=int, default=0, metavar="M",
+                   help="only time the surrogate's tensor-core GEMM on M rows (for profiling) and exit")
     p.add_argument("--map-side", type=int, default=4096)
     p.add_argument("--train-steps", type=int, default=8000)
     return p.parse_args()
@@ -326,6 +328,10 @@ def run_variants(args, wl, peaks, dev, stream, main_value):
         if prec == args.precision:
             continue
         cfg = dataclasses.replace(wl.cfg, precision=prec)
+        if prec.startswith("mixed"):
+            from excalibur_tool_gb300.trace import autotune
+
+            cfg = autotune(wl.metric, wl.states, cfg, use_cache=False)    # whole-batch trials
         try:
             r = trace_batch(wl.metric, wl.states, cfg)
         except N.NativeError as e:
@@ -341,7 +347,8 @@ def run_variants(args, wl, peaks, dev, stream, main_value):
         s = e0.elapsed_time(e1) / 3e3
         steps = int(r.n_steps[r.status != N.PH_RETRACE].sum())
         out[prec] = {"photon_steps_per_s": steps / s, "rays_per_s": wl.states.shape[0] / s,
-                     f"speedup_vs_{args.precision}": steps / s / main_value}
+                     f"speedup_vs_{args.precision}": steps / s / main_value,
+                     "schedule": {"block_size": cfg.block_size, "blocks_per_sm": cfg.blocks_per_sm}}
         if prec == "mixed":
             # a stream of batches: each batch's FP64 re-traces overlap the next batches' mixed launches
             from excalibur_tool_gb300.trace import trace_pipelined
@@ -699,6 +706,13 @@ def run_reference(args, rank, world):
 
 def main():
     args = parse()
+    if args.profile_gemm:
+        import torch
+
+        dev = torch.device("cuda", 0)
+        tf, sec, fl = gemm_tflops(dev, torch.cuda.current_stream(dev), m=args.profile_gemm)
+        print(json.dumps({"gemm_tflops": tf, "ms": sec * 1e3, "flops": fl, "rows": args.profile_gemm}), flush=True)
+        return
     rank, world, local = dist_setup(args.gpus)
     if args.impl == "reference":
         run_reference(args, rank, world)

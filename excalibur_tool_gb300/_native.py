@@ -74,6 +74,17 @@ class ExcTraceArgs(C.Structure):
                 ("queue", C.c_void_p), ("abort_flag", C.c_void_p), ("deadline_cycles", C.c_int64)]
 
 
+GEN_PATCH_GRID, GEN_PATCH_POINTS, GEN_CONE_GRID, GEN_FULL_SKY = 0, 1, 2, 3
+
+
+class ExcPhotonGen(C.Structure):
+    _fields_ = [("mode", C.c_int32), ("n_side", C.c_int32), ("n_theta", C.c_int32), ("n_phi", C.c_int32),
+                ("n", C.c_int64), ("origin", C.c_double * 4), ("axis", C.c_double * 3), ("e1", C.c_double * 3),
+                ("e2", C.c_double * 3), ("half", C.c_double), ("rot_axis", C.c_double * 3), ("rot_cos", C.c_double),
+                ("rot_sin", C.c_double), ("uv", C.c_void_p), ("seed", C.c_uint64), ("speed", C.c_double),
+                ("sign", C.c_double)]
+
+
 EXC_TUNE_MAX_TRIALS = 32
 
 
@@ -112,6 +123,9 @@ EXPORTS = {
     "exc_null_error": (C.c_int, [C.POINTER(ExcMetric), C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                  C.c_int64, C.c_void_p]),
     "exc_trace_noalloc": (C.c_int, [C.POINTER(ExcMetric), C.POINTER(ExcTraceArgs), C.c_void_p]),
+    "exc_gen_count": (C.c_int64, [C.POINTER(ExcPhotonGen)]),
+    "exc_generate_photons": (C.c_int, [C.POINTER(ExcMetric), C.POINTER(ExcPhotonGen), C.c_void_p, C.c_void_p,
+                                       C.c_void_p]),
     "exc_autotune": (C.c_int, [C.POINTER(ExcMetric), C.POINTER(ExcTraceArgs), C.c_void_p,
                                C.POINTER(ExcLaunchPlan), C.c_void_p]),
     # surrogate kernels (include/excalibur_mlp.h)

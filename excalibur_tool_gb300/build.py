@@ -28,6 +28,7 @@ UNITS = {
     "exc_noalloc.cu": [],
     "exc_mlp.cu": [],
     "exc_tune.cu": [],
+    "exc_gen.cu": ["--fmad=false"],
 }
 
 

@@ -1,0 +1,115 @@
+// exc_gen.cu -- device-side photon generation (include/excalibur_gb300.h, ExcPhotonGen).
+//
+// The host generators (photon/photons.py) build millions of initial states in
+// numpy and copy them over; here each thread writes one photon's state in
+// place and the null condition then sets u^0 (exc_null_init), so a batch of
+// any size is produced in two launches with no host work. The arithmetic of
+// the patch and cone generators follows the host code operation for
+// operation, so the states agree with the host's to the last bit (patch) or
+// to the rounding of a 3-term dot product (cone).
+#include <cuda_runtime.h>
+
+#include <cmath>
+
+#include "../../include/excalibur_gb300.h"
+
+namespace exc {
+void set_last_error(const char* msg);
+}
+
+namespace {
+
+__device__ __forceinline__ uint64_t splitmix64(uint64_t x) {
+  x += 0x9E3779B97F4A7C15ull;
+  x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+  x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+  return x ^ (x >> 31);
+}
+// uniform in [0, 1) from the top 53 bits
+__device__ __forceinline__ double unit53(uint64_t x) { return (double)(x >> 11) * (1.0 / 9007199254740992.0); }
+
+__global__ void gen_kernel(const ExcPhotonGen g, int64_t n, double* states) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    double d[3];
+    if (g.mode == EXC_GEN_PATCH_GRID || g.mode == EXC_GEN_PATCH_POINTS) {
+      double A, B;
+      if (g.mode == EXC_GEN_PATCH_GRID) {
+        const int64_t ia = i / g.n_side, ib = i - ia * g.n_side;
+        A = ((double)ia + 0.5) / g.n_side * 2.0 - 1.0;
+        B = ((double)ib + 0.5) / g.n_side * 2.0 - 1.0;
+      } else {
+        A = g.uv[2 * i];
+        B = g.uv[2 * i + 1];
+      }
+      const double ah = A * g.half, bh = B * g.half;
+      for (int k = 0; k < 3; ++k) d[k] = (g.axis[k] + ah * g.e1[k]) + bh * g.e2[k];
+    } else if (g.mode == EXC_GEN_CONE_GRID) {
+      const int64_t it = i / g.n_phi, ip = i - it * g.n_phi;
+      const double th = ((double)it + 0.5) * g.half / g.n_theta;
+      const double ph = 2.0 * M_PI * (double)ip / g.n_phi;
+      const double v[3] = {sin(th) * cos(ph), sin(th) * sin(ph), cos(th)};
+      const double* k = g.rot_axis;
+      const double kv[3] = {k[1] * v[2] - k[2] * v[1], k[2] * v[0] - k[0] * v[2], k[0] * v[1] - k[1] * v[0]};
+      const double vk = (v[0] * k[0] + v[1] * k[1]) + v[2] * k[2];
+      for (int c = 0; c < 3; ++c) d[c] = (v[c] * g.rot_cos + kv[c] * g.rot_sin) + k[c] * vk * (1.0 - g.rot_cos);
+    } else {
+      // uniform on the sphere: z uniform in [-1, 1), azimuth uniform in [0, 2 pi)
+      const uint64_t h = splitmix64(g.seed ^ splitmix64((uint64_t)i));
+      const double z = 1.0 - 2.0 * unit53(h);
+      const double p = 2.0 * M_PI * unit53(splitmix64(h));
+      const double r = sqrt(fmax(0.0, 1.0 - z * z));
+      d[0] = r * cos(p);
+      d[1] = r * sin(p);
+      d[2] = z;
+    }
+    const double nrm = sqrt((d[0] * d[0] + d[1] * d[1]) + d[2] * d[2]);
+    double* s = states + i * 8;
+    s[0] = g.origin[0];
+    s[1] = g.origin[1];
+    s[2] = g.origin[2];
+    s[3] = g.origin[3];
+    s[4] = 0.0;
+    for (int k = 0; k < 3; ++k) s[5 + k] = (d[k] / nrm) * g.speed;
+  }
+}
+
+}  // namespace
+
+extern "C" int64_t exc_gen_count(const ExcPhotonGen* g) {
+  if (!g) return -1;
+  switch (g->mode) {
+    case EXC_GEN_PATCH_GRID: return (int64_t)g->n_side * g->n_side;
+    case EXC_GEN_CONE_GRID: return (int64_t)g->n_theta * g->n_phi;
+    case EXC_GEN_PATCH_POINTS:
+    case EXC_GEN_FULL_SKY: return g->n;
+    default: return -1;
+  }
+}
+
+extern "C" int exc_generate_photons(const ExcMetric* metric, const ExcPhotonGen* g, double* states, int32_t* status,
+                                    void* stream) {
+  if (!g || !states) {
+    exc::set_last_error("generate: gen and states are required");
+    return EXC_ERR_INVALID;
+  }
+  const int64_t n = exc_gen_count(g);
+  if (n < 0) {
+    exc::set_last_error("generate: unknown mode");
+    return EXC_ERR_INVALID;
+  }
+  if ((g->mode == EXC_GEN_PATCH_GRID && g->n_side < 1) || (g->mode == EXC_GEN_CONE_GRID && (g->n_theta < 1 || g->n_phi < 1)) ||
+      (g->mode == EXC_GEN_PATCH_POINTS && !g->uv)) {
+    exc::set_last_error("generate: sizes must be >= 1 (and uv given for PATCH_POINTS)");
+    return EXC_ERR_INVALID;
+  }
+  if (n == 0) return EXC_SUCCESS;
+  int64_t blocks = (n + 255) / 256;
+  if (blocks > 152 * 32) blocks = 152 * 32;
+  gen_kernel<<<(unsigned)blocks, 256, 0, (cudaStream_t)stream>>>(*g, n, states);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    exc::set_last_error(cudaGetErrorString(e));
+    return EXC_ERR_CUDA;
+  }
+  return exc_null_init(metric, states, g->sign, status, nullptr, n, stream);
+}

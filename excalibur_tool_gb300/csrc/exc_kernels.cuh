@@ -15,6 +15,7 @@
 
 #include <cooperative_groups.h>
 #include "exc_device.cuh"
+#include "exc_stepctl.h"
 
 namespace EXC_NS {
 
@@ -221,11 +222,11 @@ struct Tracer {
     const double mean = (((q[0] + q[1]) + (q[2] + q[3])) + ((q[4] + q[5]) + (q[6] + q[7]))) / 8.0;
     const double err_ratio = sqrt(mean);
     if (err_ratio <= 1.0) {
-      const double g = (err_ratio > 0.0) ? 0.9 * pow(err_ratio, -0.2) : 5.0;
+      const double g = (err_ratio > 0.0) ? 0.9 * exc_ctl_pow_m1_5(err_ratio) : 5.0;
       dt_new = dt * ((g < 5.0) ? g : 5.0);
       accepted = true;
     } else {
-      const double g = 0.9 * pow(err_ratio, -0.25);
+      const double g = 0.9 * exc_ctl_pow_m1_4(err_ratio);
       dt_new = dt * ((g > 0.1) ? g : 0.1);
       accepted = false;
     }

@@ -114,6 +114,7 @@ struct MixParams {
   df ic2d, H0, om, orad, ok, ol;
   df eta_min, inv_eta_step;
   int table_n, table_in_smem;
+  float a_stop_f;     // a_stop rounded once on the host (no FP64 conversion in the step loop)
 };
 
 // c * x with c = c.hi + c.lo, rounded once: the FMA adds the small c.lo * x to
@@ -675,7 +676,7 @@ __device__ __forceinline__ bool photon_iterate(const MixParams& Pm, const float*
     cosmo_f32(Pm, tab_s, B.ce, B.fe, a, aa, r2);
     // FP32 a(eta) carries ~3e-7 relative error; within a guard band of a_stop the
     // decision is taken on the FP64 table interpolation the reference performs.
-    const float as = (float)A.a_stop;
+    const float as = Pm.a_stop_f;
     if (a <= as * (1.0f - 1e-5f)) { P.status = EXC_PH_A_STOP; return true; }
     if (a <= as * (1.0f + 1e-5f)) {
       double a64, adot64, inv_a64;
@@ -691,7 +692,10 @@ __device__ __forceinline__ bool photon_iterate(const MixParams& Pm, const float*
   return false;
 }
 
-__global__ void __launch_bounds__(128) trace_mixed_kernel(const MixParams Pm, const ExcTraceArgs A) {
+// MINB = 1: registers as the compiler likes (144, three 128-thread blocks per SM);
+// MINB = 4: capped at 128 registers (a few spills to L1) for four blocks per SM.
+template <int MINB>
+__global__ void __launch_bounds__(128, MINB) trace_mixed_kernel(const MixParams Pm, const ExcTraceArgs A) {
   extern __shared__ float tab_s[];
   if (Pm.table_in_smem) {
     for (int i = threadIdx.x; i < Pm.table_n; i += blockDim.x) tab_s[i] = (float)__ldg(Pm.D.m.a_table + i);
@@ -792,10 +796,13 @@ cudaError_t trace(const DevMetric& D, const ExcTraceArgs& A, int block, int bloc
     P->table_in_smem = 1;
     smem = (size_t)m.a_table_n * sizeof(float);
   }
+  P->a_stop_f = (float)A.a_stop;
   int per_sm = blocks_per_sm;
+  // a plan with four or more resident blocks per SM takes the 128-register build
+  void (*kern)(const MixParams, const ExcTraceArgs) = per_sm >= 4 ? trace_mixed_kernel<4> : trace_mixed_kernel<1>;
   cudaError_t e = cudaSuccess;
   if (per_sm <= 0) {
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, trace_mixed_kernel, block, smem);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, block, smem);
     if (e != cudaSuccess) { delete P; return e; }
     if (per_sm < 1) per_sm = 1;
   }
@@ -803,7 +810,7 @@ cudaError_t trace(const DevMetric& D, const ExcTraceArgs& A, int block, int bloc
   const int64_t need = (A.n_photons + block - 1) / block;
   if (grid > need) grid = need;
   if (grid < 1) grid = 1;
-  trace_mixed_kernel<<<(int)grid, block, smem, s>>>(*P, A);
+  kern<<<(int)grid, block, smem, s>>>(*P, A);
   e = cudaGetLastError();
   delete P;
   return e;

@@ -32,8 +32,8 @@ extern "C" int exc_autotune(const ExcMetric* metric, const ExcTraceArgs* args, c
   cudaStream_t s = (cudaStream_t)stream;
   const size_t bytes = (size_t)args->n_photons * 8 * sizeof(double);
   int cand_b[EXC_TUNE_MAX_TRIALS], cand_p[EXC_TUNE_MAX_TRIALS], n = 0;
-  const int per_sm[] = {0, 1, 2, 3, 4, 6, 8};
-  for (int b = 32; b <= 128; b += 32)
+  const int per_sm[] = {0, 2, 3, 4, 5, 6, 8};
+  for (int b = 64; b <= 128; b += 32)
     for (int p : per_sm)
       if (p * b <= 2048 && n < EXC_TUNE_MAX_TRIALS) {
         cand_b[n] = b;

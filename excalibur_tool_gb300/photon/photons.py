@@ -289,6 +289,97 @@ class Photons:
         return self.generate_patch_points(np.stack([A.reshape(-1), B.reshape(-1)], 1), origin, central_direction,
                                           patch_deg, sign)
 
+    # ---- device-side generators (exc_generate_photons) --------------------
+    def _device_generate(self, gen, n):
+        import ctypes as C
+
+        import torch
+
+        from .. import _native as N
+
+        dev = torch.device("cuda", torch.cuda.current_device())
+        desc = self.metric.descriptor(dev)
+        states = torch.empty((n, 8), dtype=torch.float64, device=dev)
+        status = torch.empty(n, dtype=torch.int32, device=dev)
+        lib = N.load()
+        N.check(lib.exc_generate_photons(C.byref(desc.struct), C.byref(gen), N.ptr(states), N.ptr(status),
+                                         N.stream_handle(dev)), "exc_generate_photons")
+        if int((status != 0).sum()) != 0:
+            raise ValueError("metric evaluation failed at a photon origin (outside the grid?)")
+        self._batch.append(states)
+        self._photons = None
+        return states
+
+    def _gen_base(self, mode, origin, sign):
+        from .. import _native as N
+
+        g = N.ExcPhotonGen()
+        g.mode = mode
+        for i in range(4):
+            g.origin[i] = float(origin[i])
+        g.speed = float(c)
+        g.sign = float(sign)
+        return g
+
+    def device_patch_grid(self, n_side, origin, central_direction, patch_deg, sign=-1.0):
+        """generate_patch_grid computed on the device (bit-identical states)."""
+        from .. import _native as N
+
+        k, e1, e2 = self.patch_basis(central_direction)
+        g = self._gen_base(N.GEN_PATCH_GRID, origin, sign)
+        g.n_side = int(n_side)
+        for i in range(3):
+            g.axis[i], g.e1[i], g.e2[i] = k[i], e1[i], e2[i]
+        g.half = float(np.tan(np.deg2rad(patch_deg / 2.0)))
+        return self._device_generate(g, int(n_side) ** 2)
+
+    def device_patch_points(self, uv, origin, central_direction, patch_deg, sign=-1.0):
+        """generate_patch_points computed on the device; uv is a [n, 2] float64 device tensor."""
+        from .. import _native as N
+
+        k, e1, e2 = self.patch_basis(central_direction)
+        g = self._gen_base(N.GEN_PATCH_POINTS, origin, sign)
+        g.n = int(uv.shape[0])
+        for i in range(3):
+            g.axis[i], g.e1[i], g.e2[i] = k[i], e1[i], e2[i]
+        g.half = float(np.tan(np.deg2rad(patch_deg / 2.0)))
+        self._uv_keep = uv.contiguous()
+        g.uv = self._uv_keep.data_ptr()
+        return self._device_generate(g, g.n)
+
+    def device_polar_grid(self, n_theta, n_phi, origin, central_direction, cone_angle, sign=-1.0):
+        """generate_polar_grid (cartesian basis) computed on the device."""
+        from .. import _native as N
+
+        t = np.asarray(central_direction, dtype=float)
+        t = t / np.linalg.norm(t)
+        z = np.array([0.0, 0.0, 1.0])
+        if np.allclose(t, z):
+            kr, ca, sa = np.array([1.0, 0.0, 0.0]), 1.0, 0.0
+        elif np.allclose(t, -z):
+            kr, ca, sa = np.array([1.0, 0.0, 0.0]), -1.0, 0.0
+        else:
+            kr = np.cross(z, t)
+            kr = kr / np.linalg.norm(kr)
+            ca, sa = float(np.dot(z, t)), float(np.linalg.norm(np.cross(z, t)))
+        g = self._gen_base(N.GEN_CONE_GRID, origin, sign)
+        g.n_theta, g.n_phi = int(n_theta), int(n_phi)
+        g.half = float(cone_angle)
+        for i in range(3):
+            g.rot_axis[i] = kr[i]
+        g.rot_cos, g.rot_sin = ca, sa
+        return self._device_generate(g, int(n_theta) * int(n_phi))
+
+    def device_full_sky(self, n_photons, origin, seed, sign=-1.0):
+        """Uniform directions on the sphere from the device's counter-based generator (seeded;
+        a different stream from generate_full_sky's numpy one)."""
+        from .. import _native as N
+
+        g = self._gen_base(N.GEN_FULL_SKY, origin, sign)
+        g.n = int(n_photons)
+        g.seed = int(seed) & ((1 << 64) - 1)
+        return self._device_generate(g, g.n)
+
     def generate_full_sky(self, n_photons, origin, seed, sign=-1.0):
         """Uniform random directions on the sphere (numpy default_rng(seed))."""
         rng = np.random.default_rng(seed)

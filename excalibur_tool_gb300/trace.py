@@ -307,27 +307,29 @@ def trace_pipelined(metric, batches: Sequence, cfg: TraceConfig, *, side_stream=
 _TUNE_CACHE: dict = {}
 
 
-def autotune(metric, states, cfg: TraceConfig, *, field_index=None, sample: int = 131072, seed: int = 0,
-             time_box_cycles: int = 100_000_000, use_cache: bool = True) -> TraceConfig:
+def autotune(metric, states, cfg: TraceConfig, *, field_index=None, sample: Optional[int] = None, seed: int = 0,
+             time_box_cycles: int = 1_000_000_000, use_cache: bool = True) -> TraceConfig:
     """`cfg` with the (block_size, blocks_per_sm) that exc_autotune measured fastest.
 
-    The sample is a seeded random subset of `states` (and `field_index`) in shuffled
-    order, and each trial is time-boxed (`time_box_cycles` SM clock cycles, ~50 ms):
-    the score is steps tried per second over the box, i.e. the steady-state rate of
-    the mix, not the time of the longest trajectory. Plans are cached per device,
-    metric kind, stepper, tableau, precision, grid dtype and number of fields."""
+    By default every trial traces the whole batch (in a seeded shuffled order), so
+    the score -- steps tried per second -- includes the wave quantisation and the
+    tail of the batch as it will run; each trial is time-boxed (`time_box_cycles`
+    SM clock cycles, ~0.5 s), which turns the score into the steady-state rate for
+    batches too large to finish in the box. `sample` traces a random subset
+    instead. Plans are cached per device, metric kind, stepper, tableau,
+    precision, grid dtype, number of fields and batch size."""
     import torch
 
     dev = states.device
     desc = metric.descriptor(dev, split=cfg.precision in ("mixed", "mixed_raw", "retrace"))
     key = (torch.cuda.get_device_name(dev), desc.kind, cfg.stepper, cfg.tableau, cfg.precision,
-           int(desc.struct.fields[0].dtype), int(desc.struct.n_fields))
+           int(desc.struct.fields[0].dtype), int(desc.struct.n_fields), int(states.shape[0]))
     if use_cache and key in _TUNE_CACHE:
         b, p = _TUNE_CACHE[key][:2]
         return dataclasses.replace(cfg, block_size=b, blocks_per_sm=p)
     n = states.shape[0]
     g = torch.Generator(device="cpu").manual_seed(seed)
-    idx = torch.randperm(n, generator=g)[:min(sample, n)].to(dev)
+    idx = torch.randperm(n, generator=g)[:min(sample or n, n)].to(dev)
     pristine = states[idx].contiguous()
     fidx = field_index[idx].contiguous() if field_index is not None else None
     m = pristine.shape[0]

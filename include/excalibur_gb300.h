@@ -239,9 +239,47 @@ int exc_null_error(const ExcMetric* metric, const double* state, double* rel_err
 #define EXC_NOALLOC_MAX_DEVICES 64
 int exc_trace_noalloc(const ExcMetric* metric, const ExcTraceArgs* args, void* stream);
 
+/* ---- device-side photon generation (photon/photons.py:295-459, 540-568): initial
+ * states written on the device, then u^0 from the null condition (exc_null_init).
+ *   PATCH_GRID   n_side^2 pixel centres of a square tangent-plane patch:
+ *                d = axis + (A half) e1 + (B half) e2, A, B = (i + 1/2) / n_side * 2 - 1
+ *                (first index A), normalised.
+ *   PATCH_POINTS the same at given (A, B) = uv[i] ([n][2] float64, device).
+ *   CONE_GRID    theta_i = (i + 1/2) half / n_theta, phi_j = 2 pi j / n_phi (no on-axis ray),
+ *                (sin t cos p, sin t sin p, cos t) turned from +z onto the axis by the
+ *                Rodrigues rotation v cos + (k x v) sin + k (v . k)(1 - cos) with
+ *                rot_axis = k, rot_cos, rot_sin (the host's rotate_to_direction values).
+ *   FULL_SKY     n directions uniform on the sphere from a counter-based generator
+ *                (splitmix64 of seed and photon index; not numpy's stream).
+ * u_spatial = speed * d; origin (eta, x, y, z) for every photon; u^0 = sign * |u^0|.
+ * status ([n], optional) gets the null initialisation's status. */
+enum { EXC_GEN_PATCH_GRID = 0, EXC_GEN_PATCH_POINTS = 1, EXC_GEN_CONE_GRID = 2, EXC_GEN_FULL_SKY = 3 };
+typedef struct ExcPhotonGen {
+  int32_t mode;
+  int32_t n_side;            /* PATCH_GRID */
+  int32_t n_theta, n_phi;    /* CONE_GRID */
+  int64_t n;                 /* PATCH_POINTS, FULL_SKY */
+  double origin[4];
+  double axis[3];
+  double e1[3], e2[3];       /* PATCH_*: tangent basis */
+  double half;               /* PATCH_*: tan(patch / 2); CONE_GRID: cone half-angle (rad) */
+  double rot_axis[3];        /* CONE_GRID rotation */
+  double rot_cos, rot_sin;
+  const double* uv;          /* PATCH_POINTS */
+  uint64_t seed;             /* FULL_SKY */
+  double speed;
+  double sign;
+} ExcPhotonGen;
+
+/* Number of photons a generator produces. */
+int64_t exc_gen_count(const ExcPhotonGen* gen);
+/* states: [exc_gen_count(gen)][8] float64, device. */
+int exc_generate_photons(const ExcMetric* metric, const ExcPhotonGen* gen, double* states, int32_t* status,
+                         void* stream);
+
 /* ---- launch-schedule autotuner (no reference counterpart: the reference has no
  * GPU schedule). Runs exc_trace on a sample batch for each candidate (block size
- * 32, 64, 96, 128) x (blocks per SM 1, 2, 3, 4, 6, 8 within 2048 threads per SM, and
+ * 64, 96, 128) x (blocks per SM 2, 3, 4, 5, 6, 8 within 2048 threads per SM, and
  * 0 = the occupancy limit) and returns the one with the highest rate. The sample's
  * buffers are scratch: before every trial the library copies pristine_state
  * ([n][8] float64, device) into args->state; args->dt_state must be NULL (trials

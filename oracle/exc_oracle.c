@@ -22,6 +22,7 @@
 #include <string.h>
 
 #include "../include/excalibur_gb300.h"
+#include "../excalibur_tool_gb300/csrc/exc_stepctl.h"
 
 /* ------------------------------------------------------------ helpers */
 static double py_fmod(double a, double b) { /* CPython float_rem */
@@ -478,11 +479,11 @@ static int step_rk45(const ExcMetric* m, int fi, int tableau, const double* s, d
   }
   const double err = sqrt((((r2[0] + r2[1]) + (r2[2] + r2[3])) + ((r2[4] + r2[5]) + (r2[6] + r2[7]))) / 8);
   if (err <= 1.0) {
-    const double g = err > 0 ? 0.9 * pow(err, -0.2) : 5.0;
+    const double g = err > 0 ? 0.9 * exc_ctl_pow_m1_5(err) : 5.0;
     *dt_new = dt * (g < 5.0 ? g : 5.0);
     *accepted = 1;
   } else {
-    const double g = 0.9 * pow(err, -0.25);
+    const double g = 0.9 * exc_ctl_pow_m1_4(err);
     *dt_new = dt * (g > 0.1 ? g : 0.1);
     *accepted = 0;
     memcpy(out, s, 8 * sizeof(double)); /* a rejected trial returns the input state */

@@ -116,10 +116,11 @@ def test_struct_layout_matches_c():
 #include "excalibur_gb300.h"
 #include "excalibur_mlp.h"
 int main(void) {
-  printf("%zu %zu %zu %zu %zu %zu %zu %zu %zu %zu\n", sizeof(ExcField), sizeof(ExcMetric), sizeof(ExcTraceArgs),
-         offsetof(ExcMetric, fields), offsetof(ExcTraceArgs, dt), offsetof(ExcTraceArgs, queue),
+  printf("%zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu\n", sizeof(ExcField), sizeof(ExcMetric),
+         sizeof(ExcTraceArgs), offsetof(ExcMetric, fields), offsetof(ExcTraceArgs, dt), offsetof(ExcTraceArgs, queue),
          offsetof(ExcTraceArgs, deadline_cycles), sizeof(ExcGemm), offsetof(ExcGemm, bias),
-         offsetof(ExcGemm, stride_ct));
+         offsetof(ExcGemm, stride_ct), sizeof(ExcPhotonGen), offsetof(ExcPhotonGen, uv), sizeof(ExcLaunchPlan),
+         offsetof(ExcLaunchPlan, trial_rate));
   return 0;
 }
 '''
@@ -131,5 +132,6 @@ int main(void) {
         got = [int(v) for v in subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split()]
     want = [C.sizeof(N.ExcField), C.sizeof(N.ExcMetric), C.sizeof(N.ExcTraceArgs), N.ExcMetric.fields.offset,
             N.ExcTraceArgs.dt.offset, N.ExcTraceArgs.queue.offset, N.ExcTraceArgs.deadline_cycles.offset,
-            C.sizeof(N.ExcGemm), N.ExcGemm.bias.offset, N.ExcGemm.stride_ct.offset]
+            C.sizeof(N.ExcGemm), N.ExcGemm.bias.offset, N.ExcGemm.stride_ct.offset, C.sizeof(N.ExcPhotonGen),
+            N.ExcPhotonGen.uv.offset, C.sizeof(N.ExcLaunchPlan), N.ExcLaunchPlan.trial_rate.offset]
     assert got == want

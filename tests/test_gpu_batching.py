@@ -31,15 +31,12 @@ def _spec(wl):
 
 
 def test_multi_field_rk45_matches_oracle(cuda):
-    """Full-sky rays through the lens grid and patch rays through three random fields, one launch.
-
-    Adaptive stepping does not keep bit-parity over long runs: the step-size factor
-    err^-0.2 goes through pow, whose last-ulp results differ between CUDA and glibc,
-    and err itself is a ratio of the small difference y5 - y4, so one ulp in a state
-    becomes ~1e-9 in the next step size. Trajectories therefore part at the
-    integrator's own tolerance level (rtol = 1e-8); the test holds the statuses, the
-    typical state difference and the deflection to that level. Single RK45 steps
-    match the oracle to the last bits (test_gpu_parity)."""
+    """Full-sky rays through the lens grid and patch rays through three random fields, one launch,
+    against the C oracle: the same accepted/rejected step sequence for every ray (the controller's
+    err**-0.2 / err**-0.25 come from the shared IEEE-only routine in csrc/exc_stepctl.h, so no libm
+    ulp separates the two), states bit-identical or within 1e-12 for all but a few rays; on those,
+    a last-ulp difference of adot (the GPU's correctly rounded cube against libm's pow) enters the
+    error estimate y5 - y4 and is amplified by the step-size control to ~1e-8."""
     import torch
     from excalibur_tool_gb300.observables.lensing import deflection_angle
     from excalibur_tool_gb300.trace import trace_batch
@@ -51,10 +48,12 @@ def test_multi_field_rk45_matches_oracle(cuda):
     o = O.trace(_spec(wl), states, wl.cfg, field_index=wl.field_index.cpu().numpy(), threads=8)
     steps = r.n_steps.cpu().numpy()
     assert np.array_equal(r.status.cpu().numpy(), o.status)
-    assert np.median(np.abs(steps - o.n_steps)) <= 1
-    assert np.median(rel_err(r.state.cpu().numpy()[:, :4], o.state[:, :4]).max(axis=1)) <= 1e-7
+    assert np.array_equal(steps, o.n_steps)
+    assert np.array_equal(r.n_iter.cpu().numpy(), o.n_iter)
+    per_ray = rel_err(r.state.cpu().numpy(), o.state).max(axis=1)
+    assert (per_ray <= 1e-12).mean() >= 0.95 and per_ray.max() <= 1e-6
     a_gpu, a_ref = deflection_angle(r.obs.cpu().numpy()), deflection_angle(o.obs)
-    assert (np.abs(a_gpu - a_ref) <= 1e-3 * np.abs(a_ref) + 1e-8).all()
+    assert (np.abs(a_gpu - a_ref) <= 1e-6 * np.abs(a_ref) + 1e-15).all()
     assert steps.max() > 5 * np.median(steps[steps > 1])       # uneven trajectory lengths in one launch
 
 
@@ -67,7 +66,7 @@ def test_autotune_and_graph_replay_reproduce_the_launch(cuda):
     ref = trace_batch(wl.metric, wl.states, wl.cfg, field_index=wl.field_index)
     tuned = autotune(wl.metric, wl.states, wl.cfg, field_index=wl.field_index, sample=1024, use_cache=False)
     assert tune_report()  # plan recorded
-    assert tuned.block_size in (32, 64, 96, 128) and tuned.blocks_per_sm in (0, 1, 2, 3, 4, 6, 8)
+    assert tuned.block_size in (64, 96, 128) and tuned.blocks_per_sm in (0, 2, 3, 4, 5, 6, 8)
     rep = next(iter(tune_report().values()))
     assert len(rep["trials"]) >= 20 and rep["best_rate"] > 0
     cap = CapturedTrace(wl.metric, wl.states, tuned, field_index=wl.field_index)

@@ -110,3 +110,37 @@ def test_exit_geometry_crossing():
     assert axc[0] == 0 and np.isclose(eta_c[0], 7.0 - 0.15 * 4.0)
     assert np.allclose(x_c[0], [10.0, 5.85, 5.0])
     assert ExitGeometry.in_face(np.array([0, 1, 2])).tolist() == [[1, 2], [2, 0], [0, 1]]
+
+
+def test_step_controller_powers_match_libm():
+    """The RK45 controller's err^(-1/5), err^(-1/4) (IEEE basic ops only) against libm pow."""
+    import os
+    import subprocess
+    import tempfile
+
+    from conftest import ROOT
+
+    src = r"""
+#include <stdio.h>
+#include <stdlib.h>
+#include "exc_stepctl.h"
+int main(void) {
+  double x;
+  while (scanf("%lf", &x) == 1) printf("%.17g %.17g\n", exc_ctl_pow_m1_5(x), exc_ctl_pow_m1_4(x));
+  return 0;
+}
+"""
+    rng = np.random.default_rng(0)
+    xs = np.concatenate([10.0 ** rng.uniform(-300, 300, 2000), rng.uniform(0.5, 2.0, 2000), [1.0, 2.0, 1e-320]])
+    with tempfile.TemporaryDirectory() as d:
+        c = os.path.join(d, "p.c")
+        open(c, "w").write(src)
+        exe = os.path.join(d, "p")
+        subprocess.run(["gcc", "-O2", "-ffp-contract=off", "-I", os.path.join(ROOT, "excalibur_tool_gb300", "csrc"),
+                        c, "-o", exe, "-lm"], check=True)
+        out = subprocess.run([exe], input="\n".join(repr(float(v)) for v in xs), capture_output=True, text=True,
+                             check=True).stdout.split()
+    got = np.array(out, dtype=float).reshape(-1, 2)
+    for col, p in ((0, -0.2), (1, -0.25)):
+        want = xs ** p
+        assert (np.abs(got[:, col] - want) <= 4e-16 * np.abs(want)).all(), col
