@@ -549,7 +549,7 @@ def run_surrogate(args, dev, stream, peaks, fp64_rays_s):
     cz = workloads.lcdm()
     patch = Patch((cz._eta_at_a1, *workloads.OBSERVER), tuple(workloads.LENS - workloads.OBSERVER), 20.0)
     n_train = 1 << 20
-    uv, y, info = training_set(wl.metric, patch, n_train, cfg, seed=1)
+    uv, y, feats, info = training_set(wl.metric, patch, n_train, cfg, seed=1)
     tracer_rays_s = n_train / info["trace_s"]
     model = SkySurrogate(n_members=4, n_out=y.shape[1], seed=0, device=dev)
     rep = model.fit(uv, y, steps=args.train_steps, batch=8192, lr=2e-3, log_every=1000)

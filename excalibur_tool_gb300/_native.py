@@ -105,6 +105,12 @@ class ExcGemm(C.Structure):
 
 EPI_F32, EPI_BIAS_SILU, EPI_DSILU, EPI_SPLITK = 0, 1, 2, 3
 
+
+class ExcBornArgs(C.Structure):
+    _fields_ = [("n", C.c_int64), ("uv", C.c_void_p), ("origin", C.c_double * 3), ("axis", C.c_double * 3),
+                ("e1", C.c_double * 3), ("e2", C.c_double * 3), ("half", C.c_double), ("box_lo", C.c_double * 3),
+                ("box_hi", C.c_double * 3), ("step", C.c_double), ("c", C.c_double), ("out", C.c_void_p)]
+
 _V = C.c_void_p
 EXPORTS = {
     "exc_abi_version": (C.c_int, []),
@@ -139,6 +145,7 @@ EXPORTS = {
     "exc_mlp_adam": (C.c_int, [_V, _V, _V, _V, C.c_int64, C.c_float, C.c_float, C.c_float, C.c_float, C.c_int32,
                                _V, _V, C.c_int32, C.c_int32, _V]),
     "exc_mlp_error_count": (C.c_int, [C.POINTER(C.c_uint32)]),
+    "exc_born_patch": (C.c_int, [C.POINTER(ExcMetric), C.POINTER(ExcBornArgs), _V]),
 }
 
 _lib = None

@@ -29,6 +29,7 @@ UNITS = {
     "exc_mlp.cu": [],
     "exc_tune.cu": [],
     "exc_gen.cu": ["--fmad=false"],
+    "exc_born.cu": [],
 }
 
 

@@ -28,9 +28,14 @@ from . import kernels as K
 N_OUT_MAX = 8
 
 
-def _baseline_design(uv: np.ndarray) -> np.ndarray:
+def _baseline_design(uv: np.ndarray, extra: Optional[np.ndarray] = None) -> np.ndarray:
+    """Columns of the least-squares baseline: a quadratic in (u, v) plus optional
+    per-direction features (e.g. first-order line integrals along the ray)."""
     u, v = uv[:, 0], uv[:, 1]
-    return np.stack([np.ones_like(u), u, v, u * u, u * v, v * v], 1)
+    cols = [np.ones_like(u), u, v, u * u, u * v, v * v]
+    if extra is not None:
+        cols += [extra[:, k] for k in range(extra.shape[1])]
+    return np.stack(cols, 1)
 
 
 @dataclasses.dataclass
@@ -66,6 +71,7 @@ class SkySurrogate:
         self.b_head = torch.zeros(self.E, n_out, device=self.device)
         self._sync_bf16()
         self.baseline = np.zeros((6, n_out))
+        self.n_extra = 0
         self.t_mean = np.zeros(n_out)
         self.t_std = np.ones(n_out)
         self._adam = None
@@ -90,18 +96,19 @@ class SkySurrogate:
         return x
 
     # ------------------------------------------------------------ targets
-    def set_normalisation(self, uv: np.ndarray, targets: np.ndarray):
-        A = _baseline_design(uv)
-        self.baseline, *_ = np.linalg.lstsq(A, targets, rcond=None)
+    def set_normalisation(self, uv: np.ndarray, targets: np.ndarray, extra: Optional[np.ndarray] = None):
+        A = _baseline_design(uv, extra)
+        # columns scaled to unit norm for the solve (the features span many decades)
+        self._col_scale = np.maximum(np.linalg.norm(A, axis=0), 1e-300)
+        coef, *_ = np.linalg.lstsq(A / self._col_scale, targets, rcond=None)
+        self.baseline = coef / self._col_scale[:, None]
+        self.n_extra = 0 if extra is None else extra.shape[1]
         resid = targets - A @ self.baseline
         self.t_mean = resid.mean(0)
         self.t_std = resid.std(0) + 1e-300
 
-    def _normalise(self, uv: np.ndarray, targets: np.ndarray) -> np.ndarray:
-        return ((targets - _baseline_design(uv) @ self.baseline - self.t_mean) / self.t_std).astype(np.float32)
-
-    def _denormalise(self, uv: np.ndarray, y: np.ndarray) -> np.ndarray:
-        return y.astype(np.float64) * self.t_std + self.t_mean + _baseline_design(uv) @ self.baseline
+    def _normalise(self, uv: np.ndarray, targets: np.ndarray, extra: Optional[np.ndarray] = None) -> np.ndarray:
+        return ((targets - _baseline_design(uv, extra) @ self.baseline - self.t_mean) / self.t_std).astype(np.float32)
 
     # ------------------------------------------------------------ training
     def _buffers(self, B: int, k_splits: int = 32):
@@ -151,8 +158,11 @@ class SkySurrogate:
                 K.gemm(dZ[l], self.wtb[l], epilogue="dsilu", z_in=Z[l - 1], c=dZ[l - 1], ct=dZT[l - 1])
 
     def fit(self, uv: np.ndarray, targets: np.ndarray, steps: int = 3000, batch: int = 8192, lr: float = 2e-3,
-            lr_final: float = 2e-5, seed: int = 1, k_splits: int = 32, log_every: int = 100) -> TrainReport:
-        """Train every member on (uv [n, 2] in [-1, 1]^2, targets [n, 4]) with Adam and a cosine schedule."""
+            lr_final: float = 2e-5, seed: int = 1, k_splits: int = 32, log_every: int = 100,
+            extra: Optional[np.ndarray] = None) -> TrainReport:
+        """Train every member on (uv [n, 2] in [-1, 1]^2, targets [n, n_out]) with Adam and a cosine
+        schedule; `extra` [n, k] are per-direction baseline features (the same must be given to
+        prediction)."""
         import time
 
         import torch
@@ -160,10 +170,10 @@ class SkySurrogate:
         if batch % 128:
             raise ValueError("batch must be a multiple of 128")
         n = uv.shape[0]
-        self.set_normalisation(uv, targets)
+        self.set_normalisation(uv, targets, extra)
         dev = self.device
         uv_d = torch.as_tensor(np.ascontiguousarray(uv, dtype=np.float64), device=dev)
-        t_d = torch.as_tensor(self._normalise(uv, targets), device=dev)
+        t_d = torch.as_tensor(self._normalise(uv, targets, extra), device=dev)
         B = batch
         buf = self._buffers(B, k_splits)
         if self._adam is None:
@@ -198,9 +208,10 @@ class SkySurrogate:
         return TrainReport(steps, B, curve[-1][1] if curve else [], secs, curve)
 
     # ------------------------------------------------------------ inference
-    def predict_members(self, uv, out=None):
+    def predict_members(self, uv, extra=None):
         """Every member's outputs [E, m, n_out] (physical units, float64, on the device) for
-        directions uv ([m, 2] float64 device tensor)."""
+        directions uv ([m, 2] float64 device tensor) and their baseline features `extra`
+        ([m, k] device tensor, as given to fit)."""
         import torch
 
         m = uv.shape[0]
@@ -217,20 +228,28 @@ class SkySurrogate:
         K.head(inp, self.w_head, self.b_head, y=y)
         # undo the target normalisation (six-term quadratic baseline + per-output scale)
         u, v = uv[:, 0], uv[:, 1]
-        design = torch.stack([torch.ones_like(u), u, v, u * u, u * v, v * v], 1)
+        cols = [torch.ones_like(u), u, v, u * u, u * v, v * v]
+        if self.n_extra:
+            if extra is None or extra.shape[1] != self.n_extra:
+                raise ValueError(f"this model was fitted with {self.n_extra} baseline features")
+            cols += [extra[:, k].double() for k in range(self.n_extra)]
+        design = torch.stack(cols, 1)
         base = design @ torch.as_tensor(self.baseline, device=dev)
         scale = torch.as_tensor(self.t_std, device=dev)
         shift = torch.as_tensor(self.t_mean, device=dev)
         return y[:, :m].double() * scale + shift + base[None]
 
-    def predict(self, uv: np.ndarray, chunk: int = 1 << 20, return_members: bool = False):
+    def predict(self, uv: np.ndarray, chunk: int = 1 << 20, return_members: bool = False,
+                extra: Optional[np.ndarray] = None):
         """Ensemble mean and standard deviation [n, n_out] (physical units) for directions uv [n, 2]."""
         import torch
 
         means, stds, mems = [], [], []
         for s in range(0, uv.shape[0], chunk):
             uvd = torch.as_tensor(np.ascontiguousarray(uv[s:s + chunk], dtype=np.float64), device=self.device)
-            y = self.predict_members(uvd)
+            ex = None if extra is None else torch.as_tensor(np.ascontiguousarray(extra[s:s + chunk]),
+                                                            device=self.device)
+            y = self.predict_members(uvd, ex)
             means.append(y.mean(0).cpu().numpy())
             stds.append(y.std(0, unbiased=False).cpu().numpy())
             if return_members:

@@ -92,6 +92,35 @@ int exc_mlp_row_sums(const void* x, int64_t rows, int64_t m, int64_t ld, float* 
 int exc_mlp_adam(float* p, const float* grad, float* m1, float* m2, int64_t n, float lr, float beta1, float beta2,
                  float eps, int32_t t, void* p_bf16, void* pt_bf16, int32_t rows, int32_t cols, void* stream);
 
+/* First-order (Born) line integrals along the straight rays of a tangent-plane
+ * patch, the baseline features of the sky-map surrogate. For ray i, d = unit(axis
+ * + uv[i][0] half e1 + uv[i][1] half e2) from origin (x, y, z) to the first face of
+ * [box_lo, box_hi) at distance L, sampled at the midpoints of n = ceil(L / step)
+ * equal segments with the field's trilinear Phi and base-node gradient (FP32):
+ *   out[i][0] = -(2 / c^3) sum Phi dl                        (Shapiro delay, s)
+ *   out[i][1..2] = D . e1, D . e2,  D = -(2 / c^2) sum (L - l) grad_perp Phi dl  (m)
+ *   out[i][3] = tau_B = (S2 - |S1|^2 / L) / (2 c),  theta(l) = -(2 / c^2) int_0^l grad_perp Phi,
+ *               S1 = sum theta dl, S2 = sum |theta|^2 dl       (geometric delay, s)
+ *   out[i][4..5] = theta(L) . e1, theta(L) . e2              (deflection, rad)
+ *   out[i][6..7] = -(2 / c^3) sum Phi (l / L)^k dl, k = 1, 2   (moments of the delay integrand)
+ * grad_perp = the gradient minus its component along d. Field 0 of the metric
+ * (float64, float32 or float32x2; periodic, clamp or error boundary: samples
+ * outside an error-mode interior are skipped). out: [n][8] float64, device. */
+typedef struct ExcBornArgs {
+  int64_t n;
+  const double* uv;
+  double origin[3];
+  double axis[3], e1[3], e2[3];
+  double half;
+  double box_lo[3], box_hi[3];
+  double step;          /* segment length (m) */
+  double c;
+  double* out;
+} ExcBornArgs;
+
+struct ExcMetric;
+int exc_born_patch(const struct ExcMetric* metric, const ExcBornArgs* args, void* stream);
+
 /* Number of GEMM launches whose bounded tensor-core waits ran out since the
  * library was loaded (0 in a healthy run; such a launch leaves its outputs
  * unwritten). Synchronous: copies one word from the device. */

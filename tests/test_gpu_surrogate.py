@@ -58,24 +58,31 @@ def test_sky_map_pipeline_small(cuda):
     """Train on rays of a 32^3 lens + random field, fill a 128^2 map, audit it."""
     from excalibur_tool_gb300 import workloads
     from excalibur_tool_gb300.surrogate.model import SkySurrogate
-    from excalibur_tool_gb300.surrogate.sky import (ExitGeometry, Patch, compose, fill_sky_map, observer_terms,
-                                                    traced_quantities, training_set)
+    from excalibur_tool_gb300.surrogate.sky import (ExitGeometry, Patch, born_features, compose, fill_sky_map,
+                                                    observer_terms, traced_quantities, training_set)
 
     wl = workloads.flrw_patch(32, 2, device="cuda")
     cfg = dataclasses.replace(wl.cfg, precision="mixed")
     cz = workloads.lcdm()
     patch = Patch((cz._eta_at_a1, *workloads.OBSERVER), tuple(workloads.LENS - workloads.OBSERVER), 10.0)
-    uv, y, info = training_set(wl.metric, patch, 32768, cfg, seed=1)
-    assert info["kept"] == 32768 and y.shape == (32768, 6)
+    uv, y, feats, info = training_set(wl.metric, patch, 32768, cfg, seed=1)
+    assert info["kept"] == 32768 and y.shape == (32768, 6) and feats.shape == (32768, 8)
     m = SkySurrogate(n_members=4, n_out=6, seed=0)
-    rep = m.fit(uv, y, steps=400, batch=4096, lr=2e-3, log_every=50)
+    rep = m.fit(uv, y, steps=400, batch=4096, lr=2e-3, log_every=50, extra=feats)
     first, last = rep.loss_curve[0][1], rep.loss_curve[-1][1]
     assert all(l1 < 0.3 * l0 for l0, l1 in zip(first, last)), (first, last)
     # held-out rays: the composed redshift tracks the traced one far better than the straight line does
     geo = ExitGeometry(patch, cfg.stop_box)
     hold = np.random.default_rng(9).uniform(-1, 1, (2048, 2))
-    _, ref = traced_quantities(wl.metric, patch, hold, cfg, geo)
-    mean, _ = m.predict(hold)
+    learned_ref, ref = traced_quantities(wl.metric, patch, hold, cfg, geo)
+    import torch
+
+    hf = born_features(wl.metric, patch, torch.as_tensor(hold, device="cuda"), cfg.stop_box).cpu().numpy()
+    # the first-order line integrals explain the deflection and the exit offsets
+    for j, col in ((1, 0), (2, 1), (4, 4), (5, 5)):
+        cc = np.corrcoef(hf[:, j], learned_ref[:, col])[0, 1]
+        assert abs(cc) > 0.9, (j, cc)
+    mean, _ = m.predict(hold, extra=hf)
     terms = observer_terms(wl.metric, patch)
     pred = compose(wl.metric, patch, geo, hold, mean, terms)
     straight = compose(wl.metric, patch, geo, hold, np.zeros_like(mean), terms)

@@ -144,3 +144,21 @@ int main(void) {
     for col, p in ((0, -0.2), (1, -0.25)):
         want = xs ** p
         assert (np.abs(got[:, col] - want) <= 4e-16 * np.abs(want)).all(), col
+
+
+def test_trajectory_file_layout(tmp_path):
+    """Stacked NaN-padded trajectories written like the runners (npz when h5py is absent)."""
+    from excalibur_tool_gb300.records import write_trajectories
+
+    traj = np.full((3, 5, 14), np.nan)
+    traj[0, :5] = 1.0
+    traj[1, :2] = 2.0
+    p = write_trajectories(str(tmp_path / "out" / "run.h5"), traj, {"mass_kg": 1.5, "label": "x"})
+    if p.endswith(".npz"):
+        z = np.load(p)
+        assert np.array_equal(z["trajectories"], traj, equal_nan=True) and float(z["mass_kg"]) == 1.5
+    else:
+        import h5py
+
+        with h5py.File(p) as f:
+            assert np.array_equal(f["trajectories"][()], traj, equal_nan=True) and f.attrs["mass_kg"] == 1.5
