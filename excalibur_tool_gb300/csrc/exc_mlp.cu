@@ -1,15 +1,15 @@
 // exc_mlp.cu -- kernels of the sky-map surrogate (include/excalibur_mlp.h).
 //
-// The GEMM is a Blackwell tensor-core kernel: operand tiles are staged in
-// shared memory in the UMMA canonical K-major layout (8-row x 16-byte core
-// matrices, no swizzle), one elected thread issues tcgen05.mma (kind::f16,
-// BF16 x BF16 -> FP32) into a 128 x N accumulator in tensor memory, the
-// completion is signalled through tcgen05.commit on an mbarrier, and the four
-// warps read their 32-lane slices back with tcgen05.ld for the fused
-// epilogue. Shared-memory stages are double-buffered so that the loads of
-// chunk k+1 overlap the MMAs of chunk k. Every wait is bounded; a timeout is
+// The GEMM is a Blackwell tensor-core kernel: one thread streams 64-wide K
+// chunks of both operands into a ring of shared-memory stages with TMA
+// (cp.async.bulk.tensor, 128-byte swizzle, completion counted in bytes on an
+// mbarrier), a second thread issues tcgen05.mma (kind::f16, BF16 x BF16 -> FP32)
+// into a 128 x N accumulator in tensor memory and frees each stage with
+// tcgen05.commit, and the four warps read their 32-lane slices back with
+// tcgen05.ld for the fused epilogue. Every wait is bounded; a timeout is
 // counted in a device word the host can read (exc_mlp_error_count) and the
 // kernel still releases its tensor memory.
+#include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -30,24 +30,10 @@ constexpr int kChunkK = 64;                      // K elements per shared-memory
 constexpr int kStageA = kTileM * kChunkK * 2;    // 16 KB
 constexpr int kStageB = 256 * kChunkK * 2;       // 32 KB (N <= 256)
 constexpr int kStage = kStageA + kStageB;
-constexpr int kStages = 2;
-constexpr int kSmem = kStages * kStage;          // 96 KB: at most two CTAs per SM, 2 x 256 TMEM columns
 constexpr uint32_t kTmemCols = 256;
 constexpr long long kSpinLimit = 1ll << 24;      // try_wait polls before a wait is declared lost
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-// UMMA shared-memory descriptor for a K-major operand without swizzle:
-// start address, leading byte offset (between K-adjacent core matrices) and
-// stride byte offset (between 8-row groups), all in 16-byte units; bits 46-47
-// hold the descriptor version of the sm_100 family (1); layout type 0.
-__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
-  uint64_t d = (uint64_t)((addr >> 4) & 0x3FFFu);
-  d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
-  d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
-  d |= (uint64_t)1 << 46;
-  return d;
-}
 
 // Instruction descriptor, kind::f16: D format F32 (bits 4-5 = 1), A and B
 // format BF16 (bits 7-9 = 1, 10-12 = 1), both K-major (bits 15, 16 = 0),
@@ -117,160 +103,239 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
   for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
-__device__ __forceinline__ float sigmoid(float z) { return 1.0f / (1.0f + __expf(-z)); }
+// BF16 outputs: the fast exponential and division intrinsics are ample
+__device__ __forceinline__ float sigmoid(float z) { return __fdividef(1.0f, 1.0f + __expf(-z)); }
 
-// Stage one K chunk of A (128 rows from m0) and B (n rows) into the canonical
-// K-major layout: element (r, k) at (r / 8) * 1024 + (k / 8) * 128 + (r % 8) * 16 + (k % 8) * 2.
-__device__ __forceinline__ void load_stage(uint8_t* sA, uint8_t* sB, const __nv_bfloat16* A, const __nv_bfloat16* B,
-                                           int64_t m0, int64_t m, int n, int k, int k0) {
-  const int t = threadIdx.x;
-  for (int v = t; v < kTileM * 8; v += blockDim.x) {
-    const int r = v >> 3, kv = v & 7;
-    uint4 val = make_uint4(0u, 0u, 0u, 0u);
-    if (m0 + r < m) val = __ldg(reinterpret_cast<const uint4*>(A + (m0 + r) * (int64_t)k + k0 + kv * 8));
-    *reinterpret_cast<uint4*>(sA + (r >> 3) * 1024 + kv * 128 + (r & 7) * 16) = val;
+// TMA: one 3-D tile (x = K element, y = row, z = batch member) into shared memory,
+// completion counted in bytes on an mbarrier. The tensor map lives in the kernel's
+// parameter space (__grid_constant__); its generic address is what the
+// instruction takes.
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, int x, int y, int z, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];"
+      ::"r"(smem_u32(dst)), "l"((uint64_t)map), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+
+// UMMA shared-memory descriptor for a K-major operand in the 128-byte swizzled
+// layout TMA writes (rows of 128 B = 64 BF16, 8-row atoms of 1024 B): stride byte
+// offset 1024 B between 8-row groups, leading byte offset unused (16 B), descriptor
+// version 1 (bits 46-47), layout type 2 = SWIZZLE_128B (bits 61-63). A K step of 16
+// elements inside the 128-byte row advances the start address by 32 B; the stage
+// base is 1024-byte aligned so the hardware swizzle lines up with TMA's.
+__device__ __forceinline__ uint64_t smem_desc_sw128(uint32_t addr) {
+  uint64_t d = (uint64_t)((addr >> 4) & 0x3FFFu);
+  d |= (uint64_t)1 << 16;
+  d |= (uint64_t)(1024 >> 4) << 32;
+  d |= (uint64_t)1 << 46;
+  d |= (uint64_t)2 << 61;
+  return d;
+}
+
+constexpr int kTmaStages = 4;                          // K chunks in flight (192 KB: one CTA per SM)
+constexpr int kTmaSmem = kTmaStages * kStage + 1024;  // + alignment slack
+
+// Fused epilogue, staged through shared memory, on all kGemmWarps warps. A warp
+// can read only its quarter of the TMEM lanes (warp w: lanes 32 (w % 4) ..), so
+// the four warps of a quarter split the 16-column chunks among them (chunk j to
+// warp group j % 4). Pass 1: each thread reads its lane (tile row) chunk by
+// chunk, applies the epilogue and writes the results into row-major tiles in
+// shared memory (the operand stages are free once the last MMA has completed).
+// Pass 2: the warps copy the tiles out with coalesced stores -- one whole
+// output row per warp instruction, and the transposed output one column (up to
+// 128 consecutive rows of ct) per pass. Row pitch: 264 BF16 / 260 FP32 elements.
+constexpr int kPitchH = 264, kPitchF = 260;
+constexpr int kGemmWarps = 16;
+
+template <int EPI>
+__device__ __forceinline__ void epilogue(const ExcGemm& g, uint32_t tmem, int64_t m0, int split, int splits, int bidx,
+                                         uint8_t* smem, const float* sbias) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int q = warp & 3, grp = warp >> 2;
+  const int n = g.n;
+  const int r = q * 32 + lane;
+  const int64_t row = m0 + r;
+  const uint32_t lane_addr = tmem + ((uint32_t)(q * 32) << 16);
+  float* tf = reinterpret_cast<float*>(smem);                                   // FP32 tile
+  __nv_bfloat16* t1 = reinterpret_cast<__nv_bfloat16*>(smem);                   // first BF16 tile
+  __nv_bfloat16* t2 = t1 + kTileM * kPitchH;                                    // second BF16 tile
+  const __nv_bfloat16* Z =
+      EPI == EXC_EPI_DSILU ? reinterpret_cast<const __nv_bfloat16*>(g.z_in) + bidx * g.stride_c + row * n : nullptr;
+  // pass 1
+  for (int c0 = grp * 16; c0 < n; c0 += 16 * (kGemmWarps / 4)) {
+    float v[16];
+    tmem_ld16(lane_addr + (uint32_t)c0, v);
+    if (EPI == EXC_EPI_F32 || EPI == EXC_EPI_SPLITK) {
+#pragma unroll
+      for (int i = 0; i < 16; i += 4)
+        *reinterpret_cast<float4*>(tf + r * kPitchF + c0 + i) = make_float4(v[i], v[i + 1], v[i + 2], v[i + 3]);
+    } else if (EPI == EXC_EPI_BIAS_SILU) {
+      const float* bias = sbias + c0;
+      __align__(16) __nv_bfloat16 zb[16], hb[16];
+#pragma unroll
+      for (int i = 0; i < 16; ++i) {
+        const float z = v[i] + bias[i];
+        zb[i] = __float2bfloat16_rn(z);
+        const float zr = __bfloat162float(zb[i]);   // the value the backward pass will see
+        hb[i] = __float2bfloat16_rn(zr * sigmoid(zr));
+      }
+      uint4* d1 = reinterpret_cast<uint4*>(t1 + r * kPitchH + c0);
+      uint4* d2 = reinterpret_cast<uint4*>(t2 + r * kPitchH + c0);
+      d1[0] = *reinterpret_cast<uint4*>(&zb[0]);
+      d1[1] = *reinterpret_cast<uint4*>(&zb[8]);
+      d2[0] = *reinterpret_cast<uint4*>(&hb[0]);
+      d2[1] = *reinterpret_cast<uint4*>(&hb[8]);
+    } else {  // EXC_EPI_DSILU
+      __align__(16) __nv_bfloat16 db[16];
+      if (row < g.m) {
+        __align__(16) __nv_bfloat16 zin[16];
+        *reinterpret_cast<uint4*>(&zin[0]) = __ldg(reinterpret_cast<const uint4*>(Z + c0));
+        *reinterpret_cast<uint4*>(&zin[8]) = __ldg(reinterpret_cast<const uint4*>(Z + c0 + 8));
+#pragma unroll
+        for (int i = 0; i < 16; ++i) {
+          const float z = __bfloat162float(zin[i]);
+          const float sg = sigmoid(z);
+          db[i] = __float2bfloat16_rn(v[i] * (sg * (1.0f + z * (1.0f - sg))));
+        }
+      } else {
+#pragma unroll
+        for (int i = 0; i < 16; ++i) db[i] = __float2bfloat16_rn(0.0f);
+      }
+      uint4* d1 = reinterpret_cast<uint4*>(t1 + r * kPitchH + c0);
+      d1[0] = *reinterpret_cast<uint4*>(&db[0]);
+      d1[1] = *reinterpret_cast<uint4*>(&db[8]);
+    }
   }
-  for (int v = t; v < n * 8; v += blockDim.x) {
-    const int r = v >> 3, kv = v & 7;
-    const uint4 val = __ldg(reinterpret_cast<const uint4*>(B + (int64_t)r * k + k0 + kv * 8));
-    *reinterpret_cast<uint4*>(sB + (r >> 3) * 1024 + kv * 128 + (r & 7) * 16) = val;
+  __syncthreads();
+  // pass 2: rows (coalesced), warp w handles rows w, w + kGemmWarps, ...
+  const int rows = (int)(g.m - m0 < kTileM ? g.m - m0 : kTileM);
+  if (EPI == EXC_EPI_F32 || EPI == EXC_EPI_SPLITK) {
+    float* C = reinterpret_cast<float*>(g.c) +
+               (EPI == EXC_EPI_SPLITK ? ((int64_t)bidx * splits + split) * g.m * n : bidx * g.stride_c);
+    for (int rr = warp; rr < rows; rr += kGemmWarps)
+      for (int c = lane * 4; c < n; c += 128)
+        *reinterpret_cast<float4*>(C + (m0 + rr) * n + c) = *reinterpret_cast<const float4*>(tf + rr * kPitchF + c);
+  } else {
+    __nv_bfloat16* outs[2] = {reinterpret_cast<__nv_bfloat16*>(g.c), EPI == EXC_EPI_BIAS_SILU
+                                                                        ? reinterpret_cast<__nv_bfloat16*>(g.c2)
+                                                                        : nullptr};
+    const __nv_bfloat16* tiles[2] = {t1, t2};
+    for (int o = 0; o < 2; ++o) {
+      if (!outs[o]) continue;
+      __nv_bfloat16* C = outs[o] + bidx * g.stride_c;
+      for (int rr = warp; rr < rows; rr += kGemmWarps)
+        for (int c = lane * 8; c < n; c += 256)
+          *reinterpret_cast<uint4*>(C + (m0 + rr) * n + c) = *reinterpret_cast<const uint4*>(tiles[o] + rr * kPitchH + c);
+    }
+    if (g.ct) {
+      // the transposed output: SiLU values (BIAS_SILU) or the masked gradient (DSILU)
+      const __nv_bfloat16* src = EPI == EXC_EPI_BIAS_SILU ? t2 : t1;
+      __nv_bfloat16* T = reinterpret_cast<__nv_bfloat16*>(g.ct) + bidx * g.stride_ct + m0;
+      for (int cc = warp; cc < n; cc += kGemmWarps)
+        for (int rr = lane; rr < rows; rr += 32) T[(int64_t)cc * g.ldt + rr] = src[rr * kPitchH + cc];
+    }
   }
 }
 
+// C tile [128 x n] of one batch member (blockIdx.z) and K range (blockIdx.y of
+// split-K). Thread 0 produces: TMA loads of 64-wide K chunks of A and B into a
+// ring of kTmaStages 128-byte-swizzled stages (full[s] counts the bytes); thread 32
+// consumes: four tcgen05.mma per chunk into the TMEM accumulator and a commit to
+// empty[s] that frees the stage; a final commit to `done` releases the epilogue.
 template <int EPI>
-__global__ void __launch_bounds__(128, 1) gemm_kernel(const ExcGemm g) {
-  extern __shared__ __align__(1024) uint8_t smem[];
-  __shared__ uint64_t bars[kStages];
+__global__ void __launch_bounds__(kGemmWarps * 32, 1) gemm_tma_kernel(const __grid_constant__ CUtensorMap tmA,
+                                                                      const __grid_constant__ CUtensorMap tmB,
+                                                                      const ExcGemm g) {
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
+  __shared__ uint64_t full[kTmaStages], empty[kTmaStages], done;
   __shared__ uint32_t tmem_base;
   __shared__ int lost;
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  __shared__ float sbias[256];
+  const int warp = threadIdx.x >> 5;
   const int64_t m0 = (int64_t)blockIdx.x * kTileM;
   const int split = blockIdx.y, bidx = blockIdx.z;
-  const int n = g.n, k = g.k;
-  const __nv_bfloat16* A = reinterpret_cast<const __nv_bfloat16*>(g.a) + bidx * g.stride_a;
-  const __nv_bfloat16* B = reinterpret_cast<const __nv_bfloat16*>(g.b) + bidx * g.stride_b;
+  const int splits = EPI == EXC_EPI_SPLITK ? gridDim.y : 1;
+  const int nch = g.k / kChunkK;
+  const int c_begin = (int)((int64_t)nch * split / splits), c_end = (int)((int64_t)nch * (split + 1) / splits);
+  const int used = c_end - c_begin;
+  const uint32_t stage_bytes = (uint32_t)(kStageA + g.n * kChunkK * 2);
+  const int za = g.stride_a ? bidx : 0, zb = g.stride_b ? bidx : 0;
 
   if (warp == 0) {
     tmem_alloc(&tmem_base, kTmemCols);
     tmem_relinquish();
   }
   if (threadIdx.x == 0) {
-    for (int s = 0; s < kStages; ++s) mbar_init(&bars[s], 1);
+    for (int s = 0; s < kTmaStages; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    mbar_init(&done, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     lost = 0;
   }
+  if (EPI == EXC_EPI_BIAS_SILU)
+    for (int i = threadIdx.x; i < g.n; i += blockDim.x) sbias[i] = __ldg(g.bias + (int64_t)bidx * g.n + i);
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = tmem_base;
 
-  const int nch = k / kChunkK;
-  const int splits = EPI == EXC_EPI_SPLITK ? gridDim.y : 1;
-  const int c_begin = (int)((int64_t)nch * split / splits), c_end = (int)((int64_t)nch * (split + 1) / splits);
-  const uint32_t idesc = idesc_bf16_f32(kTileM, n);
-  uint32_t phase[kStages] = {0u, 0u};
-  bool ok = true;
-
-  for (int c = c_begin; c < c_end; ++c) {
-    const int s = (c - c_begin) & 1;
-    uint8_t* sA = smem + s * kStage;
-    uint8_t* sB = sA + kStageA;
-    // the MMAs that last read this stage (chunk c - 2) must be complete before it is overwritten
-    if (c - c_begin >= kStages) {
-      if (!mbar_wait(&bars[s], phase[s])) ok = false;
-      phase[s] ^= 1u;
+  if (threadIdx.x == 0) {
+    // producer
+    for (int i = 0; i < used; ++i) {
+      const int s = i % kTmaStages;
+      if (i >= kTmaStages && !mbar_wait(&empty[s], (uint32_t)((i / kTmaStages - 1) & 1))) {
+        atomicOr(&lost, 1);
+        break;
+      }
+      uint8_t* sA = smem + s * kStage;
+      uint8_t* sB = sA + kStageA;
+      const int k0 = (c_begin + i) * kChunkK;
+      mbar_expect_tx(&full[s], stage_bytes);
+      tma_load_3d(sA, &tmA, k0, (int)m0, za, &full[s]);
+      tma_load_3d(sB, &tmB, k0, 0, zb, &full[s]);
     }
-    load_stage(sA, sB, A, B, m0, g.m, n, k, c * kChunkK);
-    fence_proxy_async_smem();
-    __syncthreads();
-    if (threadIdx.x == 0) {
+  } else if (threadIdx.x == 32) {
+    // MMA issuer
+    const uint32_t idesc = idesc_bf16_f32(kTileM, g.n);
+    bool ok = true;
+    for (int i = 0; i < used && ok; ++i) {
+      const int s = i % kTmaStages;
+      if (!mbar_wait(&full[s], (uint32_t)((i / kTmaStages) & 1))) {
+        ok = false;
+        break;
+      }
       tc_fence_after();
-      const uint32_t a0 = smem_u32(sA), b0 = smem_u32(sB);
+      const uint32_t a0 = smem_u32(smem + s * kStage), b0 = a0 + kStageA;
 #pragma unroll
       for (int j = 0; j < kChunkK / 16; ++j)
-        umma_bf16(tmem, smem_desc(a0 + j * 256, 128, 1024), smem_desc(b0 + j * 256, 128, 1024), idesc,
-                  (c > c_begin || j > 0) ? 1u : 0u);
-      umma_commit(&bars[s]);
+        umma_bf16(tmem, smem_desc_sw128(a0 + j * 32), smem_desc_sw128(b0 + j * 32), idesc, (i > 0 || j > 0) ? 1u : 0u);
+      umma_commit(&empty[s]);
     }
+    if (ok) umma_commit(&done);
+    else atomicOr(&lost, 1);
   }
-  // drain: the last commit of each used stage
-  const int used = c_end - c_begin;
-  for (int s = 0; s < kStages && s < used; ++s) {
-    // stage s was last committed by chunk index (used-1) or (used-2) with matching parity
-    if (!mbar_wait(&bars[s], phase[s])) ok = false;
+  // everyone waits for the accumulator (or for the bail-out flag)
+  if (used > 0) {
+    bool ready = false;
+    for (long long t = 0; t < kSpinLimit && !ready; ++t) {
+      ready = mbar_try_wait(&done, 0u);
+      if (!ready && *(volatile int*)&lost) break;
+    }
+    if (!ready) atomicOr(&lost, 1);
   }
-  if (!ok) atomicOr(&lost, 1);
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
   if (lost) {
     if (threadIdx.x == 0) atomicAdd(&g_timeouts, 1u);
   } else {
-    // epilogue: warp w owns TMEM lanes (rows) 32w .. 32w + 31
-    const int r = warp * 32 + lane;
-    const int64_t row = m0 + r;
-    const bool live = row < g.m && used > 0;
-    const uint32_t lane_addr = tmem + ((uint32_t)(warp * 32) << 16);
-    for (int c0 = 0; c0 < n; c0 += 16) {
-      float v[16];
-      tmem_ld16(lane_addr + (uint32_t)c0, v);
-      if (!live) continue;
-      if (EPI == EXC_EPI_F32) {
-        float* C = reinterpret_cast<float*>(g.c) + bidx * g.stride_c + row * n + c0;
-#pragma unroll
-        for (int i = 0; i < 16; i += 4) *reinterpret_cast<float4*>(C + i) = make_float4(v[i], v[i + 1], v[i + 2], v[i + 3]);
-      } else if (EPI == EXC_EPI_SPLITK) {
-        float* C = reinterpret_cast<float*>(g.c) + ((int64_t)bidx * splits + split) * g.m * n + row * n + c0;
-#pragma unroll
-        for (int i = 0; i < 16; i += 4) *reinterpret_cast<float4*>(C + i) = make_float4(v[i], v[i + 1], v[i + 2], v[i + 3]);
-      } else if (EPI == EXC_EPI_BIAS_SILU) {
-        const float* bias = g.bias + (int64_t)bidx * n + c0;
-        __nv_bfloat16 zb[16], hb[16];
-#pragma unroll
-        for (int i = 0; i < 16; ++i) {
-          const float z = v[i] + __ldg(bias + i);
-          zb[i] = __float2bfloat16_rn(z);
-          const float zr = __bfloat162float(zb[i]);   // the value the backward pass will see
-          hb[i] = __float2bfloat16_rn(zr * sigmoid(zr));
-        }
-        const int64_t off = bidx * g.stride_c + row * n + c0;
-        if (g.c) {
-          uint4* dst = reinterpret_cast<uint4*>(reinterpret_cast<__nv_bfloat16*>(g.c) + off);
-          dst[0] = *reinterpret_cast<uint4*>(&zb[0]);
-          dst[1] = *reinterpret_cast<uint4*>(&zb[8]);
-        }
-        if (g.c2) {
-          uint4* dst = reinterpret_cast<uint4*>(reinterpret_cast<__nv_bfloat16*>(g.c2) + off);
-          dst[0] = *reinterpret_cast<uint4*>(&hb[0]);
-          dst[1] = *reinterpret_cast<uint4*>(&hb[8]);
-        }
-        if (g.ct) {
-          __nv_bfloat16* T = reinterpret_cast<__nv_bfloat16*>(g.ct) + bidx * g.stride_ct + row;
-#pragma unroll
-          for (int i = 0; i < 16; ++i) T[(int64_t)(c0 + i) * g.ldt] = hb[i];
-        }
-      } else {  // EXC_EPI_DSILU
-        const int64_t off = bidx * g.stride_c + row * n + c0;
-        const __nv_bfloat16* Z = reinterpret_cast<const __nv_bfloat16*>(g.z_in) + off;
-        __nv_bfloat16 db[16];
-#pragma unroll
-        for (int i = 0; i < 16; ++i) {
-          const float z = __bfloat162float(Z[i]);
-          const float sg = sigmoid(z);
-          db[i] = __float2bfloat16_rn(v[i] * (sg * (1.0f + z * (1.0f - sg))));
-        }
-        if (g.c) {
-          uint4* dst = reinterpret_cast<uint4*>(reinterpret_cast<__nv_bfloat16*>(g.c) + off);
-          dst[0] = *reinterpret_cast<uint4*>(&db[0]);
-          dst[1] = *reinterpret_cast<uint4*>(&db[8]);
-        }
-        if (g.ct) {
-          __nv_bfloat16* T = reinterpret_cast<__nv_bfloat16*>(g.ct) + bidx * g.stride_ct + row;
-#pragma unroll
-          for (int i = 0; i < 16; ++i) T[(int64_t)(c0 + i) * g.ldt] = db[i];
-        }
-      }
-    }
+    epilogue<EPI>(g, tmem, m0, split, splits, bidx, smem, sbias);
   }
   tc_fence_before();
   __syncthreads();
@@ -478,13 +543,49 @@ static int mlp_cuda(cudaError_t e) {
 }
 static bool aligned16(const void* p) { return ((uintptr_t)p & 15u) == 0; }
 
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static EncodeTiledFn encode_fn() {
+  static EncodeTiledFn fn = nullptr;
+  if (!fn) {
+    cudaDriverEntryPointQueryResult q;
+    void* p = nullptr;
+    if (cudaGetDriverEntryPoint("cuTensorMapEncodeTiled", &p, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (EncodeTiledFn)p;
+  }
+  return fn;
+}
+
+// [batch][rows][K] BF16 (batch stride 0 = one matrix shared by every member) as a
+// 3-D tensor map with 64 x box_rows x 1 boxes, 128-byte swizzle, zero fill.
+static bool make_map(CUtensorMap* map, const void* base, int64_t rows, int k, int64_t batch_stride, int batch,
+                     int box_rows) {
+  EncodeTiledFn fn = encode_fn();
+  if (!fn) return false;
+  const int nb = batch_stride ? batch : 1;
+  const cuuint64_t dims[3] = {(cuuint64_t)k, (cuuint64_t)rows, (cuuint64_t)nb};
+  const cuuint64_t strides[2] = {(cuuint64_t)k * 2, (cuuint64_t)(batch_stride ? batch_stride : rows * (int64_t)k) * 2};
+  const cuuint32_t box[3] = {(cuuint32_t)kChunkK, (cuuint32_t)box_rows, 1};
+  const cuuint32_t estr[3] = {1, 1, 1};
+  return fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<void*>(base), dims, strides, box, estr,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 template <int EPI>
 static cudaError_t launch_gemm(const ExcGemm& g, cudaStream_t s) {
-  cudaError_t e = cudaFuncSetAttribute(gemm_kernel<EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmem);
+  CUtensorMap ta, tb;
+  if (!make_map(&ta, g.a, g.m, g.k, g.stride_a, g.n_batch, kTileM) ||
+      !make_map(&tb, g.b, g.n, g.k, g.stride_b, g.n_batch, g.n))
+    return cudaErrorInvalidValue;
+  cudaError_t e = cudaFuncSetAttribute(gemm_tma_kernel<EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTmaSmem);
   if (e != cudaSuccess) return e;
   dim3 grid((unsigned)((g.m + kTileM - 1) / kTileM), EPI == EXC_EPI_SPLITK ? (unsigned)g.k_splits : 1u,
             (unsigned)g.n_batch);
-  gemm_kernel<EPI><<<grid, 128, kSmem, s>>>(g);
+  gemm_tma_kernel<EPI><<<grid, kGemmWarps * 32, kTmaSmem, s>>>(ta, tb, g);
   return cudaGetLastError();
 }
 
