@@ -31,6 +31,7 @@ FAILED_STATUSES = (PH_OUTSIDE_GRID, PH_HORIZON, PH_NONFINITE, PH_TIMED_OUT, PH_A
 METRIC_FLRW, METRIC_SCHWARZSCHILD = 1, 2
 COSMO_STATIC, COSMO_TABLE, COSMO_TABLE_FD = 0, 1, 2
 BOUNDARY = {"periodic": 0, "clamp": 1, "error": 2}
+GRAD = {"base_node": 0, "trilinear": 1}
 DTYPE_F64, DTYPE_F32, DTYPE_F32X2 = 0, 1, 2
 STEPPER = {"rk4": 0, "rk45": 1, "leapfrog4": 2}
 TABLEAU = {"reference": 0, "fehlberg": 1}

@@ -40,7 +40,7 @@ __global__ void interp_kernel(const ExcField f, const double fi0, const double f
                               int32_t* status, int64_t n) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  const double fi[8] = {fi0, fi1, fi2, fi3, 0.5 * fi0, 0.5 * fi1, 0.5 * fi2, 0.0};
+  const double fi[8] = {fi0, fi1, fi2, fi3, 0.5 * fi0, 0.5 * fi1, 0.5 * fi2, 0.5 * fi3};
   InterpOut o;
   const int st = interp_field<FT>(f, fi, pts[i * 4 + 0], pts[i * 4 + 1], pts[i * 4 + 2], pts[i * 4 + 3], o);
   out[i * 5 + 0] = st ? NAN : o.val;

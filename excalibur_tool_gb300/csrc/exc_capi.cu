@@ -57,9 +57,17 @@ int check_field(const ExcField& f, int idx) {
       return fail(EXC_ERR_INVALID, "field %d: spacing[%d] must be finite and > 0", idx, d);
     if (!std::isfinite(f.origin[d])) return fail(EXC_ERR_INVALID, "field %d: origin[%d] not finite", idx, d);
   }
-  if (f.boundary == EXC_BOUNDARY_ERROR)
+  if (f.grad_mode != EXC_GRAD_BASE_NODE && f.grad_mode != EXC_GRAD_TRILINEAR)
+    return fail(EXC_ERR_INVALID, "field %d: unknown grad_mode %d", idx, f.grad_mode);
+  if (f.grad_mode == EXC_GRAD_TRILINEAR) {
+    if (f.boundary != EXC_BOUNDARY_ERROR)
+      return fail(EXC_ERR_INVALID, "field %d: the trilinear gradient needs the error boundary", idx);
+    for (int d = 0; d < 3; ++d)
+      if (f.n[d] < 3) return fail(EXC_ERR_INVALID, "field %d: the trilinear gradient needs n >= 3 per axis", idx);
+  } else if (f.boundary == EXC_BOUNDARY_ERROR) {
     for (int d = 0; d < 3; ++d)
       if (f.n[d] < 4) return fail(EXC_ERR_INVALID, "field %d: error boundary needs n >= 4 per axis", idx);
+  }
   return 0;
 }
 
@@ -84,6 +92,7 @@ int build_dev_metric(const ExcMetric* m, exc::DevMetric& D) {
       const ExcField& f = m->fields[i];
       for (int d = 0; d < f.ndim; ++d) D.finv[i][d] = 1.0 / f.spacing[d];
       for (int d = 0; d < 3; ++d) D.finv[i][4 + d] = 1.0 / (2.0 * f.spacing[d]);
+      if (f.ndim == 4) D.finv[i][7] = 1.0 / (2.0 * f.spacing[3]);
     }
     if (m->cosmology != EXC_COSMO_STATIC && m->cosmology != EXC_COSMO_TABLE &&
         m->cosmology != EXC_COSMO_TABLE_FD)

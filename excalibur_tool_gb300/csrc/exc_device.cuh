@@ -205,13 +205,150 @@ __device__ __forceinline__ int interp_snapshot(const ExcField& f, const double* 
 #undef EXC_IDX
 }
 
+// ---- the slow Interpolator (grid/interpolator.py), grad_mode EXC_GRAD_TRILINEAR
+
+// Difference of two grid nodes. numpy subtracts two float32 elements in
+// float32 (grid/interpolator.py:147-152 on a float32 field); every other grid
+// type differences in FP64.
+template <class FT>
+__device__ __forceinline__ double node_diff(const FT* __restrict__ d, int64_t a, int64_t b) {
+  return ldf(d, a) - ldf(d, b);
+}
+template <>
+__device__ __forceinline__ double node_diff<float>(const float* __restrict__ d, int64_t a, int64_t b) {
+  return (double)(__ldg(d + a) - __ldg(d + b));
+}
+
+// numpy's sum of eight float64 terms (its pairwise summation with eight
+// partial sums, as np.sum applies it to a length-8 array).
+__device__ __forceinline__ double sum8(const double p[8]) {
+  return ((p[0] + p[1]) + (p[2] + p[3])) + ((p[4] + p[5]) + (p[6] + p[7]));
+}
+
+// Integer index of an already-floored coordinate, clipped to [lo, hi] in the
+// double domain first so that no out-of-range value is converted.
+__device__ __forceinline__ int64_t clip_index(double v, int64_t lo, int64_t hi) {
+  if (!(v > (double)lo)) return lo;
+  if (v >= (double)hi) return hi;
+  return (int64_t)v;
+}
+
+// Interpolator.gradient (grid/interpolator.py:88-158) on snapshot `it`: the
+// central differences at the eight corners of the cell whose base index is
+// floor(rel) clipped to [1, n-2] (each corner clipped again), blended with
+// the trilinear weights of the unclipped fraction rel - floor(rel). Corner
+// order (:117-126) and weight expressions (:129-138) as listed there.
+template <class FT>
+__device__ __forceinline__ void slow_gradient(const ExcField& f, const double* fi, const FT* __restrict__ d,
+                                              int64_t nt, int64_t it, double rx, double ry, double rz,
+                                              InterpOut& o) {
+  const int64_t nx = f.n[0], ny = f.n[1], nz = f.n[2];
+#define EXC_IDX(i, j, k) ((((int64_t)(i) * ny + (j)) * nz + (k)) * nt + it)
+  const double flx = floor(rx), fly = floor(ry), flz = floor(rz);
+  const double wx = rx - flx, wy = ry - fly, wz = rz - flz;
+  const int64_t bi = clip_index(flx, 1, nx - 2), bj = clip_index(fly, 1, ny - 2), bk = clip_index(flz, 1, nz - 2);
+  const double w[8] = {(1.0 - wx) * (1.0 - wy) * (1.0 - wz), wx * (1.0 - wy) * (1.0 - wz),
+                       (1.0 - wx) * wy * (1.0 - wz),         (1.0 - wx) * (1.0 - wy) * wz,
+                       wx * wy * (1.0 - wz),                 wx * (1.0 - wy) * wz,
+                       (1.0 - wx) * wy * wz,                 wx * wy * wz};
+  // corner c's offsets: x for c in {1,4,5,7}, y for {2,4,6,7}, z for {3,5,6,7}
+  constexpr unsigned kOx = 0xB2u, kOy = 0xD4u, kOz = 0xE8u;
+  double px[8], py[8], pz[8];
+#pragma unroll
+  for (int c = 0; c < 8; ++c) {
+    const int64_t i = min(bi + (int64_t)((kOx >> c) & 1u), nx - 2);
+    const int64_t j = min(bj + (int64_t)((kOy >> c) & 1u), ny - 2);
+    const int64_t k = min(bk + (int64_t)((kOz >> c) & 1u), nz - 2);
+    px[c] = div_c(node_diff(d, EXC_IDX(i + 1, j, k), EXC_IDX(i - 1, j, k)), 2.0 * f.spacing[0], fi[4]) * w[c];
+    py[c] = div_c(node_diff(d, EXC_IDX(i, j + 1, k), EXC_IDX(i, j - 1, k)), 2.0 * f.spacing[1], fi[5]) * w[c];
+    pz[c] = div_c(node_diff(d, EXC_IDX(i, j, k + 1), EXC_IDX(i, j, k - 1)), 2.0 * f.spacing[2], fi[6]) * w[c];
+  }
+  o.gx = sum8(px);
+  o.gy = sum8(py);
+  o.gz = sum8(pz);
+#undef EXC_IDX
+}
+
+// Interpolator.value_gradient_and_time_derivative (grid/interpolator.py:198-206)
+// for an ExcField with grad_mode EXC_GRAD_TRILINEAR. Unlike the fast classes,
+// the slow one raises only for a position outside the bounds: a NaN grid value
+// passes through (and ends a traced photon as non-finite).
+template <class FT>
+__device__ __forceinline__ int interp_slow(const ExcField& f, const double* fi, const FT* __restrict__ d,
+                                           double x, double y, double z, double t, InterpOut& o) {
+  const int64_t nx = f.n[0], ny = f.n[1], nz = f.n[2];
+  // _index_and_weights (:13-44): bounds rel in [0, n-1), no clipping needed after it
+  const double rx = (x - f.origin[0]) / f.spacing[0];
+  const double ry = (y - f.origin[1]) / f.spacing[1];
+  const double rz = (z - f.origin[2]) / f.spacing[2];
+  if (rx < 0.0 || rx >= (double)(nx - 1) || ry < 0.0 || ry >= (double)(ny - 1) || rz < 0.0 ||
+      rz >= (double)(nz - 1))
+    return EXC_PH_OUTSIDE_GRID;
+  if (!isfinite(rx) || !isfinite(ry) || !isfinite(rz)) return EXC_PH_NONFINITE;
+  const double flx = floor(rx), fly = floor(ry), flz = floor(rz);
+  const int64_t i0 = (int64_t)flx, j0 = (int64_t)fly, k0 = (int64_t)flz;
+  const double wx = rx - flx, wy = ry - fly, wz = rz - flz;
+  if (f.ndim != 4) {
+#define EXC_IDX(i, j, k) (((int64_t)(i) * ny + (j)) * nz + (k))
+    // _interpolate_3d (:52-69)
+    o.val = trilinear(ldf(d, EXC_IDX(i0, j0, k0)), ldf(d, EXC_IDX(i0 + 1, j0, k0)), ldf(d, EXC_IDX(i0, j0 + 1, k0)),
+                      ldf(d, EXC_IDX(i0, j0, k0 + 1)), ldf(d, EXC_IDX(i0 + 1, j0 + 1, k0)),
+                      ldf(d, EXC_IDX(i0 + 1, j0, k0 + 1)), ldf(d, EXC_IDX(i0, j0 + 1, k0 + 1)),
+                      ldf(d, EXC_IDX(i0 + 1, j0 + 1, k0 + 1)), wx, wy, wz);
+#undef EXC_IDX
+    slow_gradient<FT>(f, fi, d, 1, 0, rx, ry, rz, o);
+    o.dtd = 0.0;
+    return 0;
+  }
+  const int64_t nt = f.n[3];
+#define EXC_IDX(i, j, k, l) ((((int64_t)(i) * ny + (j)) * nz + (k)) * nt + (l))
+  const double rt = (t - f.origin[3]) / f.spacing[3];
+  if (!isfinite(rt)) return EXC_PH_NONFINITE;
+  const double flt = floor(rt);
+  const double wt = rt - flt;
+  // _interpolate_4d (:71-86): w[a][b][c][e] = ((wx_a * wy_b) * wz_c) * wt_e summed
+  // as numpy sums the sixteen products in C order (eight partial sums)
+  const int64_t l0 = clip_index(flt, 0, nt - 2);
+  const double Wx[2] = {1.0 - wx, wx}, Wy[2] = {1.0 - wy, wy}, Wz[2] = {1.0 - wz, wz}, Wt[2] = {1.0 - wt, wt};
+  double r[8];
+#pragma unroll
+  for (int q = 0; q < 16; ++q) {
+    const int a = q >> 3, b = (q >> 2) & 1, c = (q >> 1) & 1, e = q & 1;
+    const double p = ldf(d, EXC_IDX(i0 + a, j0 + b, k0 + c, l0 + e)) * (((Wx[a] * Wy[b]) * Wz[c]) * Wt[e]);
+    if (q < 8) r[q] = p;
+    else r[q - 8] += p;
+  }
+  o.val = sum8(r);
+  // gradient on the nearest snapshot (:92-96): round half to even, clipped to [0, nt-1]
+  slow_gradient<FT>(f, fi, d, nt, clip_index(rint(rt), 0, nt - 1), rx, ry, rz, o);
+  // time_derivative (:160-174): snapshots lt -/+ 1 around lt = clip(floor(rel_t), 1, nt-2);
+  // numpy's clip gives nt-2 when that bound is below 1, and index -1 is the last snapshot
+  const double lv = fmin(fmax(flt, 1.0), (double)(nt - 2));
+  const int64_t lt = (int64_t)lv;
+  const int64_t lp = lt - 1 < 0 ? lt - 1 + nt : lt - 1, ln = lt + 1;
+  double v[2];
+#pragma unroll
+  for (int s = 0; s < 2; ++s) {
+    const int64_t l = s ? ln : lp;
+    v[s] = trilinear(ldf(d, EXC_IDX(i0, j0, k0, l)), ldf(d, EXC_IDX(i0 + 1, j0, k0, l)),
+                     ldf(d, EXC_IDX(i0, j0 + 1, k0, l)), ldf(d, EXC_IDX(i0, j0, k0 + 1, l)),
+                     ldf(d, EXC_IDX(i0 + 1, j0 + 1, k0, l)), ldf(d, EXC_IDX(i0 + 1, j0, k0 + 1, l)),
+                     ldf(d, EXC_IDX(i0, j0 + 1, k0 + 1, l)), ldf(d, EXC_IDX(i0 + 1, j0 + 1, k0 + 1, l)), wx, wy, wz);
+  }
+#undef EXC_IDX
+  o.dtd = div_c(v[1] - v[0], 2.0 * f.spacing[3], fi[7]);
+  return 0;
+}
+
 // InterpolatorFast.value_gradient_and_time_derivative (interpolator_4d_fast.py:443-502),
 // including the 4-D snapshot blend (:265-402). A NaN value maps to
 // EXC_PH_OUTSIDE_GRID, like the reference's ValueError at :500-501.
+// grad_mode EXC_GRAD_TRILINEAR selects the slow Interpolator instead.
 template <class FT>
 __device__ __forceinline__ int interp_field(const ExcField& f, const double* fi, double x, double y, double z,
                                             double t, InterpOut& o) {
   const FT* d = (const FT*)f.data;
+  if (f.grad_mode == EXC_GRAD_TRILINEAR) return interp_slow<FT>(f, fi, d, x, y, z, t, o);
   if (f.ndim != 4) {
     int st = interp_snapshot<FT>(f, fi, d, 1, 0, x, y, z, o);
     if (st) return st;

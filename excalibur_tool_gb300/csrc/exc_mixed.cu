@@ -732,6 +732,7 @@ int check(const DevMetric& D, const ExcTraceArgs& A) {
   if (A.renormalize_every) return 4;
   for (int i = 0; i < D.m.n_fields; ++i) {
     if (D.m.fields[i].ndim != 3) return 5;
+    if (D.m.fields[i].grad_mode != EXC_GRAD_BASE_NODE) return 8;
     const int64_t* n = D.m.fields[i].n;
     if (n[0] * n[1] * n[2] >= (int64_t)1 << 31) return 6;
   }
@@ -748,6 +749,7 @@ const char* why(int code) {
     case 5: return "mixed precision supports 3-D (static) potential grids only";
     case 6: return "mixed precision needs grids below 2^31 nodes";
     case 7: return "mixed precision has no ISW accumulator (static grids only)";
+    case 8: return "mixed precision supports the base-node gradient only";
     default: return "mixed precision: unsupported";
   }
 }

@@ -16,6 +16,8 @@ from .. import _native as N
 
 
 class InterpolatorFast:
+    gradient_mode = "base_node"   # central difference at the cell's base node
+
     def __init__(self, grid, boundary: str = "periodic", field_dtype=None):
         if boundary not in ("error", "clamp", "periodic"):
             raise ValueError("boundary must be one of: 'error', 'clamp', 'periodic'")
@@ -44,9 +46,10 @@ class InterpolatorFast:
         if split and str(t.dtype) == "torch.float64":
             planes = self.grid.device_field_split(field, device)
             f = field_struct(planes, self.shape[:nd], self.spacing[:nd], self.origin[:nd], self.boundary,
-                             split=True)
+                             split=True, gradient=self.gradient_mode)
             return f, planes
-        return field_struct(t, self.shape[:nd], self.spacing[:nd], self.origin[:nd], self.boundary), t
+        return field_struct(t, self.shape[:nd], self.spacing[:nd], self.origin[:nd], self.boundary,
+                            gradient=self.gradient_mode), t
 
     # ---- batched evaluation ----------------------------------------------
     def evaluate(self, points, field="Phi", device="cuda"):

@@ -104,7 +104,8 @@ def base_metric_struct(kind: int) -> N.ExcMetric:
     return m
 
 
-def field_struct(data, shape, spacing, origin, boundary: str, split: bool = False) -> N.ExcField:
+def field_struct(data, shape, spacing, origin, boundary: str, split: bool = False,
+                 gradient: str = "base_node") -> N.ExcField:
     import torch
 
     f = N.ExcField()
@@ -122,9 +123,12 @@ def field_struct(data, shape, spacing, origin, boundary: str, split: bool = Fals
         raise ValueError("field data must be C-contiguous")
     if boundary not in N.BOUNDARY:
         raise ValueError("boundary must be one of: 'error', 'clamp', 'periodic'")
+    if gradient not in N.GRAD:
+        raise ValueError("gradient must be 'base_node' or 'trilinear'")
     f.data = data.data_ptr()
     f.ndim = len(shape)
     f.boundary = N.BOUNDARY[boundary]
+    f.grad_mode = N.GRAD[gradient]
     for d in range(len(shape)):
         f.n[d] = int(shape[d])
         f.spacing[d] = float(spacing[d])

@@ -75,7 +75,19 @@ enum {
 enum { EXC_METRIC_FLRW = 1, EXC_METRIC_SCHWARZSCHILD = 2 };
 enum { EXC_COSMO_STATIC = 0, EXC_COSMO_TABLE = 1, EXC_COSMO_TABLE_FD = 2 };
 enum { EXC_BOUNDARY_PERIODIC = 0, EXC_BOUNDARY_CLAMP = 1, EXC_BOUNDARY_ERROR = 2 };
-enum { EXC_GRAD_BASE_NODE = 0 };                 /* fast interpolators' gradient */
+/* EXC_GRAD_BASE_NODE: the fast interpolators (grid/interpolator_4d_fast.py,
+ *   grid/interpolator_fast.py): trilinear value, central difference at the
+ *   cell's base node, boundary per ExcField.boundary.
+ * EXC_GRAD_TRILINEAR: the slow Interpolator (grid/interpolator.py:4-206):
+ *   trilinear value with the bounds rule rel in [0, n-1) per spatial axis
+ *   (EXC_PH_OUTSIDE_GRID outside); gradient = trilinear blend of the central
+ *   differences at the cell's eight corners (base index clipped to [1, n-2]);
+ *   4-D: quadrilinear value (time index clipped to [0, nt-2], weights not,
+ *   no time bounds check), gradient on the snapshot nearest in time (round
+ *   half to even, clipped), dPhi/deta from the snapshots either side of
+ *   clip(floor(rel_t), 1, nt-2). Needs boundary EXC_BOUNDARY_ERROR and n >= 3
+ *   per spatial axis. */
+enum { EXC_GRAD_BASE_NODE = 0, EXC_GRAD_TRILINEAR = 1 };
 /* EXC_DTYPE_F32X2: a float64 grid stored as interleaved float32 pairs, node i
  * at data[2i] = hi = (float)x_i and data[2i + 1] = lo = (float)(x_i - hi);
  * read by the mixed-precision tracer, whose FP32 arithmetic then takes grid

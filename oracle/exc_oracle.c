@@ -136,11 +136,133 @@ static int snapshot(const ExcField* f, int64_t nt, int64_t it, double x, double 
 #undef IX
 }
 
-/* InterpolatorFast.value_gradient_and_time_derivative (interpolator_4d_fast.py:443-502). */
+/* ---- the slow Interpolator (grid/interpolator.py), grad_mode EXC_GRAD_TRILINEAR */
+
+/* f[a] - f[b]: numpy subtracts two float32 elements in float32 (:147-152). */
+static double node_diff(const ExcField* f, int64_t a, int64_t b) {
+  if (f->dtype == EXC_DTYPE_F32) {
+    const float* p = (const float*)f->data;
+    const float d = p[a] - p[b];
+    return (double)d;
+  }
+  return fld(f, a) - fld(f, b);
+}
+
+/* np.sum of eight float64 terms: numpy's pairwise sum keeps eight partial sums
+ * r[j] (here one term each) and adds them as ((r0+r1)+(r2+r3))+((r4+r5)+(r6+r7)). */
+static double np_sum8(const double p[8]) {
+  return ((p[0] + p[1]) + (p[2] + p[3])) + ((p[4] + p[5]) + (p[6] + p[7]));
+}
+
+/* np.clip of a floored coordinate to [lo, hi] (lo <= hi). */
+static int64_t clip_floor(double v, int64_t lo, int64_t hi) {
+  if (!(v > (double)lo)) return lo;
+  if (v >= (double)hi) return hi;
+  return (int64_t)v;
+}
+
+/* Interpolator.gradient (:88-158) on snapshot `it` of nt. */
+static void slow_gradient(const ExcField* f, int64_t nt, int64_t it, double rx, double ry, double rz, Interp* o) {
+  const int64_t nx = f->n[0], ny = f->n[1], nz = f->n[2];
+#define IX(i, j, k) (((((int64_t)(i)) * ny + (j)) * nz + (k)) * nt + it)
+  const double flx = floor(rx), fly = floor(ry), flz = floor(rz);
+  const double wx = rx - flx, wy = ry - fly, wz = rz - flz;
+  /* :102-106, base index clipped to [1, n-2]; the fraction is not */
+  const int64_t bi = clip_floor(flx, 1, nx - 2), bj = clip_floor(fly, 1, ny - 2), bk = clip_floor(flz, 1, nz - 2);
+  /* corners and weights in the order of :117-138 */
+  static const int off[8][3] = {{0, 0, 0}, {1, 0, 0}, {0, 1, 0}, {0, 0, 1},
+                                {1, 1, 0}, {1, 0, 1}, {0, 1, 1}, {1, 1, 1}};
+  const double w[8] = {(1 - wx) * (1 - wy) * (1 - wz), wx * (1 - wy) * (1 - wz), (1 - wx) * wy * (1 - wz),
+                       (1 - wx) * (1 - wy) * wz,       wx * wy * (1 - wz),       wx * (1 - wy) * wz,
+                       (1 - wx) * wy * wz,             wx * wy * wz};
+  double px[8], py[8], pz[8];
+  for (int c = 0; c < 8; ++c) {
+    int64_t i = bi + off[c][0], j = bj + off[c][1], k = bk + off[c][2];
+    if (i > nx - 2) i = nx - 2; /* :144-146 (the lower clip cannot bind: base >= 1) */
+    if (j > ny - 2) j = ny - 2;
+    if (k > nz - 2) k = nz - 2;
+    px[c] = node_diff(f, IX(i + 1, j, k), IX(i - 1, j, k)) / (2 * f->spacing[0]) * w[c];
+    py[c] = node_diff(f, IX(i, j + 1, k), IX(i, j - 1, k)) / (2 * f->spacing[1]) * w[c];
+    pz[c] = node_diff(f, IX(i, j, k + 1), IX(i, j, k - 1)) / (2 * f->spacing[2]) * w[c];
+  }
+  o->gx = np_sum8(px);
+  o->gy = np_sum8(py);
+  o->gz = np_sum8(pz);
+#undef IX
+}
+
+/* Interpolator.value_gradient_and_time_derivative (:198-206). Only the bounds
+ * check raises there: NaN grid values pass through. */
+static int slow_interp(const ExcField* f, double x, double y, double z, double t, Interp* o) {
+  const int64_t nx = f->n[0], ny = f->n[1], nz = f->n[2];
+  /* _index_and_weights (:13-44) */
+  const double rx = (x - f->origin[0]) / f->spacing[0];
+  const double ry = (y - f->origin[1]) / f->spacing[1];
+  const double rz = (z - f->origin[2]) / f->spacing[2];
+  if (rx < 0 || rx >= (double)(nx - 1) || ry < 0 || ry >= (double)(ny - 1) || rz < 0 || rz >= (double)(nz - 1))
+    return EXC_PH_OUTSIDE_GRID;
+  if (!isfinite(rx) || !isfinite(ry) || !isfinite(rz)) return EXC_PH_NONFINITE;
+  const double flx = floor(rx), fly = floor(ry), flz = floor(rz);
+  const int64_t i0 = (int64_t)flx, j0 = (int64_t)fly, k0 = (int64_t)flz;
+  const double wx = rx - flx, wy = ry - fly, wz = rz - flz;
+  if (f->ndim != 4) {
+#define IX(i, j, k) ((((int64_t)(i)) * ny + (j)) * nz + (k))
+    /* _interpolate_3d (:52-69) */
+    o->val = trilinear(fld(f, IX(i0, j0, k0)), fld(f, IX(i0 + 1, j0, k0)), fld(f, IX(i0, j0 + 1, k0)),
+                       fld(f, IX(i0, j0, k0 + 1)), fld(f, IX(i0 + 1, j0 + 1, k0)), fld(f, IX(i0 + 1, j0, k0 + 1)),
+                       fld(f, IX(i0, j0 + 1, k0 + 1)), fld(f, IX(i0 + 1, j0 + 1, k0 + 1)), wx, wy, wz);
+#undef IX
+    slow_gradient(f, 1, 0, rx, ry, rz, o);
+    o->dtd = 0.0;
+    return 0;
+  }
+  const int64_t nt = f->n[3];
+#define IX(i, j, k, l) (((((int64_t)(i)) * ny + (j)) * nz + (k)) * nt + (l))
+  const double rt = (t - f->origin[3]) / f->spacing[3];
+  if (!isfinite(rt)) return EXC_PH_NONFINITE;
+  const double flt = floor(rt);
+  const double wt = rt - flt;
+  /* _interpolate_4d (:71-86): weights ((wx_a * wy_b) * wz_c) * wt_e, the sixteen
+   * products summed in C order by numpy's pairwise sum (eight partial sums) */
+  const int64_t l0 = clip_floor(flt, 0, nt - 2);
+  const double Wx[2] = {1 - wx, wx}, Wy[2] = {1 - wy, wy}, Wz[2] = {1 - wz, wz}, Wt[2] = {1 - wt, wt};
+  double r[8];
+  for (int q = 0; q < 16; ++q) {
+    const int a = q >> 3, b = (q >> 2) & 1, c = (q >> 1) & 1, e = q & 1;
+    const double p = fld(f, IX(i0 + a, j0 + b, k0 + c, l0 + e)) * (((Wx[a] * Wy[b]) * Wz[c]) * Wt[e]);
+    if (q < 8) r[q] = p;
+    else r[q - 8] += p;
+  }
+  o->val = np_sum8(r);
+  /* gradient on the nearest snapshot (:92-96): np.round is round-half-even */
+  slow_gradient(f, nt, clip_floor(nearbyint(rt), 0, nt - 1), rx, ry, rz, o);
+  /* time_derivative (:160-174): np.clip(floor, 1, nt-2) is nt-2 when nt-2 < 1,
+   * and Python index -1 is the last snapshot */
+  double lv = flt > 1.0 ? flt : 1.0;
+  if (lv > (double)(nt - 2)) lv = (double)(nt - 2);
+  const int64_t lt = (int64_t)lv;
+  const int64_t lp = lt - 1 < 0 ? lt - 1 + nt : lt - 1, ln = lt + 1;
+  double v[2];
+  for (int s = 0; s < 2; ++s) {
+    const int64_t l = s ? ln : lp;
+    v[s] = trilinear(fld(f, IX(i0, j0, k0, l)), fld(f, IX(i0 + 1, j0, k0, l)), fld(f, IX(i0, j0 + 1, k0, l)),
+                     fld(f, IX(i0, j0, k0 + 1, l)), fld(f, IX(i0 + 1, j0 + 1, k0, l)),
+                     fld(f, IX(i0 + 1, j0, k0 + 1, l)), fld(f, IX(i0, j0 + 1, k0 + 1, l)),
+                     fld(f, IX(i0 + 1, j0 + 1, k0 + 1, l)), wx, wy, wz);
+  }
+#undef IX
+  o->dtd = (v[1] - v[0]) / (2 * f->spacing[3]);
+  return 0;
+}
+
+/* InterpolatorFast.value_gradient_and_time_derivative (interpolator_4d_fast.py:443-502);
+ * grad_mode EXC_GRAD_TRILINEAR selects the slow Interpolator. */
 int oracle_interp_one(const ExcField* f, double x, double y, double z, double t, double out[5]) {
   Interp o;
   int st;
-  if (f->ndim != 4) {
+  if (f->grad_mode == EXC_GRAD_TRILINEAR) {
+    st = slow_interp(f, x, y, z, t, &o);
+  } else if (f->ndim != 4) {
     st = snapshot(f, 1, 0, x, y, z, &o);
     if (!st && isnan(o.val)) st = EXC_PH_OUTSIDE_GRID;
   } else {

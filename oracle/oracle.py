@@ -50,6 +50,7 @@ class FieldSpec:
     spacing: tuple
     origin: tuple
     boundary: str = "periodic"
+    gradient: str = "base_node"         # "base_node" | "trilinear" (the slow Interpolator)
 
 
 @dataclasses.dataclass
@@ -92,17 +93,18 @@ class Spacetime:
         for i, f in enumerate(self.fields):
             arr = np.ascontiguousarray(f.data)
             self._fields.append(arr)
-            m.fields[i] = field_struct(arr, f.spacing, f.origin, f.boundary)
+            m.fields[i] = field_struct(arr, f.spacing, f.origin, f.boundary, f.gradient)
         m.n_fields = len(self.fields)
         return m
 
 
-def field_struct(arr, spacing, origin, boundary):
+def field_struct(arr, spacing, origin, boundary, gradient="base_node"):
     fs = N.ExcField()
     fs.data = arr.ctypes.data
     fs.dtype = N.DTYPE_F32 if arr.dtype == np.float32 else N.DTYPE_F64
     fs.ndim = arr.ndim
     fs.boundary = N.BOUNDARY[boundary]
+    fs.grad_mode = N.GRAD[gradient]
     for d in range(arr.ndim):
         fs.n[d] = arr.shape[d]
         fs.spacing[d] = float(spacing[d])
@@ -112,7 +114,7 @@ def field_struct(arr, spacing, origin, boundary):
 
 def interp(field: FieldSpec, pts4):
     arr = np.ascontiguousarray(field.data)
-    fs = field_struct(arr, field.spacing, field.origin, field.boundary)
+    fs = field_struct(arr, field.spacing, field.origin, field.boundary, field.gradient)
     pts = np.ascontiguousarray(pts4, dtype=np.float64)
     n = pts.shape[0]
     out = np.empty((n, 5))

@@ -145,6 +145,79 @@ def gen_interp():
     save("interp.npz", **out)
 
 
+def _slow_eval(ip, pts, times=None):
+    vals, ok = [], []
+    for i, p in enumerate(pts):
+        try:
+            t = 0.0 if times is None else float(times[i])
+            v, gr, dt = ip.value_gradient_and_time_derivative(p, "Phi", t)
+            vals.append([v, *gr, dt])
+            ok.append(1)
+        except ValueError:
+            vals.append([np.nan] * 5)
+            ok.append(0)
+    return np.array(vals), np.array(ok)
+
+
+def gen_interp_slow(cz):
+    """The slow Interpolator (grid/interpolator.py): 3-D float64 and float32
+    grids, 4-D grids with three and two snapshots (times inside, outside and on
+    half-integers, where np.round goes to even), and RK4 traces through
+    PerturbedFLRWMetricFast with that interpolator."""
+    from excalibur.grid.interpolator import Interpolator
+
+    out = {}
+    shape, spacing, origin = (9, 7, 8), (2.5e22, 3.0e22, 2.0e22), (1.0e22, -4.0e22, 0.0)
+    g, data, pts = _grid_and_points(shape, spacing, origin, 13, 300, lo_frac=-0.1, hi_frac=1.1)
+    # points in the first and last cells (gradient base clipped to 1 / n-2)
+    ext = np.array(shape) * np.array(spacing)
+    edge = np.array(origin) + np.array([[0.3, 0.5, 0.2], [0.99, 0.5, 0.5], [0.01, 0.99, 0.5]]) * \
+        (np.array(shape) - 1) * np.array(spacing)
+    pts = np.concatenate([pts, edge, (np.array(origin) + ext * 0.5)[None]])
+    out.update(f3=data, f3_spacing=np.array(spacing), f3_origin=np.array(origin), pts3=pts)
+    out["out3"], out["ok3"] = _slow_eval(Interpolator(g), pts)
+    g32 = Grid(shape, spacing, origin)
+    g32.add_field("Phi", data.astype(np.float32))
+    out["out3_f32"], out["ok3_f32"] = _slow_eval(Interpolator(g32), pts)
+    rng = np.random.default_rng(17)
+    for nt in (3, 2):
+        shape4, spacing4, origin4 = (8, 9, 7, nt), (2.0e22, 2.5e22, 3.0e22, 4.0e15), (0.0, 1.0e22, -2.0e22, 1.0e17)
+        data4 = rng.standard_normal(shape4) * 3.0e4
+        g4 = Grid(shape4, spacing4, origin4)
+        g4.add_field("Phi", data4)
+        n4 = 200
+        p4 = np.array(origin4[:3]) + rng.uniform(-0.1, 1.1, (n4, 3)) * (np.array(shape4[:3]) - 1) * \
+            np.array(spacing4[:3])
+        rel_t = np.concatenate([rng.uniform(-0.6, nt + 0.4, n4 - 8), [-0.5, 0.5, 1.5, 2.5, 0.0, 1.0, nt - 1.0, 3.5]])
+        t4 = origin4[3] + rel_t * spacing4[3]
+        o4, k4 = _slow_eval(Interpolator(g4), p4, t4)
+        out.update({f"f4_{nt}": data4, f"f4_{nt}_spacing": np.array(spacing4), f"f4_{nt}_origin": np.array(origin4),
+                    f"pts4_{nt}": np.column_stack([p4, t4]), f"out4_{nt}": o4, f"ok4_{nt}": k4})
+    # RK4 traces through the fast FLRW metric with the slow interpolator
+    n, box = 16, 40 * one_Mpc
+    rng = np.random.default_rng(19)
+    field = rng.standard_normal((n, n, n)) * 1e-5 * c ** 2
+    gt = Grid((n, n, n), (box / n,) * 3, (0.0, 0.0, 0.0))
+    gt.add_field("Phi", field)
+    m = PerturbedFLRWMetricFast(cz.a_of_eta, gt, Interpolator(gt), adot_of_eta=cz.adot_of_eta)
+    dt = 0.25 * one_Mpc / c
+    eta0 = cz._eta_at_a1
+    inits, finals, recs = [], [], []
+    for k in range(4):
+        d = rng.standard_normal(3)
+        d /= np.linalg.norm(d)
+        x0 = np.array([eta0, *(rng.uniform(0.35, 0.65, 3) * box)])
+        u0 = Photons(m)._solve_u0_from_null_condition(x0, d * c, sign=-1.0)
+        p = Photon(x0, np.array([u0, *(d * c)]))
+        Integrator(m, dt=dt, integrator="rk4", dt_min=dt, dt_max=dt).integrate_single(p, "steps", 40, record_every=1)
+        inits.append(np.concatenate([x0, [u0], d * c]))
+        finals.append(np.concatenate([p.x, p.u]))
+        recs.append(np.array([np.asarray(h, dtype=float)[:8] for h in p.history.states]))
+    out.update(trace_field=field, trace_box=box, trace_dt=dt, trace_init=np.array(inits),
+               trace_final=np.array(finals), trace_records=np.array(recs))
+    save("interp_slow.npz", **out)
+
+
 # ----------------------------------------------------------------- RHS
 def _flrw_setup(cz, n=16, box=40 * one_Mpc, seed=7, boundary="periodic"):
     rng = np.random.default_rng(seed)
@@ -460,6 +533,7 @@ if __name__ == "__main__":
     np.seterr(all="ignore")
     cz = gen_cosmology()
     gen_interp()
+    gen_interp_slow(cz)
     gen_rhs(cz)
     gen_steps(cz)
     gen_integrate(cz)

@@ -50,11 +50,16 @@ def gpu_metric(spec, field_dtype=None):
         return SchwarzschildMetricFast(spec.mass, spec.radius, center=np.array(spec.center, dtype=float),
                                        analytical_geodesics=spec.analytical, free_time_geodesic=spec.free_time,
                                        coords="spherical")
+    from excalibur_tool_gb300.grid.interpolator import Interpolator
+
     interps = []
     for f in spec.fields:
         g = Grid(f.data.shape, f.spacing, f.origin)
         g.add_field("Phi", f.data)
-        interps.append(InterpolatorFast(g, boundary=f.boundary, field_dtype=field_dtype))
+        if f.gradient == "trilinear":
+            interps.append(Interpolator(g, field_dtype=field_dtype))
+        else:
+            interps.append(InterpolatorFast(g, boundary=f.boundary, field_dtype=field_dtype))
     if spec.cosmology == "static":
         cz = StaticCosmology()
         a_of, adot_of = cz.a_of_eta, cz.adot_of_eta
