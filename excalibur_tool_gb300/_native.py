@@ -32,6 +32,7 @@ METRIC_FLRW, METRIC_SCHWARZSCHILD = 1, 2
 COSMO_STATIC, COSMO_TABLE, COSMO_TABLE_FD = 0, 1, 2
 BOUNDARY = {"periodic": 0, "clamp": 1, "error": 2}
 GRAD = {"base_node": 0, "trilinear": 1}
+PROBE = {"addmul": 0, "div": 1, "sqrt": 2, "fmod": 3}
 DTYPE_F64, DTYPE_F32, DTYPE_F32X2 = 0, 1, 2
 STEPPER = {"rk4": 0, "rk45": 1, "leapfrog4": 2}
 TABLEAU = {"reference": 0, "fehlberg": 1}
@@ -135,6 +136,8 @@ EXPORTS = {
                                        C.c_void_p]),
     "exc_autotune": (C.c_int, [C.POINTER(ExcMetric), C.POINTER(ExcTraceArgs), C.c_void_p,
                                C.POINTER(ExcLaunchPlan), C.c_void_p]),
+    "exc_probe_scratch_len": (C.c_int64, []),
+    "exc_probe_fp64_rates": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(C.c_double), C.c_void_p]),
     # surrogate kernels (include/excalibur_mlp.h)
     "exc_gemm_bf16": (C.c_int, [C.POINTER(ExcGemm), _V]),
     "exc_mlp_features": (C.c_int, [_V, C.c_int64, C.c_int64, C.c_int32, C.POINTER(C.c_double),

@@ -2,7 +2,8 @@
 
 Each translation unit is compiled by nvcc in parallel, then linked into one
 shared library next to this file. The parity units (exc_exact_*.cu) are compiled
-with --fmad=false so no multiply-add is contracted.
+with --fmad=false so no multiply-add is contracted. The *_slow units hold the
+tracer kernels of launches with a slow-Interpolator field.
 """
 from __future__ import annotations
 
@@ -23,6 +24,8 @@ COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xptxas", "-
 UNITS = {
     **{f"exc_exact_{s}.cu": ["--fmad=false"] for s in ("rk4", "rk45", "lf4", "aux")},
     **{f"exc_fast_{s}.cu": ["--fmad=true"] for s in ("rk4", "rk45", "lf4", "aux")},
+    **{f"exc_exact_{s}_slow.cu": ["--fmad=false"] for s in ("rk4", "rk45", "lf4")},
+    **{f"exc_fast_{s}_slow.cu": ["--fmad=true"] for s in ("rk4", "rk45", "lf4")},
     "exc_mixed.cu": ["--fmad=true"],
     "exc_capi.cu": [],
     "exc_noalloc.cu": [],
@@ -30,6 +33,7 @@ UNITS = {
     "exc_tune.cu": [],
     "exc_gen.cu": ["--fmad=false"],
     "exc_born.cu": [],
+    "exc_probe.cu": ["--fmad=false"],
 }
 
 

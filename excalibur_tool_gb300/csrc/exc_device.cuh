@@ -343,12 +343,17 @@ __device__ __forceinline__ int interp_slow(const ExcField& f, const double* fi, 
 // InterpolatorFast.value_gradient_and_time_derivative (interpolator_4d_fast.py:443-502),
 // including the 4-D snapshot blend (:265-402). A NaN value maps to
 // EXC_PH_OUTSIDE_GRID, like the reference's ValueError at :500-501.
-// grad_mode EXC_GRAD_TRILINEAR selects the slow Interpolator instead.
-template <class FT>
+// grad_mode EXC_GRAD_TRILINEAR selects the slow Interpolator instead. SLOW =
+// false compiles that path out (callers whose host side has ruled such fields
+// out: the tracer kernels of base-node launches, the mixed tracer), so that it
+// does not weigh on their register allocation.
+template <class FT, bool SLOW = true>
 __device__ __forceinline__ int interp_field(const ExcField& f, const double* fi, double x, double y, double z,
                                             double t, InterpOut& o) {
   const FT* d = (const FT*)f.data;
-  if (f.grad_mode == EXC_GRAD_TRILINEAR) return interp_slow<FT>(f, fi, d, x, y, z, t, o);
+  if constexpr (SLOW) {
+    if (f.grad_mode == EXC_GRAD_TRILINEAR) return interp_slow<FT>(f, fi, d, x, y, z, t, o);
+  }
   if (f.ndim != 4) {
     int st = interp_snapshot<FT>(f, fi, d, 1, 0, x, y, z, o);
     if (st) return st;
@@ -526,13 +531,13 @@ __device__ __forceinline__ void flrw_accel_analytical(const DevMetric& D, double
 }
 
 // PerturbedFLRWMetricFast.geodesic_equations, perturbed_flrw_metric_fast.py:227-273.
-template <class FT>
+template <class FT, bool SLOW = true>
 __device__ __forceinline__ int flrw_rhs(const DevMetric& D, int fi, const double s[8], double out[8]) {
   double a, adot, inv_a;
   int st = scale_factor(D, s[0], a, adot, inv_a);
   if (st) return st;
   InterpOut ip;
-  st = interp_field<FT>(D.m.fields[fi], D.finv[fi], s[1], s[2], s[3], s[0], ip);
+  st = interp_field<FT, SLOW>(D.m.fields[fi], D.finv[fi], s[1], s[2], s[3], s[0], ip);
   if (st) return st;
   const double phi_n = div_c(ip.val, D.m.c2, D.ic2);
   const double phid_n = div_c(ip.dtd, D.m.c2, D.ic2);
@@ -613,7 +618,7 @@ __device__ __forceinline__ int schw_rhs(const DevMetric& D, const double s[8], d
 // PerturbedFLRWMetricFast.metric_tensor (perturbed_flrw_metric_fast.py:126-141) /
 // SchwarzschildMetricFast.metric_tensor (schwarzschild_metric_fast.py:190-201).
 // Both metrics are diagonal; every off-diagonal entry is 0.
-template <class FT>
+template <class FT, bool SLOW = true>
 __device__ __forceinline__ int metric_diag(const DevMetric& D, int fi, const double x[4], double g[4]) {
   const ExcMetric& m = D.m;
   if (m.kind == EXC_METRIC_SCHWARZSCHILD) {
@@ -630,7 +635,7 @@ __device__ __forceinline__ int metric_diag(const DevMetric& D, int fi, const dou
   int st = scale_factor(D, x[0], a, adot, inv_a);
   if (st) return st;
   InterpOut ip;
-  st = interp_field<FT>(m.fields[fi], D.finv[fi], x[1], x[2], x[3], x[0], ip);
+  st = interp_field<FT, SLOW>(m.fields[fi], D.finv[fi], x[1], x[2], x[3], x[0], ip);
   if (st) return st;
   const double phi = ip.val / m.c2;
   const double psi = phi;

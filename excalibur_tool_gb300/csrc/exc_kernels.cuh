@@ -21,6 +21,13 @@ namespace EXC_NS {
 
 namespace cg = cooperative_groups;
 
+// Template tag of the FLRW kernels that can read slow-Interpolator fields
+// (ExcField.grad_mode EXC_GRAD_TRILINEAR): a separate instantiation, so that the
+// base-node kernels are compiled without that path.
+constexpr int kFlrwSlowInterp = 0x100 | EXC_METRIC_FLRW;
+constexpr bool is_flrw(int mk) { return (mk & 0xff) == EXC_METRIC_FLRW; }
+constexpr bool slow_interp(int mk) { return mk == kFlrwSlowInterp; }
+
 // ------------------------------------------------------- photon context
 struct Photon {
   double s[8];
@@ -96,7 +103,7 @@ struct Tracer {
 
   __device__ __forceinline__ int rhs(const double s[8], double out[8]) const {
     if (MK == EXC_METRIC_SCHWARZSCHILD) return schw_rhs(D, s, out);
-    return flrw_rhs<FT>(D, fi, s, out);
+    return flrw_rhs<FT, slow_interp(MK)>(D, fi, s, out);
   }
 
   // Metric.metric_physical_quantities (perturbed_flrw_metric_fast.py:275-282;
@@ -110,7 +117,7 @@ struct Tracer {
     int st = scale_factor(D, s[0], a, adot, inv_a);
     if (st) return st;
     InterpOut ip;
-    st = interp_field<FT>(D.m.fields[fi], D.finv[fi], s[1], s[2], s[3], s[0], ip);
+    st = interp_field<FT, slow_interp(MK)>(D.m.fields[fi], D.finv[fi], s[1], s[2], s[3], s[0], ip);
     if (st) return st;
     q[0] = a; q[1] = ip.val; q[2] = ip.gx; q[3] = ip.gy; q[4] = ip.gz; q[5] = ip.dtd;
     return 0;
@@ -236,7 +243,7 @@ struct Tracer {
   // Integrator._renormalize_state_to_null, integrator.py:298-335.
   __device__ __forceinline__ int renormalize(double s[8]) const {
     double g[4];
-    int st = metric_diag<FT>(D, fi, s, g);
+    int st = metric_diag<FT, slow_interp(MK)>(D, fi, s, g);
     if (st) return st;
     const double u1 = s[5], u2 = s[6], u3 = s[7];
     const double Acoef = g[0];
@@ -294,7 +301,7 @@ template <int MK, class FT, bool REC>
 __device__ __forceinline__ void photon_begin(Tracer<MK, FT>& T, const ExcTraceArgs& A, Photon& P, int64_t p) {
   P.idx = p;
   T.fi = A.field_index ? A.field_index[p] : 0;
-  P.bad_field = (unsigned)T.fi >= (unsigned)T.D.m.n_fields && MK == EXC_METRIC_FLRW;
+  P.bad_field = (unsigned)T.fi >= (unsigned)T.D.m.n_fields && is_flrw(MK);
   if (P.bad_field) T.fi = 0;   // never index past the descriptor table
   const double* src = A.state + p * 8;
 #pragma unroll
@@ -318,7 +325,7 @@ __device__ __forceinline__ void photon_begin(Tracer<MK, FT>& T, const ExcTraceAr
     else { for (int i = 0; i < 3; ++i) rel[i] = P.p0[i] - A.lens_center[i]; }
     P.min_r = norm3(rel);
     P.a_obs = NAN; P.phi_obs = NAN;
-    if (MK == EXC_METRIC_FLRW) {
+    if (is_flrw(MK)) {
       double q[6];
       if (T.quantities(P.s, q) == 0) { P.a_obs = q[0]; P.phi_obs = q[1]; P.pdot_prev = q[5]; }
     }
@@ -343,7 +350,7 @@ __device__ __forceinline__ void photon_accumulate(const Tracer<MK, FT>& T, const
     const double r = norm3(rel);
     if (r < P.min_r) P.min_r = r;
   }
-  if (MK == EXC_METRIC_FLRW && (A.obs_flags & EXC_OBS_ISW)) {
+  if (is_flrw(MK) && (A.obs_flags & EXC_OBS_ISW)) {
     double q[6];
     if (T.quantities(P.s, q) == 0) {
       P.isw += 0.5 * (P.pdot_prev + q[5]) * (P.s[0] - s_old[0]);
@@ -382,7 +389,7 @@ __device__ __forceinline__ void photon_finish(const Tracer<MK, FT>& T, const Exc
     o[EXC_OBSCOL_ETA_EM] = P.s[0];
     o[EXC_OBSCOL_A_OBS] = P.a_obs;
     o[EXC_OBSCOL_PHI_OBS] = P.phi_obs;
-    if (MK == EXC_METRIC_FLRW && !failed && qst == 0) { o[EXC_OBSCOL_A_EM] = qf[0]; o[EXC_OBSCOL_PHI_EM] = qf[1]; }
+    if (is_flrw(MK) && !failed && qst == 0) { o[EXC_OBSCOL_A_EM] = qf[0]; o[EXC_OBSCOL_PHI_EM] = qf[1]; }
     o[EXC_OBSCOL_ISW_INT] = P.isw;
     if (A.obs_flags & EXC_OBS_PATH) {
       double pc[3];
@@ -446,7 +453,7 @@ __device__ __forceinline__ bool photon_iterate(Tracer<MK, FT>& T, const ExcTrace
         stop = true;
       }
     }
-    if (!stop && MK == EXC_METRIC_FLRW && (A.stop_flags & EXC_STOP_A)) {
+    if (!stop && is_flrw(MK) && (A.stop_flags & EXC_STOP_A)) {
       double a, adot, inv_a;
       if (scale_factor(T.D, P.s[0], a, adot, inv_a) == 0 && a <= A.a_stop) {
         P.status = EXC_PH_A_STOP;
@@ -525,11 +532,32 @@ cudaError_t launch_trace_r(const DevMetric& D, const ExcTraceArgs& A, LaunchCfg 
   return launch_trace_t<MK, FT, STEPPER, false>(D, A, lc, s);
 }
 
-// The dtype of field 0 selects the instantiation (all fields of a launch share it).
+// Slow-Interpolator launches (defined in the *_slow translation units, which
+// compile in parallel with the base-node ones).
+cudaError_t trace_rk4_slow(const DevMetric& D, const ExcTraceArgs& A, LaunchCfg lc, cudaStream_t s);
+cudaError_t trace_rk45_slow(const DevMetric& D, const ExcTraceArgs& A, LaunchCfg lc, cudaStream_t s);
+cudaError_t trace_lf4_slow(const DevMetric& D, const ExcTraceArgs& A, LaunchCfg lc, cudaStream_t s);
+
+template <int STEPPER>
+cudaError_t launch_trace_slow(const DevMetric& D, const ExcTraceArgs& A, LaunchCfg lc, cudaStream_t s) {
+  if (D.m.fields[0].dtype == EXC_DTYPE_F32) return launch_trace_r<kFlrwSlowInterp, float, STEPPER>(D, A, lc, s);
+  if (D.m.fields[0].dtype == EXC_DTYPE_F64) return launch_trace_r<kFlrwSlowInterp, double, STEPPER>(D, A, lc, s);
+  return cudaErrorInvalidValue;   // split grids never carry the slow Interpolator
+}
+
+// The dtype of field 0 selects the instantiation (all fields of a launch share it);
+// a slow-Interpolator field anywhere in the launch selects the kernels that read it.
 template <int STEPPER>
 cudaError_t launch_trace_stepper(const DevMetric& D, const ExcTraceArgs& A, LaunchCfg lc, cudaStream_t s) {
   if (D.m.kind == EXC_METRIC_SCHWARZSCHILD)
     return launch_trace_r<EXC_METRIC_SCHWARZSCHILD, double, STEPPER>(D, A, lc, s);
+  bool slow = false;
+  for (int i = 0; i < D.m.n_fields; ++i) slow = slow || D.m.fields[i].grad_mode == EXC_GRAD_TRILINEAR;
+  if (slow) {
+    if constexpr (STEPPER == EXC_STEPPER_RK4) return trace_rk4_slow(D, A, lc, s);
+    else if constexpr (STEPPER == EXC_STEPPER_RK45) return trace_rk45_slow(D, A, lc, s);
+    else return trace_lf4_slow(D, A, lc, s);
+  }
   if (D.m.fields[0].dtype == EXC_DTYPE_F32) return launch_trace_r<EXC_METRIC_FLRW, float, STEPPER>(D, A, lc, s);
   if (D.m.fields[0].dtype == EXC_DTYPE_F32X2) {
     // split grids reach the FP64 tracer only as the mixed tracer's RK4 re-trace pass (fast build)

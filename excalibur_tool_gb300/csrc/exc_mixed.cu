@@ -383,11 +383,11 @@ __device__ __forceinline__ int endpoint(const MixParams& Pm, int fi, const doubl
   if (st) return st;
   exc_mixed_f64::InterpOut ip;
   if (f.dtype == EXC_DTYPE_F32)
-    st = exc_mixed_f64::interp_field<float>(f, Pm.D.finv[fi], s[1], s[2], s[3], s[0], ip);
+    st = exc_mixed_f64::interp_field<float, false>(f, Pm.D.finv[fi], s[1], s[2], s[3], s[0], ip);
   else if (f.dtype == EXC_DTYPE_F32X2)
-    st = exc_mixed_f64::interp_field<float2>(f, Pm.D.finv[fi], s[1], s[2], s[3], s[0], ip);
+    st = exc_mixed_f64::interp_field<float2, false>(f, Pm.D.finv[fi], s[1], s[2], s[3], s[0], ip);
   else
-    st = exc_mixed_f64::interp_field<double>(f, Pm.D.finv[fi], s[1], s[2], s[3], s[0], ip);
+    st = exc_mixed_f64::interp_field<double, false>(f, Pm.D.finv[fi], s[1], s[2], s[3], s[0], ip);
   phi = ip.val;
   return st;
 }

@@ -10,6 +10,17 @@ contraction) + the RK4 combination.
 # floating-point add/sub/mul/div (+ the periodic wrap's fmod) per RK4 photon-step
 FLOPS_PER_RK4_STEP_FLRW = 1009
 SQRT_PER_RK4_STEP_FLRW = 4
+# the same, by kind (a division or fmod costs several multiply/add slots of the FP64
+# pipe; exc_probe_fp64_rates measures how many)
+OPS_PER_RK4_STEP_FLRW = {"add": 228, "sub": 128, "mul": 492, "div": 149, "fmod": 12, "sqrt": 4}
+
+
+def fp64_pipe_slots(ops: dict, rates: dict) -> float:
+    """Multiply/add-equivalent FP64 pipe slots of an operation mix, each kind weighted by
+    the measured multiply/add rate over its own measured rate."""
+    base = rates["addmul"]
+    return (ops["add"] + ops["sub"] + ops["mul"] + ops["div"] * base / rates["div"] +
+            ops["fmod"] * base / rates["fmod"] + ops["sqrt"] * base / rates["sqrt"])
 # bytes gathered per RK4 photon-step: 4 RHS x (11 distinct grid nodes + 2 a(eta) table entries)
 NODES_PER_RHS = 11
 TABLE_ENTRIES_PER_RHS = 2

@@ -30,6 +30,18 @@ cone by ~17 % over 1000 Mpc, a smooth path-history effect), and with them the
 network's redshift error is larger (median 3e-7 against 1.8e-7 on the 20 deg
 patch), so the default pipeline leaves them out.
 
+How smooth the target is depends on the interpolator. With the fast
+interpolators' base-node gradient (piecewise constant per cell), each RK4 stage
+point that crosses a cell face as the direction moves changes that step's
+increment by a finite amount, so the traced z is rough at the pixel scale: on
+the 20 deg patch of a 128^3 field at 4096^2 pixels, adjacent-pixel second
+differences of the FP64-traced z are ~2e-7 rms, growing like the square root of
+the pixel separation (a random walk of small jumps). No smooth model reaches
+1e-7 there; the ensemble reaches ~1.4e-7 median. The slow Interpolator's
+gradient (trilinear blend of corner differences) is continuous, the map is
+smooth (second differences ~4e-9) and the same pipeline reaches a median
+|dz| of ~7e-9 with 99.99 % of audited pixels within 1e-7.
+
 Pipeline: `training_set` traces seeded uniform-random patch positions;
 `SkySurrogate.fit` trains the ensemble; `fill_sky_map` predicts all pixel
 centres, sends pixels whose ensemble spread in z exceeds `std_threshold` to the

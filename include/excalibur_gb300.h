@@ -317,6 +317,18 @@ typedef struct ExcLaunchPlan {
 int exc_autotune(const ExcMetric* metric, const ExcTraceArgs* args, const double* pristine_state,
                  ExcLaunchPlan* plan, void* stream);
 
+/* ---- FP64 pipe probe (measurement only; no reference counterpart) --------
+ * Throughput of the FP64 operations the parity build issues, measured on the
+ * current device with IEEE semantics and no FMA contraction (the parity
+ * build's flags): rates_out[EXC_PROBE_*] in operations per second over the
+ * whole GPU. A bench turns the algorithmic operation mix of a photon-step into
+ * FP64-pipe time with them (a division costs several multiply/add slots).
+ * `scratch` is a caller-owned device buffer of at least exc_probe_scratch_len()
+ * doubles. Synchronous on `stream`. */
+enum { EXC_PROBE_ADDMUL = 0, EXC_PROBE_DIV = 1, EXC_PROBE_SQRT = 2, EXC_PROBE_FMOD = 3, EXC_PROBE_N = 4 };
+int64_t exc_probe_scratch_len(void);
+int exc_probe_fp64_rates(double* scratch, int64_t n_scratch, double* rates_out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

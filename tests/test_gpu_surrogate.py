@@ -90,3 +90,66 @@ def test_sky_map_pipeline_small(cuda):
     out, report = fill_sky_map(m, wl.metric, patch, cfg, n_side=128, std_threshold=1e-5, audit_fraction=0.05)
     assert out.shape == (128 * 128, 4) and np.isfinite(out).all()
     assert report["audit_pixels"] > 0 and report["pixels"] == 128 * 128
+
+
+def _patch_metric(n, seed, slow):
+    from excalibur_tool_gb300 import workloads
+    from excalibur_tool_gb300.core.constants import one_Mpc
+    from excalibur_tool_gb300.grid.grid import Grid
+    from excalibur_tool_gb300.grid.interpolator import Interpolator
+    from excalibur_tool_gb300.grid.interpolator_4d_fast import InterpolatorFast
+    from excalibur_tool_gb300.metrics.perturbed_flrw_metric_fast import PerturbedFLRWMetricFast
+    from excalibur_tool_gb300.objects.fields import lens_plus_grf
+
+    cz = workloads.lcdm()
+    phi = lens_plus_grf(n, workloads.BOX, workloads.LENS_MASS, 5 * one_Mpc, workloads.LENS, seed=seed)
+    grid = Grid((n,) * 3, (workloads.BOX / n,) * 3, (0.0, 0.0, 0.0))
+    grid.add_field("Phi", phi)
+    ip = Interpolator(grid) if slow else InterpolatorFast(grid, boundary="periodic")
+    return PerturbedFLRWMetricFast(cz.a_of_eta, grid, ip, adot_of_eta=cz.adot_of_eta)
+
+
+def test_smooth_gradient_map_is_learnable(cuda):
+    """The base-node gradient of the fast interpolators makes the traced redshift map rough
+    at the pixel scale (RK4 stage points switch cells as the direction moves); the slow
+    Interpolator's continuous gradient does not, and on its map the surrogate's held-out
+    redshift error falls below 1e-7."""
+    from excalibur_tool_gb300 import workloads
+    from excalibur_tool_gb300.core.constants import one_Mpc
+    from excalibur_tool_gb300.surrogate.model import SkySurrogate
+    from excalibur_tool_gb300.surrogate.sky import (ExitGeometry, Patch, compose, observer_terms,
+                                                    traced_quantities, training_set)
+    from excalibur_tool_gb300.trace import TraceConfig
+
+    cz = workloads.lcdm()
+    patch = Patch((cz._eta_at_a1, *workloads.OBSERVER), tuple(workloads.LENS - workloads.OBSERVER), 10.0)
+    hi = 980 * one_Mpc   # inside the slow class's bounds [0, 63 spacings) of a 64^3 grid
+    dl = workloads.DLAMBDA
+    cfg = TraceConfig(stepper="rk4", precision="fp64_fast", dt=dl, dt_min=dl, dt_max=dl, max_steps=2 ** 62,
+                      max_iter=100_000, stop_box=((0, 0, 0), (hi, hi, hi)), a_stop=0.5)
+    geo = ExitGeometry(patch, cfg.stop_box)
+    t = (np.arange(1024) + 0.5) / 1024 * 2 - 1
+    A, B = np.meshgrid(t[480:544], t[480:544], indexing="ij")
+    block = np.stack([A.reshape(-1), B.reshape(-1)], 1)
+    rough = {}
+    for slow in (False, True):
+        metric = _patch_metric(64, 1, slow)
+        _, v = traced_quantities(metric, patch, block, cfg, geo)
+        z = v[:, 0].reshape(64, 64)
+        assert np.isfinite(z).all()
+        d2 = np.concatenate([(z[2:] - 2 * z[1:-1] + z[:-2]).ravel(), (z[:, 2:] - 2 * z[:, 1:-1] + z[:, :-2]).ravel()])
+        rough[slow] = float(np.sqrt(np.mean(d2 ** 2)))
+    print("adjacent-pixel second differences of z (rms): base-node", rough[False], "slow", rough[True])
+    assert rough[False] > 10 * rough[True]
+    metric = _patch_metric(64, 1, True)
+    uv, y, _, info = training_set(metric, patch, 65536, cfg, seed=1)
+    assert info["kept"] == 65536
+    m = SkySurrogate(n_members=4, n_out=6, seed=0)
+    m.fit(uv, y, steps=3000, batch=8192, lr=2e-3, log_every=500)
+    hold = np.random.default_rng(9).uniform(-1, 1, (4096, 2))
+    _, ref = traced_quantities(metric, patch, hold, cfg, geo)
+    mean, _ = m.predict(hold)
+    pred = compose(metric, patch, geo, hold, mean, observer_terms(metric, patch))
+    err = np.abs(pred[:, 0] - ref[:, 0])
+    print("held-out |dz|: median", np.median(err), "p95", np.percentile(err, 95), "max", err.max())
+    assert np.median(err) < 1e-7
