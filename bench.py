@@ -13,6 +13,12 @@ precision workload (4,194,304 photons, 2048x2048 directions in a 20x20 deg
 patch, Phi on a 512^3 float32 grid, seed 4) against the FP64 tracer on a
 seeded 65,536-ray subset (numpy default_rng(40)).
 
+Further keys: `roofline.fp64_pipe` (the parity tracer against the FP64 pipe, each
+operation kind weighted by its throughput measured with exc_probe_fp64_rates),
+`variants`, `batching` (multi-field RK45 launch, autotuned), `surrogate` and
+`surrogate_smooth` (learned 4096^2 sky maps on the fast and the slow
+interpolator's reading of one field, against tracing every pixel).
+
 `--impl reference` times the CPU oracle (the C restatement of the reference's
 integrate_single loop, oracle/exc_oracle.c) on all host threads over the same
 workload instead. Under torchrun (N > 1) each rank traces its own batch (weak

@@ -135,20 +135,28 @@ __device__ __forceinline__ uint64_t smem_desc_sw128(uint32_t addr) {
   return d;
 }
 
-constexpr int kTmaStages = 4;                          // K chunks in flight (192 KB: one CTA per SM)
+// Two K chunks in flight (96 KB of stages) so that two CTAs fit on an SM (and the
+// two 256-column accumulators fill its TMEM): one CTA's epilogue overlaps the
+// other's loads and MMAs.
+constexpr int kTmaStages = 2;
 constexpr int kTmaSmem = kTmaStages * kStage + 1024;  // + alignment slack
+constexpr int kGemmCtasPerSm = 2;
 
-// Fused epilogue, staged through shared memory, on all kGemmWarps warps. A warp
-// can read only its quarter of the TMEM lanes (warp w: lanes 32 (w % 4) ..), so
-// the four warps of a quarter split the 16-column chunks among them (chunk j to
-// warp group j % 4). Pass 1: each thread reads its lane (tile row) chunk by
-// chunk, applies the epilogue and writes the results into row-major tiles in
-// shared memory (the operand stages are free once the last MMA has completed).
-// Pass 2: the warps copy the tiles out with coalesced stores -- one whole
-// output row per warp instruction, and the transposed output one column (up to
-// 128 consecutive rows of ct) per pass. Row pitch: 264 BF16 / 260 FP32 elements.
-constexpr int kPitchH = 264, kPitchF = 260;
+// Fused epilogue, staged through shared memory, on all kGemmWarps warps, in
+// blocks of up to 128 columns (the staging tiles then fit in the operand stages,
+// which are free once the last MMA has completed). A warp can read only its
+// quarter of the TMEM lanes (warp w: lanes 32 (w % 4) ..), so the four warps of a
+// quarter split the 16-column chunks among them (chunk j to warp group j % 4).
+// Pass 1: each thread reads its lane (tile row) chunk by chunk, applies the
+// epilogue and writes the results into row-major tiles in shared memory. Pass 2:
+// the warps copy the tiles out with coalesced stores -- whole output rows per
+// warp instruction, and the transposed output one column (up to 128 consecutive
+// rows of ct) per pass. Row pitch: 136 BF16 / 132 FP32 elements.
+constexpr int kEpiCols = 128;
+constexpr int kPitchH = kEpiCols + 8, kPitchF = kEpiCols + 4;
 constexpr int kGemmWarps = 16;
+static_assert(2 * kTileM * kPitchH * 2 <= kTmaStages * kStage, "BF16 staging tiles must fit the stages");
+static_assert(kTileM * kPitchF * 4 <= kTmaStages * kStage, "FP32 staging tile must fit the stages");
 
 template <int EPI>
 __device__ __forceinline__ void epilogue(const ExcGemm& g, uint32_t tmem, int64_t m0, int split, int splits, int bidx,
@@ -164,78 +172,86 @@ __device__ __forceinline__ void epilogue(const ExcGemm& g, uint32_t tmem, int64_
   __nv_bfloat16* t2 = t1 + kTileM * kPitchH;                                    // second BF16 tile
   const __nv_bfloat16* Z =
       EPI == EXC_EPI_DSILU ? reinterpret_cast<const __nv_bfloat16*>(g.z_in) + bidx * g.stride_c + row * n : nullptr;
-  // pass 1
-  for (int c0 = grp * 16; c0 < n; c0 += 16 * (kGemmWarps / 4)) {
-    float v[16];
-    tmem_ld16(lane_addr + (uint32_t)c0, v);
-    if (EPI == EXC_EPI_F32 || EPI == EXC_EPI_SPLITK) {
+  const int rows = (int)(g.m - m0 < kTileM ? g.m - m0 : kTileM);
+  for (int cb = 0; cb < n; cb += kEpiCols) {
+    const int cols = n - cb < kEpiCols ? n - cb : kEpiCols;
+    if (cb) __syncthreads();   // the previous block's pass 2 has read the tiles
+    // pass 1: columns cb + c0 .. cb + c0 + 15 of this thread's row
+    for (int c0 = grp * 16; c0 < cols; c0 += 16 * (kGemmWarps / 4)) {
+      float v[16];
+      tmem_ld16(lane_addr + (uint32_t)(cb + c0), v);
+      if (EPI == EXC_EPI_F32 || EPI == EXC_EPI_SPLITK) {
 #pragma unroll
-      for (int i = 0; i < 16; i += 4)
-        *reinterpret_cast<float4*>(tf + r * kPitchF + c0 + i) = make_float4(v[i], v[i + 1], v[i + 2], v[i + 3]);
-    } else if (EPI == EXC_EPI_BIAS_SILU) {
-      const float* bias = sbias + c0;
-      __align__(16) __nv_bfloat16 zb[16], hb[16];
-#pragma unroll
-      for (int i = 0; i < 16; ++i) {
-        const float z = v[i] + bias[i];
-        zb[i] = __float2bfloat16_rn(z);
-        const float zr = __bfloat162float(zb[i]);   // the value the backward pass will see
-        hb[i] = __float2bfloat16_rn(zr * sigmoid(zr));
-      }
-      uint4* d1 = reinterpret_cast<uint4*>(t1 + r * kPitchH + c0);
-      uint4* d2 = reinterpret_cast<uint4*>(t2 + r * kPitchH + c0);
-      d1[0] = *reinterpret_cast<uint4*>(&zb[0]);
-      d1[1] = *reinterpret_cast<uint4*>(&zb[8]);
-      d2[0] = *reinterpret_cast<uint4*>(&hb[0]);
-      d2[1] = *reinterpret_cast<uint4*>(&hb[8]);
-    } else {  // EXC_EPI_DSILU
-      __align__(16) __nv_bfloat16 db[16];
-      if (row < g.m) {
-        __align__(16) __nv_bfloat16 zin[16];
-        *reinterpret_cast<uint4*>(&zin[0]) = __ldg(reinterpret_cast<const uint4*>(Z + c0));
-        *reinterpret_cast<uint4*>(&zin[8]) = __ldg(reinterpret_cast<const uint4*>(Z + c0 + 8));
+        for (int i = 0; i < 16; i += 4)
+          *reinterpret_cast<float4*>(tf + r * kPitchF + c0 + i) = make_float4(v[i], v[i + 1], v[i + 2], v[i + 3]);
+      } else if (EPI == EXC_EPI_BIAS_SILU) {
+        const float* bias = sbias + cb + c0;
+        __align__(16) __nv_bfloat16 zb[16], hb[16];
 #pragma unroll
         for (int i = 0; i < 16; ++i) {
-          const float z = __bfloat162float(zin[i]);
-          const float sg = sigmoid(z);
-          db[i] = __float2bfloat16_rn(v[i] * (sg * (1.0f + z * (1.0f - sg))));
+          const float z = v[i] + bias[i];
+          zb[i] = __float2bfloat16_rn(z);
+          const float zr = __bfloat162float(zb[i]);   // the value the backward pass will see
+          hb[i] = __float2bfloat16_rn(zr * sigmoid(zr));
         }
-      } else {
+        uint4* d1 = reinterpret_cast<uint4*>(t1 + r * kPitchH + c0);
+        uint4* d2 = reinterpret_cast<uint4*>(t2 + r * kPitchH + c0);
+        d1[0] = *reinterpret_cast<uint4*>(&zb[0]);
+        d1[1] = *reinterpret_cast<uint4*>(&zb[8]);
+        d2[0] = *reinterpret_cast<uint4*>(&hb[0]);
+        d2[1] = *reinterpret_cast<uint4*>(&hb[8]);
+      } else {  // EXC_EPI_DSILU
+        __align__(16) __nv_bfloat16 db[16];
+        if (row < g.m) {
+          __align__(16) __nv_bfloat16 zin[16];
+          *reinterpret_cast<uint4*>(&zin[0]) = __ldg(reinterpret_cast<const uint4*>(Z + cb + c0));
+          *reinterpret_cast<uint4*>(&zin[8]) = __ldg(reinterpret_cast<const uint4*>(Z + cb + c0 + 8));
 #pragma unroll
-        for (int i = 0; i < 16; ++i) db[i] = __float2bfloat16_rn(0.0f);
+          for (int i = 0; i < 16; ++i) {
+            const float z = __bfloat162float(zin[i]);
+            const float sg = sigmoid(z);
+            db[i] = __float2bfloat16_rn(v[i] * (sg * (1.0f + z * (1.0f - sg))));
+          }
+        } else {
+#pragma unroll
+          for (int i = 0; i < 16; ++i) db[i] = __float2bfloat16_rn(0.0f);
+        }
+        uint4* d1 = reinterpret_cast<uint4*>(t1 + r * kPitchH + c0);
+        d1[0] = *reinterpret_cast<uint4*>(&db[0]);
+        d1[1] = *reinterpret_cast<uint4*>(&db[8]);
       }
-      uint4* d1 = reinterpret_cast<uint4*>(t1 + r * kPitchH + c0);
-      d1[0] = *reinterpret_cast<uint4*>(&db[0]);
-      d1[1] = *reinterpret_cast<uint4*>(&db[8]);
     }
-  }
-  __syncthreads();
-  // pass 2: rows (coalesced), warp w handles rows w, w + kGemmWarps, ...
-  const int rows = (int)(g.m - m0 < kTileM ? g.m - m0 : kTileM);
-  if (EPI == EXC_EPI_F32 || EPI == EXC_EPI_SPLITK) {
-    float* C = reinterpret_cast<float*>(g.c) +
-               (EPI == EXC_EPI_SPLITK ? ((int64_t)bidx * splits + split) * g.m * n : bidx * g.stride_c);
-    for (int rr = warp; rr < rows; rr += kGemmWarps)
-      for (int c = lane * 4; c < n; c += 128)
-        *reinterpret_cast<float4*>(C + (m0 + rr) * n + c) = *reinterpret_cast<const float4*>(tf + rr * kPitchF + c);
-  } else {
-    __nv_bfloat16* outs[2] = {reinterpret_cast<__nv_bfloat16*>(g.c), EPI == EXC_EPI_BIAS_SILU
-                                                                        ? reinterpret_cast<__nv_bfloat16*>(g.c2)
-                                                                        : nullptr};
-    const __nv_bfloat16* tiles[2] = {t1, t2};
-    for (int o = 0; o < 2; ++o) {
-      if (!outs[o]) continue;
-      __nv_bfloat16* C = outs[o] + bidx * g.stride_c;
+    __syncthreads();
+    // pass 2: rows (coalesced)
+    if (EPI == EXC_EPI_F32 || EPI == EXC_EPI_SPLITK) {
+      float* C = reinterpret_cast<float*>(g.c) +
+                 (EPI == EXC_EPI_SPLITK ? ((int64_t)bidx * splits + split) * g.m * n : bidx * g.stride_c) + cb;
+      // one row (up to 128 FP32 = 512 B) per warp instruction
       for (int rr = warp; rr < rows; rr += kGemmWarps)
-        for (int c = lane * 8; c < n; c += 256)
-          *reinterpret_cast<uint4*>(C + (m0 + rr) * n + c) = *reinterpret_cast<const uint4*>(tiles[o] + rr * kPitchH + c);
-    }
-    if (g.ct) {
-      // the transposed output: SiLU values (BIAS_SILU) or the masked gradient (DSILU)
-      const __nv_bfloat16* src = EPI == EXC_EPI_BIAS_SILU ? t2 : t1;
-      __nv_bfloat16* T = reinterpret_cast<__nv_bfloat16*>(g.ct) + bidx * g.stride_ct + m0;
-      for (int cc = warp; cc < n; cc += kGemmWarps)
-        for (int rr = lane; rr < rows; rr += 32) T[(int64_t)cc * g.ldt + rr] = src[rr * kPitchH + cc];
+        for (int c = lane * 4; c < cols; c += 128)
+          *reinterpret_cast<float4*>(C + (m0 + rr) * n + c) = *reinterpret_cast<const float4*>(tf + rr * kPitchF + c);
+    } else {
+      __nv_bfloat16* outs[2] = {reinterpret_cast<__nv_bfloat16*>(g.c), EPI == EXC_EPI_BIAS_SILU
+                                                                          ? reinterpret_cast<__nv_bfloat16*>(g.c2)
+                                                                          : nullptr};
+      const __nv_bfloat16* tiles[2] = {t1, t2};
+      // two rows (up to 128 BF16 = 256 B each) per warp instruction
+      const int half = lane >> 4, l16 = lane & 15;
+      for (int o = 0; o < 2; ++o) {
+        if (!outs[o]) continue;
+        __nv_bfloat16* C = outs[o] + bidx * g.stride_c + cb;
+        for (int rr = 2 * warp + half; rr < rows; rr += 2 * kGemmWarps)
+          for (int c = l16 * 8; c < cols; c += 128)
+            *reinterpret_cast<uint4*>(C + (m0 + rr) * n + c) =
+                *reinterpret_cast<const uint4*>(tiles[o] + rr * kPitchH + c);
+      }
+      if (g.ct) {
+        // the transposed output: SiLU values (BIAS_SILU) or the masked gradient (DSILU)
+        const __nv_bfloat16* src = EPI == EXC_EPI_BIAS_SILU ? t2 : t1;
+        __nv_bfloat16* T = reinterpret_cast<__nv_bfloat16*>(g.ct) + bidx * g.stride_ct + (int64_t)cb * g.ldt + m0;
+        for (int cc = warp; cc < cols; cc += kGemmWarps)
+          for (int rr = lane; rr < rows; rr += 32) T[(int64_t)cc * g.ldt + rr] = src[rr * kPitchH + cc];
+      }
     }
   }
 }
@@ -246,7 +262,7 @@ __device__ __forceinline__ void epilogue(const ExcGemm& g, uint32_t tmem, int64_
 // consumes: four tcgen05.mma per chunk into the TMEM accumulator and a commit to
 // empty[s] that frees the stage; a final commit to `done` releases the epilogue.
 template <int EPI>
-__global__ void __launch_bounds__(kGemmWarps * 32, 1) gemm_tma_kernel(const __grid_constant__ CUtensorMap tmA,
+__global__ void __launch_bounds__(kGemmWarps * 32, kGemmCtasPerSm) gemm_tma_kernel(const __grid_constant__ CUtensorMap tmA,
                                                                       const __grid_constant__ CUtensorMap tmB,
                                                                       const ExcGemm g) {
   extern __shared__ uint8_t smem_raw[];
