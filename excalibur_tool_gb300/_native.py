@@ -76,7 +76,7 @@ class ExcTraceArgs(C.Structure):
                 ("queue", C.c_void_p), ("abort_flag", C.c_void_p), ("deadline_cycles", C.c_int64)]
 
 
-GEN_PATCH_GRID, GEN_PATCH_POINTS, GEN_CONE_GRID, GEN_FULL_SKY = 0, 1, 2, 3
+GEN_PATCH_GRID, GEN_PATCH_POINTS, GEN_CONE_GRID, GEN_FULL_SKY, GEN_CONE_RANDOM, GEN_IMPACT_BINS = 0, 1, 2, 3, 4, 5
 
 
 class ExcPhotonGen(C.Structure):
@@ -84,7 +84,8 @@ class ExcPhotonGen(C.Structure):
                 ("n", C.c_int64), ("origin", C.c_double * 4), ("axis", C.c_double * 3), ("e1", C.c_double * 3),
                 ("e2", C.c_double * 3), ("half", C.c_double), ("rot_axis", C.c_double * 3), ("rot_cos", C.c_double),
                 ("rot_sin", C.c_double), ("uv", C.c_void_p), ("seed", C.c_uint64), ("speed", C.c_double),
-                ("sign", C.c_double)]
+                ("sign", C.c_double), ("n_bins", C.c_int32), ("random_phi", C.c_int32), ("spherical", C.c_int32),
+                ("reserved", C.c_int32), ("b_edges", C.c_void_p), ("bin_offsets", C.c_void_p)]
 
 
 EXC_TUNE_MAX_TRIALS = 32

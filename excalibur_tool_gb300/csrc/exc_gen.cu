@@ -28,9 +28,65 @@ __device__ __forceinline__ uint64_t splitmix64(uint64_t x) {
 // uniform in [0, 1) from the top 53 bits
 __device__ __forceinline__ double unit53(uint64_t x) { return (double)(x >> 11) * (1.0 / 9007199254740992.0); }
 
+// CONE_* rotation of the cone-frame direction v onto the cone axis (Rodrigues,
+// the host's _rotate_to_direction).
+__device__ __forceinline__ void cone_rotate(const ExcPhotonGen& g, const double v[3], double d[3]) {
+  const double* k = g.rot_axis;
+  const double kv[3] = {k[1] * v[2] - k[2] * v[1], k[2] * v[0] - k[0] * v[2], k[0] * v[1] - k[1] * v[0]};
+  const double vk = (v[0] * k[0] + v[1] * k[1]) + v[2] * k[2];
+  for (int c = 0; c < 3; ++c) d[c] = (v[c] * g.rot_cos + kv[c] * g.rot_sin) + k[c] * vk * (1.0 - g.rot_cos);
+}
+
+// The bin of photon i: the largest ib with bin_offsets[ib] <= i (offsets non-decreasing).
+__device__ __forceinline__ int find_bin(const ExcPhotonGen& g, int64_t i) {
+  int lo = 0, hi = g.n_bins - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (g.bin_offsets[mid] <= i) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
 __global__ void gen_kernel(const ExcPhotonGen g, int64_t n, double* states) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     double d[3];
+    double* s = states + i * 8;
+    s[0] = g.origin[0];
+    s[1] = g.origin[1];
+    s[2] = g.origin[2];
+    s[3] = g.origin[3];
+    s[4] = 0.0;
+    if (g.mode == EXC_GEN_IMPACT_BINS) {
+      // generate_impact_parameter_bins (photons.py:663-701): screen point, velocity c k
+      const int ib = find_bin(g, i);
+      const int64_t j = i - g.bin_offsets[ib], nph = g.bin_offsets[ib + 1] - g.bin_offsets[ib];
+      const uint64_t h = splitmix64(g.seed ^ splitmix64((uint64_t)i));
+      const double p = g.random_phi ? 2.0 * M_PI * unit53(splitmix64(h)) : (double)j * (2.0 * M_PI / (double)nph);
+      const double b1 = g.b_edges[ib], b2 = g.b_edges[ib + 1];
+      const double b = sqrt(unit53(h) * (b2 * b2 - b1 * b1) + b1 * b1);
+      const double cp = cos(p), sp = sin(p);
+      double x[3], v[3];
+      for (int k = 0; k < 3; ++k) {
+        x[k] = g.origin[1 + k] + b * (cp * g.e1[k] + sp * g.e2[k]);
+        v[k] = g.axis[k] * g.speed;
+      }
+      if (!g.spherical) {
+        for (int k = 0; k < 3; ++k) { s[1 + k] = x[k]; s[5 + k] = v[k]; }
+        continue;
+      }
+      // cartesian_to_spherical / cartesian_velocity_to_spherical (core/coordinates.py:31-84)
+      const double rho2 = x[0] * x[0] + x[1] * x[1];
+      const double r2 = rho2 + x[2] * x[2];
+      const double r = sqrt(r2);
+      s[1] = r;
+      s[2] = acos(fmin(1.0, fmax(-1.0, x[2] / r)));
+      s[3] = atan2(x[1], x[0]);
+      s[5] = (x[0] * v[0] + x[1] * v[1] + x[2] * v[2]) / r;
+      s[6] = (x[2] * (x[0] * v[0] + x[1] * v[1]) - rho2 * v[2]) / (r * r * sqrt(rho2));
+      s[7] = (x[0] * v[1] - x[1] * v[0]) / rho2;
+      continue;
+    }
     if (g.mode == EXC_GEN_PATCH_GRID || g.mode == EXC_GEN_PATCH_POINTS) {
       double A, B;
       if (g.mode == EXC_GEN_PATCH_GRID) {
@@ -43,15 +99,20 @@ __global__ void gen_kernel(const ExcPhotonGen g, int64_t n, double* states) {
       }
       const double ah = A * g.half, bh = B * g.half;
       for (int k = 0; k < 3; ++k) d[k] = (g.axis[k] + ah * g.e1[k]) + bh * g.e2[k];
-    } else if (g.mode == EXC_GEN_CONE_GRID) {
-      const int64_t it = i / g.n_phi, ip = i - it * g.n_phi;
-      const double th = ((double)it + 0.5) * g.half / g.n_theta;
-      const double ph = 2.0 * M_PI * (double)ip / g.n_phi;
+    } else if (g.mode == EXC_GEN_CONE_GRID || g.mode == EXC_GEN_CONE_RANDOM) {
+      double th, ph;
+      if (g.mode == EXC_GEN_CONE_GRID) {
+        const int64_t it = i / g.n_phi, ip = i - it * g.n_phi;
+        th = ((double)it + 0.5) * g.half / g.n_theta;
+        ph = 2.0 * M_PI * (double)ip / g.n_phi;
+      } else {
+        // generate_cone_random (photons.py:84-88): theta uniform in [0, cone), azimuth uniform
+        const uint64_t h = splitmix64(g.seed ^ splitmix64((uint64_t)i));
+        th = g.half * unit53(h);
+        ph = 2.0 * M_PI * unit53(splitmix64(h));
+      }
       const double v[3] = {sin(th) * cos(ph), sin(th) * sin(ph), cos(th)};
-      const double* k = g.rot_axis;
-      const double kv[3] = {k[1] * v[2] - k[2] * v[1], k[2] * v[0] - k[0] * v[2], k[0] * v[1] - k[1] * v[0]};
-      const double vk = (v[0] * k[0] + v[1] * k[1]) + v[2] * k[2];
-      for (int c = 0; c < 3; ++c) d[c] = (v[c] * g.rot_cos + kv[c] * g.rot_sin) + k[c] * vk * (1.0 - g.rot_cos);
+      cone_rotate(g, v, d);
     } else {
       // uniform on the sphere: z uniform in [-1, 1), azimuth uniform in [0, 2 pi)
       const uint64_t h = splitmix64(g.seed ^ splitmix64((uint64_t)i));
@@ -63,12 +124,6 @@ __global__ void gen_kernel(const ExcPhotonGen g, int64_t n, double* states) {
       d[2] = z;
     }
     const double nrm = sqrt((d[0] * d[0] + d[1] * d[1]) + d[2] * d[2]);
-    double* s = states + i * 8;
-    s[0] = g.origin[0];
-    s[1] = g.origin[1];
-    s[2] = g.origin[2];
-    s[3] = g.origin[3];
-    s[4] = 0.0;
     for (int k = 0; k < 3; ++k) s[5 + k] = (d[k] / nrm) * g.speed;
   }
 }
@@ -81,7 +136,9 @@ extern "C" int64_t exc_gen_count(const ExcPhotonGen* g) {
     case EXC_GEN_PATCH_GRID: return (int64_t)g->n_side * g->n_side;
     case EXC_GEN_CONE_GRID: return (int64_t)g->n_theta * g->n_phi;
     case EXC_GEN_PATCH_POINTS:
-    case EXC_GEN_FULL_SKY: return g->n;
+    case EXC_GEN_FULL_SKY:
+    case EXC_GEN_CONE_RANDOM:
+    case EXC_GEN_IMPACT_BINS: return g->n;
     default: return -1;
   }
 }
@@ -100,6 +157,10 @@ extern "C" int exc_generate_photons(const ExcMetric* metric, const ExcPhotonGen*
   if ((g->mode == EXC_GEN_PATCH_GRID && g->n_side < 1) || (g->mode == EXC_GEN_CONE_GRID && (g->n_theta < 1 || g->n_phi < 1)) ||
       (g->mode == EXC_GEN_PATCH_POINTS && !g->uv)) {
     exc::set_last_error("generate: sizes must be >= 1 (and uv given for PATCH_POINTS)");
+    return EXC_ERR_INVALID;
+  }
+  if (g->mode == EXC_GEN_IMPACT_BINS && (g->n_bins < 1 || !g->b_edges || !g->bin_offsets)) {
+    exc::set_last_error("generate: IMPACT_BINS needs n_bins >= 1, b_edges and bin_offsets (device arrays)");
     return EXC_ERR_INVALID;
   }
   if (n == 0) return EXC_SUCCESS;

@@ -347,10 +347,9 @@ class Photons:
         g.uv = self._uv_keep.data_ptr()
         return self._device_generate(g, g.n)
 
-    def device_polar_grid(self, n_theta, n_phi, origin, central_direction, cone_angle, sign=-1.0):
-        """generate_polar_grid (cartesian basis) computed on the device."""
-        from .. import _native as N
-
+    @staticmethod
+    def _cone_rotation(g, central_direction):
+        """Rodrigues rotation of +z onto the cone axis (the host's _rotate_to_direction)."""
         t = np.asarray(central_direction, dtype=float)
         t = t / np.linalg.norm(t)
         z = np.array([0.0, 0.0, 1.0])
@@ -362,13 +361,77 @@ class Photons:
             kr = np.cross(z, t)
             kr = kr / np.linalg.norm(kr)
             ca, sa = float(np.dot(z, t)), float(np.linalg.norm(np.cross(z, t)))
-        g = self._gen_base(N.GEN_CONE_GRID, origin, sign)
-        g.n_theta, g.n_phi = int(n_theta), int(n_phi)
-        g.half = float(cone_angle)
         for i in range(3):
             g.rot_axis[i] = kr[i]
         g.rot_cos, g.rot_sin = ca, sa
+
+    def device_polar_grid(self, n_theta, n_phi, origin, central_direction, cone_angle, sign=-1.0):
+        """generate_polar_grid (cartesian basis) computed on the device."""
+        from .. import _native as N
+
+        g = self._gen_base(N.GEN_CONE_GRID, origin, sign)
+        g.n_theta, g.n_phi = int(n_theta), int(n_phi)
+        g.half = float(cone_angle)
+        self._cone_rotation(g, central_direction)
         return self._device_generate(g, int(n_theta) * int(n_phi))
+
+    def device_cone_random(self, n_photons, origin, central_direction, cone_angle, seed=0, sign=-1.0):
+        """generate_cone_random on the device: theta uniform in [0, cone_angle), azimuth uniform,
+        from the counter-based generator (seeded; not numpy's stream)."""
+        from .. import _native as N
+
+        g = self._gen_base(N.GEN_CONE_RANDOM, origin, sign)
+        g.n = int(n_photons)
+        g.half = float(cone_angle)
+        g.seed = int(seed) & ((1 << 64) - 1)
+        self._cone_rotation(g, central_direction)
+        return self._device_generate(g, g.n)
+
+    def device_impact_parameter_bins(self, origin, central_direction, b_edges, n_per_bin, *, random_phi=True,
+                                     seed=0, u0_sign=-1.0):
+        """generate_impact_parameter_bins on the device (photons.py:570-701): parallel rays along
+        the axis from screen points in impact-parameter annuli (b area-uniform per bin; azimuth
+        random or evenly spaced), states in the metric's coordinates (spherical-like origins
+        [t, r, theta, phi] are converted as the reference does). Random numbers come from the
+        counter-based generator (seeded; not numpy's stream)."""
+        import torch
+
+        from .. import _native as N
+
+        origin = np.asarray(origin, dtype=float)
+        b_edges = np.asarray(b_edges, dtype=float)
+        if b_edges.ndim != 1 or b_edges.size < 2:
+            raise ValueError("b_edges must be a 1D array of length >= 2")
+        if np.any(~np.isfinite(b_edges)) or np.any(b_edges[1:] <= b_edges[:-1]) or b_edges[0] < 0:
+            raise ValueError("b_edges must be finite, strictly increasing and >= 0")
+        nbins = b_edges.size - 1
+        n_list = [int(n_per_bin)] * nbins if isinstance(n_per_bin, (int, np.integer)) else [int(x) for x in n_per_bin]
+        if len(n_list) != nbins or any(n < 0 for n in n_list):
+            raise ValueError("n_per_bin must be a non-negative int or a list with length len(b_edges)-1")
+        k = np.asarray(central_direction, dtype=float).reshape(3)
+        k = k / np.linalg.norm(k)
+        up = np.array([0.0, 0.0, 1.0]) if abs(np.dot(k, [0, 0, 1.0])) <= 0.95 else np.array([0.0, 1.0, 0.0])
+        e1 = np.cross(up, k)
+        e1 /= np.linalg.norm(e1)
+        e2 = np.cross(k, e1)
+        spherical = self._origin_looks_spherical(origin)
+        o = origin.copy()
+        if spherical:
+            r0, th0, ph0 = o[1], o[2], o[3]
+            o[1:4] = [r0 * np.sin(th0) * np.cos(ph0), r0 * np.sin(th0) * np.sin(ph0), r0 * np.cos(th0)]
+        g = self._gen_base(N.GEN_IMPACT_BINS, o, u0_sign)
+        offsets = np.concatenate([[0], np.cumsum(n_list)]).astype(np.int64)
+        g.n = int(offsets[-1])
+        if g.n == 0:
+            return torch.empty((0, 8), dtype=torch.float64, device=torch.device("cuda", torch.cuda.current_device()))
+        dev = torch.device("cuda", torch.cuda.current_device())
+        self._bins_keep = (torch.as_tensor(b_edges, device=dev), torch.as_tensor(offsets, device=dev))
+        g.b_edges, g.bin_offsets = self._bins_keep[0].data_ptr(), self._bins_keep[1].data_ptr()
+        g.n_bins, g.random_phi, g.spherical = nbins, int(bool(random_phi)), int(spherical)
+        g.seed = int(seed) & ((1 << 64) - 1)
+        for i in range(3):
+            g.axis[i], g.e1[i], g.e2[i] = k[i], e1[i], e2[i]
+        return self._device_generate(g, g.n)
 
     def device_full_sky(self, n_photons, origin, seed, sign=-1.0):
         """Uniform directions on the sphere from the device's counter-based generator (seeded;

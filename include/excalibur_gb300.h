@@ -265,22 +265,40 @@ int exc_trace_noalloc(const ExcMetric* metric, const ExcTraceArgs* args, void* s
  *                (splitmix64 of seed and photon index; not numpy's stream).
  * u_spatial = speed * d; origin (eta, x, y, z) for every photon; u^0 = sign * |u^0|.
  * status ([n], optional) gets the null initialisation's status. */
-enum { EXC_GEN_PATCH_GRID = 0, EXC_GEN_PATCH_POINTS = 1, EXC_GEN_CONE_GRID = 2, EXC_GEN_FULL_SKY = 3 };
+/* EXC_GEN_CONE_RANDOM (Photons.generate_cone_random, photon/photons.py:33-157): n
+ *   directions with theta uniform in [0, half) from the cone axis and azimuth uniform in
+ *   [0, 2 pi), rotated like CONE_GRID; counter-based random numbers (seed, photon index),
+ *   so the stream is not numpy's.
+ * EXC_GEN_IMPACT_BINS (Photons.generate_impact_parameter_bins, photons.py:570-701): parallel
+ *   rays along `axis` from screen points origin + b (cos p e1 + sin p e2), photon i in the bin
+ *   ib with bin_offsets[ib] <= i < bin_offsets[ib + 1]; b uniform in area in
+ *   [b_edges[ib], b_edges[ib + 1]], p uniform in [0, 2 pi) (random_phi) or j 2 pi / n_ib for
+ *   the bin's j-th photon; `spherical` converts positions and velocities to (r, theta, phi)
+ *   with the reference's formulas (core/coordinates.py:31-84), origin[1..3] then being the
+ *   cartesian observer. n = bin_offsets[n_bins]. */
+enum { EXC_GEN_PATCH_GRID = 0, EXC_GEN_PATCH_POINTS = 1, EXC_GEN_CONE_GRID = 2, EXC_GEN_FULL_SKY = 3,
+       EXC_GEN_CONE_RANDOM = 4, EXC_GEN_IMPACT_BINS = 5 };
 typedef struct ExcPhotonGen {
   int32_t mode;
   int32_t n_side;            /* PATCH_GRID */
   int32_t n_theta, n_phi;    /* CONE_GRID */
-  int64_t n;                 /* PATCH_POINTS, FULL_SKY */
+  int64_t n;                 /* PATCH_POINTS, FULL_SKY, CONE_RANDOM, IMPACT_BINS */
   double origin[4];
   double axis[3];
   double e1[3], e2[3];       /* PATCH_*: tangent basis */
-  double half;               /* PATCH_*: tan(patch / 2); CONE_GRID: cone half-angle (rad) */
-  double rot_axis[3];        /* CONE_GRID rotation */
+  double half;               /* PATCH_*: tan(patch / 2); CONE_*: cone half-angle (rad) */
+  double rot_axis[3];        /* CONE_* rotation */
   double rot_cos, rot_sin;
   const double* uv;          /* PATCH_POINTS */
-  uint64_t seed;             /* FULL_SKY */
+  uint64_t seed;             /* FULL_SKY, CONE_RANDOM, IMPACT_BINS */
   double speed;
   double sign;
+  int32_t n_bins;            /* IMPACT_BINS */
+  int32_t random_phi;
+  int32_t spherical;
+  int32_t reserved;
+  const double* b_edges;     /* [n_bins + 1], device */
+  const int64_t* bin_offsets;  /* [n_bins + 1], device, cumulative photon counts from 0 */
 } ExcPhotonGen;
 
 /* Number of photons a generator produces. */
