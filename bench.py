@@ -656,11 +656,13 @@ def run_surrogate(args, dev, stream, peaks, fp64_rays_s):
 def run_surrogate_smooth(args, dev):
     """The same pipeline on the same field read through the reference's slow Interpolator
     (grid/interpolator.py, continuous trilinear-blended gradient): training, fallback and audit
-    rays traced with the fast FP64 build; every-pixel reference = the parity FP64 rate measured
-    on a 65,536-ray sample of the same patch."""
+    rays traced with the guarded mixed tracer; every-pixel reference = the parity FP64 rate
+    measured on a 65,536-ray sample of the same patch, on which the mixed tracer's errors
+    against the parity build are stated too."""
     import dataclasses
     import torch
 
+    from excalibur_tool_gb300 import _native as N
     from excalibur_tool_gb300 import workloads
     from excalibur_tool_gb300.core.constants import one_Mpc
     from excalibur_tool_gb300.grid.grid import Grid
@@ -680,7 +682,7 @@ def run_surrogate_smooth(args, dev):
     # the slow class's bounds are [0, (n-1) spacing): stop at 990 Mpc, inside the last cell
     hi = 990 * one_Mpc
     dl = workloads.DLAMBDA
-    cfg = TraceConfig(stepper="rk4", precision="fp64_fast", dt=dl, dt_min=dl, dt_max=dl, max_steps=2 ** 62,
+    cfg = TraceConfig(stepper="rk4", precision="mixed", dt=dl, dt_min=dl, dt_max=dl, max_steps=2 ** 62,
                       max_iter=100_000, stop_box=((0, 0, 0), (hi, hi, hi)), a_stop=0.5,
                       lens_center=tuple(workloads.LENS))
     patch = Patch((cz._eta_at_a1, *workloads.OBSERVER), tuple(workloads.LENS - workloads.OBSERVER), 20.0)
@@ -692,12 +694,22 @@ def run_surrogate_smooth(args, dev):
     r = trace_batch(metric, sample, parity)
     torch.cuda.synchronize()
     fp64_rays_s = sample.shape[0] / (time.perf_counter() - t0)
+    trace_batch(metric, sample[:4096], cfg)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    rm = trace_batch(metric, sample, cfg)
+    torch.cuda.synchronize()
+    mixed_rays_s = sample.shape[0] / (time.perf_counter() - t0)
+    raw = trace_batch(metric, sample, dataclasses.replace(cfg, precision="mixed_raw"))
+    retrace = float((raw.status == N.PH_RETRACE).float().mean())
     out = {"workload": f"{args.map_side}x{args.map_side} map of the same 20x20 deg patch and field (seed 1, 128^3 "
                        "float64) read through the slow Interpolator (continuous gradient), box stop at 990 Mpc; "
-                       "training, fallback and audit rays traced with the fast FP64 build",
+                       "training, fallback and audit rays traced with the guarded mixed tracer",
            "fp64_parity_rays_per_s": fp64_rays_s,
            "fp64_parity_sample": "65,536 pixel centres (256 x 256) of the patch, one launch",
-           "fp64_parity_status_counts": np.bincount(r.status.cpu().numpy(), minlength=12).tolist()}
+           "fp64_parity_status_counts": np.bincount(r.status.cpu().numpy(), minlength=12).tolist(),
+           "mixed_on_sample": {"rays_per_s": mixed_rays_s, "speedup_vs_fp64": mixed_rays_s / fp64_rays_s,
+                               "retrace_fraction": retrace, **errors_vs(r, rm)}}
     out.update(_surrogate_map(args, metric, patch, cfg, fp64_rays_s, args.smooth_train_steps))
     return out
 

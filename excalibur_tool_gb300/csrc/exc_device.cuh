@@ -269,6 +269,31 @@ __device__ __forceinline__ void slow_gradient(const ExcField& f, const double* f
 #undef EXC_IDX
 }
 
+// Interpolator.interpolate on a 3-D field (grid/interpolator.py:13-69): the value
+// alone, for callers that need Phi but not its gradient (the mixed tracer's
+// FP64 endpoint quantities). Same arithmetic as interp_slow's 3-D value.
+template <class FT>
+__device__ __forceinline__ int slow_value3(const ExcField& f, double x, double y, double z, double& val) {
+  const FT* d = (const FT*)f.data;
+  const int64_t nx = f.n[0], ny = f.n[1], nz = f.n[2];
+  const double rx = (x - f.origin[0]) / f.spacing[0];
+  const double ry = (y - f.origin[1]) / f.spacing[1];
+  const double rz = (z - f.origin[2]) / f.spacing[2];
+  if (rx < 0.0 || rx >= (double)(nx - 1) || ry < 0.0 || ry >= (double)(ny - 1) || rz < 0.0 ||
+      rz >= (double)(nz - 1))
+    return EXC_PH_OUTSIDE_GRID;
+  if (!isfinite(rx) || !isfinite(ry) || !isfinite(rz)) return EXC_PH_NONFINITE;
+  const double flx = floor(rx), fly = floor(ry), flz = floor(rz);
+  const int64_t i0 = (int64_t)flx, j0 = (int64_t)fly, k0 = (int64_t)flz;
+#define EXC_IDX(i, j, k) (((int64_t)(i) * ny + (j)) * nz + (k))
+  val = trilinear(ldf(d, EXC_IDX(i0, j0, k0)), ldf(d, EXC_IDX(i0 + 1, j0, k0)), ldf(d, EXC_IDX(i0, j0 + 1, k0)),
+                  ldf(d, EXC_IDX(i0, j0, k0 + 1)), ldf(d, EXC_IDX(i0 + 1, j0 + 1, k0)),
+                  ldf(d, EXC_IDX(i0 + 1, j0, k0 + 1)), ldf(d, EXC_IDX(i0, j0 + 1, k0 + 1)),
+                  ldf(d, EXC_IDX(i0 + 1, j0 + 1, k0 + 1)), rx - flx, ry - fly, rz - flz);
+#undef EXC_IDX
+  return 0;
+}
+
 // Interpolator.value_gradient_and_time_derivative (grid/interpolator.py:198-206)
 // for an ExcField with grad_mode EXC_GRAD_TRILINEAR. Unlike the fast classes,
 // the slow one raises only for a position outside the bounds: a NaN grid value

@@ -542,7 +542,13 @@ template <int STEPPER>
 cudaError_t launch_trace_slow(const DevMetric& D, const ExcTraceArgs& A, LaunchCfg lc, cudaStream_t s) {
   if (D.m.fields[0].dtype == EXC_DTYPE_F32) return launch_trace_r<kFlrwSlowInterp, float, STEPPER>(D, A, lc, s);
   if (D.m.fields[0].dtype == EXC_DTYPE_F64) return launch_trace_r<kFlrwSlowInterp, double, STEPPER>(D, A, lc, s);
-  return cudaErrorInvalidValue;   // split grids never carry the slow Interpolator
+  if (D.m.fields[0].dtype == EXC_DTYPE_F32X2) {
+    // split grids reach the FP64 tracer only as the mixed tracer's RK4 re-trace pass (fast build)
+    if constexpr (STEPPER == EXC_STEPPER_RK4 && EXC_FAST) {
+      if (!A.records) return launch_trace_t<kFlrwSlowInterp, float2, STEPPER, false>(D, A, lc, s);
+    }
+  }
+  return cudaErrorInvalidValue;
 }
 
 // The dtype of field 0 selects the instantiation (all fields of a launch share it);

@@ -101,6 +101,7 @@ struct MixField {
   float s[3];        // spacing (m)
   df inv_s[3];       // 1 / spacing as double-float
   float inv_2s[3];   // 1 / (2 spacing)
+  int slow;          // grad_mode EXC_GRAD_TRILINEAR (the slow Interpolator)
 };
 
 // Constants that multiply every step's background (Hubble) terms are kept as
@@ -289,11 +290,68 @@ __device__ __forceinline__ int interp_f32(const MixField& F, const Stage& B, flo
   return 0;
 }
 
+// The slow Interpolator (grid/interpolator.py:13-158, grad_mode EXC_GRAD_TRILINEAR)
+// at base cell + offset: trilinear value, and the gradient as the trilinear blend
+// of central differences at the cell's eight corners (base index clipped to
+// [1, n-2], each corner clipped again, weights from the unclipped fraction).
+// Value and gradient are continuous across interior cell faces, so no window
+// check is needed there; the formula changes only at the bounds rel = 0, n-1
+// and at the clip faces rel = 1, n-2, and a stage point within the error
+// window of one of those (cells 0, 1, n-3, n-2 of an axis) is handed back.
+__device__ __forceinline__ int interp_f32_slow(const MixField& F, const Stage& B, float ox, float oy, float oz,
+                                               float w0, float& val, float& gx, float& gy, float& gz) {
+  float fx, fy, fz;
+  bool nearx = false, neary = false, nearz = false;
+  const int ix = B.cx + stage_cell(B.fx, B.lx, ox, B.wx + w0, fx, nearx);
+  const int iy = B.cy + stage_cell(B.fy, B.ly, oy, B.wy + w0, fy, neary);
+  const int iz = B.cz + stage_cell(B.fz, B.lz, oz, B.wz + w0, fz, nearz);
+  const int nx = F.n[0], ny = F.n[1], nz = F.n[2];
+  if ((nearx && (ix <= 1 || ix >= nx - 3)) || (neary && (iy <= 1 || iy >= ny - 3)) ||
+      (nearz && (iz <= 1 || iz >= nz - 3)))
+    return EXC_PH_RETRACE;
+  if (ix < 0 || ix > nx - 2 || iy < 0 || iy > ny - 2 || iz < 0 || iz > nz - 2) return EXC_PH_OUTSIDE_GRID;
+  const int sy = nz, sx = ny * nz;
+  const int b = ix * sx + iy * sy + iz;
+  const float c000 = ld32(F, b), c100 = ld32(F, b + sx), c010 = ld32(F, b + sy), c001 = ld32(F, b + 1);
+  const float c110 = ld32(F, b + sx + sy), c101 = ld32(F, b + sx + 1), c011 = ld32(F, b + sy + 1);
+  const float c111 = ld32(F, b + sx + sy + 1);
+  const float c00 = fmaf(fx, c100 - c000, c000), c10 = fmaf(fx, c110 - c010, c010);
+  const float c01 = fmaf(fx, c101 - c001, c001), c11 = fmaf(fx, c111 - c011, c011);
+  const float c0 = fmaf(fy, c10 - c00, c00), c1 = fmaf(fy, c11 - c01, c01);
+  val = fmaf(fz, c1 - c0, c0);
+  // corner indices (clipped) and weights
+  const int bx = min(max(ix, 1), nx - 2), by = min(max(iy, 1), ny - 2), bz = min(max(iz, 1), nz - 2);
+  const int X[2] = {bx, min(bx + 1, nx - 2)}, Y[2] = {by, min(by + 1, ny - 2)}, Z[2] = {bz, min(bz + 1, nz - 2)};
+  const float WX[2] = {1.0f - fx, fx}, WY[2] = {1.0f - fy, fy}, WZ[2] = {1.0f - fz, fz};
+  float sgx = 0.0f, sgy = 0.0f, sgz = 0.0f;
+#pragma unroll
+  for (int a = 0; a < 2; ++a)
+#pragma unroll
+    for (int e = 0; e < 2; ++e)
+#pragma unroll
+      for (int c = 0; c < 2; ++c) {
+        const float w = WX[a] * WY[e] * WZ[c];
+        const int q = X[a] * sx + Y[e] * sy + Z[c];
+        // central differences: hi-plane difference plus (split grids) the lo-plane one
+        const float2 xp = ld32x2(F, q + sx), xm = ld32x2(F, q - sx);
+        const float2 yp = ld32x2(F, q + sy), ym = ld32x2(F, q - sy);
+        const float2 zp = ld32x2(F, q + 1), zm = ld32x2(F, q - 1);
+        sgx = fmaf(w, (xp.x - xm.x) + (xp.y - xm.y), sgx);
+        sgy = fmaf(w, (yp.x - ym.x) + (yp.y - ym.y), sgy);
+        sgz = fmaf(w, (zp.x - zm.x) + (zp.y - zm.y), sgz);
+      }
+  gx = sgx * F.inv_2s[0];
+  gy = sgy * F.inv_2s[1];
+  gz = sgz * F.inv_2s[2];
+  return 0;
+}
+
 // du^mu/dlambda in FP32 (perturbed_flrw_metric_fast.py:7-99); u in SI.
 // The spatial part is returned split as du_i = -(hub * u_i + L_i): `hub` is
 // the Hubble drag coefficient 2 (adot/a) u^0 and L the gradient (lensing)
 // terms, so the caller can integrate the velocity component perpendicular to
 // the initial direction without losing it under the much larger drag term.
+template <bool SLOW>
 __device__ __forceinline__ int rhs_f32(const MixParams& Pm, const MixField& F, const float* tab_s, const Stage& B,
                                        float ox, float oy, float oz, float oe, float w0, const float u[4],
                                        float du[4], float L[3], float& hub) {
@@ -305,7 +363,8 @@ __device__ __forceinline__ int rhs_f32(const MixParams& Pm, const MixField& F, c
   float a, aa, r2;
   cosmo_f32(Pm, tab_s, ie, fe, a, aa, r2);
   float phi_si, gx, gy, gz;
-  const int st = interp_f32(F, B, ox, oy, oz, w0, phi_si, gx, gy, gz);
+  const int st = (SLOW && F.slow) ? interp_f32_slow(F, B, ox, oy, oz, w0, phi_si, gx, gy, gz)
+                                    : interp_f32(F, B, ox, oy, oz, w0, phi_si, gx, gy, gz);
   if (st) return st;
   const float ic2 = Pm.ic2;
   const float phi = phi_si * ic2;
@@ -376,11 +435,17 @@ __device__ __forceinline__ int64_t next_photon(const ExcTraceArgs& A, int64_t& s
 }
 
 // FP64 endpoint quantities a(eta) and Phi(x) with the parity code (once per photon).
+template <bool SLOW>
 __device__ __forceinline__ int endpoint(const MixParams& Pm, int fi, const double s[4], double& a, double& phi) {
   const ExcField& f = Pm.D.m.fields[fi];
   double adot, inv_a;
   int st = exc_mixed_f64::scale_factor(Pm.D, s[0], a, adot, inv_a);
   if (st) return st;
+  if (SLOW && f.grad_mode == EXC_GRAD_TRILINEAR) {
+    if (f.dtype == EXC_DTYPE_F32) return exc_mixed_f64::slow_value3<float>(f, s[1], s[2], s[3], phi);
+    if (f.dtype == EXC_DTYPE_F32X2) return exc_mixed_f64::slow_value3<float2>(f, s[1], s[2], s[3], phi);
+    return exc_mixed_f64::slow_value3<double>(f, s[1], s[2], s[3], phi);
+  }
   exc_mixed_f64::InterpOut ip;
   if (f.dtype == EXC_DTYPE_F32)
     st = exc_mixed_f64::interp_field<float, false>(f, Pm.D.finv[fi], s[1], s[2], s[3], s[0], ip);
@@ -497,6 +562,7 @@ __device__ __forceinline__ void perp_df(const df U[3], const df e[3], float out[
 }
 
 // One RK4 step (integrator.py:10-22) in mixed precision. Returns 0 or EXC_PH_*.
+template <bool SLOW>
 __device__ __forceinline__ int step_rk4_mixed(const MixParams& Pm, const float* tab_s, MPhoton& P, const bool obs) {
   const MixField& F = field_of(Pm, P.fi);
   Stage B;
@@ -506,18 +572,18 @@ __device__ __forceinline__ int step_rk4_mixed(const MixParams& Pm, const float* 
   const float ie = Pm.inv_eta_step.hi;
   const float u[4] = {P.U[0].hi, P.U[1].hi, P.U[2].hi, P.U[3].hi};
   float k1[4], k2[4], k3[4], k4[4], L1[3], L2[3], L3[3], L4[3], hb1, hb2, hb3, hb4, us2[4], us3[4], us4[4];
-  int st = rhs_f32(Pm, F, tab_s, B, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, u, k1, L1, hb1);
+  int st = rhs_f32<SLOW>(Pm, F, tab_s, B, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, u, k1, L1, hb1);
   if (st) return st;
   for (int i = 0; i < 4; ++i) us2[i] = fmaf(h, k1[i], u[i]);
-  st = rhs_f32(Pm, F, tab_s, B, h * u[1] * isx, h * u[2] * isy, h * u[3] * isz, h * u[0] * ie, kWin0, us2, k2, L2,
+  st = rhs_f32<SLOW>(Pm, F, tab_s, B, h * u[1] * isx, h * u[2] * isy, h * u[3] * isz, h * u[0] * ie, kWin0, us2, k2, L2,
                hb2);
   if (st) return st;
   for (int i = 0; i < 4; ++i) us3[i] = fmaf(h, k2[i], u[i]);
-  st = rhs_f32(Pm, F, tab_s, B, h * us2[1] * isx, h * us2[2] * isy, h * us2[3] * isz, h * us2[0] * ie, kWin0, us3,
+  st = rhs_f32<SLOW>(Pm, F, tab_s, B, h * us2[1] * isx, h * us2[2] * isy, h * us2[3] * isz, h * us2[0] * ie, kWin0, us3,
                k3, L3, hb3);
   if (st) return st;
   for (int i = 0; i < 4; ++i) us4[i] = fmaf(dt, k3[i], u[i]);
-  st = rhs_f32(Pm, F, tab_s, B, dt * us3[1] * isx, dt * us3[2] * isy, dt * us3[3] * isz, dt * us3[0] * ie, kWin0,
+  st = rhs_f32<SLOW>(Pm, F, tab_s, B, dt * us3[1] * isx, dt * us3[2] * isy, dt * us3[3] * isz, dt * us3[0] * ie, kWin0,
                us4, k4, L4, hb4);
   if (st) return st;
   float up[3];
@@ -584,6 +650,7 @@ __device__ __forceinline__ int step_rk4_mixed(const MixParams& Pm, const float* 
   return 0;
 }
 
+template <bool SLOW>
 __device__ __forceinline__ void photon_finish(const MixParams& Pm, const ExcTraceArgs& A, MPhoton& P) {
   const int64_t p = P.idx;
   if (P.status == EXC_PH_RETRACE) {   // everything else stays as it came in, for the FP64 tracer
@@ -600,7 +667,7 @@ __device__ __forceinline__ void photon_finish(const MixParams& Pm, const ExcTrac
   const bool failed = P.status >= EXC_PH_OUTSIDE_GRID;
   double a_em = NAN, phi_em = NAN;
   if (!failed) {
-    const int qst = endpoint(Pm, P.fi, x, a_em, phi_em);   // integrator.py:403 evaluates these unconditionally
+    const int qst = endpoint<SLOW>(Pm, P.fi, x, a_em, phi_em);   // integrator.py:403 evaluates these unconditionally
     if (qst) P.status = qst;
   }
   for (int d = 0; d < 4; ++d) s[d] = x[d];
@@ -613,7 +680,7 @@ __device__ __forceinline__ void photon_finish(const MixParams& Pm, const ExcTrac
     double* o = A.obs + p * EXC_OBSCOL_N;
     for (int i = 0; i < EXC_OBSCOL_N; ++i) o[i] = NAN;
     double a_obs = NAN, phi_obs = NAN;
-    if (endpoint(Pm, P.fi, s0, a_obs, phi_obs)) { a_obs = NAN; phi_obs = NAN; }
+    if (endpoint<SLOW>(Pm, P.fi, s0, a_obs, phi_obs)) { a_obs = NAN; phi_obs = NAN; }
     o[EXC_OBSCOL_ETA_OBS] = s0[0];
     o[EXC_OBSCOL_ETA_EM] = x[0];
     o[EXC_OBSCOL_A_OBS] = a_obs;
@@ -644,12 +711,13 @@ __device__ __forceinline__ bool df_ge(df a, float b) { return a.hi > b || (a.hi 
 __device__ __forceinline__ bool df_lt(df a, float b) { return a.hi < b || (a.hi == b && a.lo < 0.0f); }
 
 // One iteration of the integrate_single loop (integrator.py:347-400) + stops.
+template <bool SLOW>
 __device__ __forceinline__ bool photon_iterate(const MixParams& Pm, const float* tab_s, const ExcTraceArgs& A,
                                                MPhoton& P) {
   if (P.status >= 0) return true;    // set at begin (bad field index)
   if (P.it >= A.max_iter) { P.status = EXC_PH_MAX_ITER; return true; }
   if (P.steps >= A.max_steps) { P.status = EXC_PH_STEPS; return true; }
-  const int st = step_rk4_mixed(Pm, tab_s, P, A.obs_flags != 0);
+  const int st = step_rk4_mixed<SLOW>(Pm, tab_s, P, A.obs_flags != 0);
   if (st) { P.status = st; return true; }
   if (!isfinite(P.U[0].hi) || !isfinite(P.P[0].hi) || !isfinite(P.P[1].hi) || !isfinite(P.P[2].hi)) {
     P.status = EXC_PH_NONFINITE;
@@ -694,7 +762,9 @@ __device__ __forceinline__ bool photon_iterate(const MixParams& Pm, const float*
 
 // MINB = 1: registers as the compiler likes (144, three 128-thread blocks per SM);
 // MINB = 4: capped at 128 registers (a few spills to L1) for four blocks per SM.
-template <int MINB>
+// SLOW: the launch has a slow-Interpolator field (a separate instantiation, so
+// the base-node kernels keep their register allocation).
+template <int MINB, bool SLOW>
 __global__ void __launch_bounds__(128, MINB) trace_mixed_kernel(const MixParams Pm, const ExcTraceArgs A) {
   extern __shared__ float tab_s[];
   if (Pm.table_in_smem) {
@@ -709,13 +779,13 @@ __global__ void __launch_bounds__(128, MINB) trace_mixed_kernel(const MixParams 
   bool active = p < A.n_photons;
   if (active) photon_begin(Pm, A, P, p);
   while (active) {
-    bool done = photon_iterate(Pm, tab_s, A, P);
+    bool done = photon_iterate<SLOW>(Pm, tab_s, A, P);
     if (!done && (P.it & 63) == 0) {
       if (A.abort_flag && *(volatile const int32_t*)A.abort_flag) { P.status = EXC_PH_ABORTED; done = true; }
       else if (A.deadline_cycles > 0 && clock64() - t0 > A.deadline_cycles) { P.status = EXC_PH_TIMED_OUT; done = true; }
     }
     if (done) {
-      photon_finish(Pm, A, P);
+      photon_finish<SLOW>(Pm, A, P);
       if (P.status == EXC_PH_ABORTED || P.status == EXC_PH_TIMED_OUT) break;
       p = next_photon(A, static_next, stride);
       active = p < A.n_photons;
@@ -732,7 +802,7 @@ int check(const DevMetric& D, const ExcTraceArgs& A) {
   if (A.renormalize_every) return 4;
   for (int i = 0; i < D.m.n_fields; ++i) {
     if (D.m.fields[i].ndim != 3) return 5;
-    if (D.m.fields[i].grad_mode != EXC_GRAD_BASE_NODE) return 8;
+    if (D.m.fields[i].grad_mode != EXC_GRAD_BASE_NODE && D.m.fields[i].grad_mode != EXC_GRAD_TRILINEAR) return 8;
     const int64_t* n = D.m.fields[i].n;
     if (n[0] * n[1] * n[2] >= (int64_t)1 << 31) return 6;
   }
@@ -749,7 +819,7 @@ const char* why(int code) {
     case 5: return "mixed precision supports 3-D (static) potential grids only";
     case 6: return "mixed precision needs grids below 2^31 nodes";
     case 7: return "mixed precision has no ISW accumulator (static grids only)";
-    case 8: return "mixed precision supports the base-node gradient only";
+    case 8: return "mixed precision: unknown gradient mode";
     default: return "mixed precision: unsupported";
   }
 }
@@ -770,6 +840,7 @@ cudaError_t trace(const DevMetric& D, const ExcTraceArgs& A, int block, int bloc
     F.data = f.data;
     F.dtype = f.dtype;
     F.boundary = f.boundary;
+    F.slow = f.grad_mode == EXC_GRAD_TRILINEAR;
     F.nodes = (int)(f.n[0] * f.n[1] * f.n[2]);
     for (int d = 0; d < 3; ++d) {
       F.n[d] = (int)f.n[d];
@@ -801,7 +872,11 @@ cudaError_t trace(const DevMetric& D, const ExcTraceArgs& A, int block, int bloc
   P->a_stop_f = (float)A.a_stop;
   int per_sm = blocks_per_sm;
   // a plan with four or more resident blocks per SM takes the 128-register build
-  void (*kern)(const MixParams, const ExcTraceArgs) = per_sm >= 4 ? trace_mixed_kernel<4> : trace_mixed_kernel<1>;
+  bool slow = false;
+  for (int i = 0; i < m.n_fields; ++i) slow = slow || P->mf[i].slow;
+  void (*kern)(const MixParams, const ExcTraceArgs) =
+      slow ? (per_sm >= 4 ? trace_mixed_kernel<4, true> : trace_mixed_kernel<1, true>)
+           : (per_sm >= 4 ? trace_mixed_kernel<4, false> : trace_mixed_kernel<1, false>);
   cudaError_t e = cudaSuccess;
   if (per_sm <= 0) {
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, block, smem);

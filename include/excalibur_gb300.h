@@ -86,7 +86,9 @@ enum { EXC_BOUNDARY_PERIODIC = 0, EXC_BOUNDARY_CLAMP = 1, EXC_BOUNDARY_ERROR = 2
  *   no time bounds check), gradient on the snapshot nearest in time (round
  *   half to even, clipped), dPhi/deta from the snapshots either side of
  *   clip(floor(rel_t), 1, nt-2). Needs boundary EXC_BOUNDARY_ERROR and n >= 3
- *   per spatial axis. */
+ *   per spatial axis. The mixed-precision tracer takes it on 3-D grids; its value
+ *   and gradient are continuous across interior cell faces, so only stage points
+ *   near the outer cells are handed back to the FP64 re-trace. */
 enum { EXC_GRAD_BASE_NODE = 0, EXC_GRAD_TRILINEAR = 1 };
 /* EXC_DTYPE_F32X2: a float64 grid stored as interleaved float32 pairs, node i
  * at data[2i] = hi = (float)x_i and data[2i + 1] = lo = (float)(x_i - hi);

@@ -159,3 +159,23 @@ def test_pipelined_batches_match_single_launches(patch):
     assert np.array_equal(got, whole["state"])
     assert np.array_equal(np.concatenate([r.status.cpu().numpy() for r in res]), whole["status"])
     assert np.array_equal(np.concatenate([r.obs.cpu().numpy() for r in res]), whole["obs"], equal_nan=True)
+
+
+@pytest.mark.parametrize("n_grid,side", [(128, 24), (32, 16)])
+def test_mixed_slow_interpolator_matches_fp64_oracle(cuda, n_grid, side):
+    """The slow Interpolator's continuous gradient (grad_mode "trilinear"): the same error bounds,
+    and no ray needs the FP64 re-trace (a discontinuity of the RHS is what makes one necessary;
+    here the formula changes only at the grid's outer cells, which the rays do not reach)."""
+    from excalibur_tool_gb300.core.constants import one_Mpc
+
+    spec, st, cfg = _cfg2_like(n_grid, side)
+    spec.fields[0].boundary = "error"
+    spec.fields[0].gradient = "trilinear"
+    hi = 990 * one_Mpc if n_grid == 128 else 960 * one_Mpc     # inside the bounds [0, (n-1) spacing)
+    cfg = dataclasses.replace(cfg, precision="mixed_raw", stop_box=((0, 0, 0), (hi, hi, hi)))
+    raw = gpu_trace(spec, st, cfg)
+    assert (raw["status"] != N.PH_RETRACE).all()
+    r = gpu_trace(spec, st, dataclasses.replace(cfg, precision="mixed"))
+    o = O.trace(spec, st, dataclasses.replace(cfg, precision="fp64"), threads=8)
+    assert (o.status == N.PH_LEFT_BOX).all()
+    _check_observables(r, o)

@@ -148,17 +148,3 @@ def test_gpu_slow_trace_matches_reference(precision):
         assert rel_err(r["state"], g["trace_final"]).max() <= 1e-13
         assert rel_err(got, want).max() <= 1e-13
     torch.cuda.synchronize()
-
-
-@pytest.mark.gpu
-def test_gpu_slow_rejected_by_mixed():
-    import torch
-    from excalibur_tool_gb300 import _native as N
-    from helpers import gpu_trace
-
-    g = golden("interp_slow.npz")
-    st, cfg = _trace_spec(g)
-    cfg = dataclasses.replace(cfg, precision="mixed", record_every=None)
-    with pytest.raises(N.NativeError, match="base-node gradient"):
-        gpu_trace(st, g["trace_init"], cfg)
-    torch.cuda.synchronize()
