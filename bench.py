@@ -64,6 +64,7 @@ def parse():
     p.add_argument("--no-surrogate", action="store_true", help="skip the learned sky-map leg")
     p.add_argument("--no-batching", action="store_true", help="skip the multi-field RK45 batching leg")
     p.add_argument("--batching-scale", type=int, default=4, help="run 1/scale of the batching configuration")
+    p.add_argument("--no-sweep", action="store_true", help="skip the comparison-sweep leg")
     p.add_argument("--profile-gemm", type=int, default=0, metavar="M",
                    help="only time the surrogate's tensor-core GEMM on M rows (for profiling) and exit")
     p.add_argument("--map-side", type=int, default=4096)
@@ -316,6 +317,9 @@ def run_ours(args, rank, world, local):
     if not args.no_batching and world == 1:
         torch.cuda.empty_cache()
         line["batching"] = run_batching(args, dev, stream)
+    if not args.no_sweep and world == 1:
+        torch.cuda.empty_cache()
+        line["sweep"] = run_sweep_leg(args, dev)
     if not args.no_surrogate and world == 1:
         torch.cuda.empty_cache()
         line["surrogate"] = run_surrogate(args, dev, stream, peaks, rays_s)
@@ -553,6 +557,73 @@ def run_batching(args, dev, stream):
             "rejected_fraction": float(1 - steps.sum() / max(1, iters.sum())),
             "status_counts": np.bincount(status, minlength=12).tolist(),
             "gpu_launches_per_replay": 1}
+
+
+SWEEP_MANIFEST = dict(masses="1e13,3e13,1e14,3e14", distances="200,300,400,500", Ns="64,128", sampling="cone",
+                      cone_nphotons=200, cone_angle_deg=10.0, integrators="rk4")
+
+
+def run_sweep_leg(args, dev):
+    """A 32-row comparison sweep (4 masses x 4 distances x 2 grid sizes, 183-photon cones, RK4,
+    records every 4 steps, static cosmology, local coordinates): every row's Schwarzschild and
+    FLRW legs and its per-run statistics, from the manifest to the tables. Timed end to end on
+    the host clock (potentials built on the device, photon generation, launches, record copies,
+    statistics), grouped launches against one launch per row; the oracle runs one row's two
+    legs on the host threads for the CPU rate."""
+    import tempfile
+
+    import torch
+
+    from excalibur_tool_gb300.runners import compare as R
+    from excalibur_tool_gb300.runners import sweep as S
+
+    with tempfile.TemporaryDirectory() as tmp:
+        path = os.path.join(tmp, "manifest.csv")
+        S.make_manifest(path, **SWEEP_MANIFEST)
+        jobs = S.read_jobs(path)
+    S.run_jobs(jobs[:2])                        # warm-up: library load, first launches
+    torch.cuda.synchronize(dev)
+    out = {}
+    for name, mf in (("grouped", 32), ("row_by_row", 1)):
+        t0 = time.perf_counter()
+        res = S.run_jobs(jobs, max_fields=mf)
+        torch.cuda.synchronize(dev)
+        out[name] = time.perf_counter() - t0
+    steps = sum(int(r.schwarzschild.n_steps.sum()) + int(r.flrw.n_steps.sum()) for r in res.values())
+    photons = sum(r.flrw.trajectories.shape[0] for r in res.values())
+    leg = {"workload": f"{len(jobs)} manifest rows ({SWEEP_MANIFEST['masses']} Msun x {SWEEP_MANIFEST['distances']} "
+                       f"Mpc x N {SWEEP_MANIFEST['Ns']}), cone of 200 requested photons (183 traced) per leg, "
+                       "RK4, record_every 4, static cosmology, observer-local FLRW coordinates",
+           "rows": len(jobs), "photons_per_leg": photons, "photon_steps": steps,
+           "grouped_s": out["grouped"], "row_by_row_s": out["row_by_row"],
+           "rows_per_s": len(jobs) / out["grouped"], "photon_steps_per_s": steps / out["grouped"],
+           "grouping_speedup": out["row_by_row"] / out["grouped"]}
+    # the oracle on one row (the largest: 500 Mpc, N = 128), both legs, host threads
+    from oracle import oracle as O
+    from oracle.oracle import FieldSpec, Spacetime
+    from excalibur_tool_gb300.trace import TraceConfig
+
+    job = max(jobs, key=lambda j: (j.distance_mpc, j.flrw_grid_N))
+    cfg = S.job_config(job)
+    geo = R.geometry(cfg)
+    _, ss, _, _ = R.schwarzschild_setup(cfg, geo)
+    _, fs, shift = R.flrw_setup(cfg, geo)
+    d = cfg.flrw_grid_size / cfg.flrw_grid_N
+    phi = R.flrw_potential(cfg, geo)
+    tc = TraceConfig(stepper="rk4", dt=geo.dlambda, dt_min=abs(geo.dlambda), dt_max=abs(geo.dlambda),
+                     max_steps=geo.n_steps, record_every=cfg.record_every, observables=False)
+    th = host_threads()
+    t0 = time.perf_counter()
+    O.trace(Spacetime(kind="schwarzschild", mass=cfg.mass, radius=cfg.radius, center=tuple(geo.lens_center),
+                      analytical=True), ss.cpu().numpy(), tc, threads=th)
+    O.trace(Spacetime(kind="flrw", cosmology="static",
+                      fields=[FieldSpec(phi, (d, d, d), (0.0, 0.0, 0.0), "periodic", shift=tuple(shift))]),
+            fs.cpu().numpy(), tc, threads=th)
+    cpu_s = time.perf_counter() - t0
+    leg["cpu_oracle_one_row"] = {"seconds": cpu_s, "threads": th, "row": job.jobid,
+                                 "photon_steps": 2 * int(ss.shape[0]) * geo.n_steps,
+                                 "note": "C restatement of the two legs (no host setup, no statistics)"}
+    return leg
 
 
 def gemm_tflops(dev, stream, m=1 << 20, members=4):

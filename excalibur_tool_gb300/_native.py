@@ -13,7 +13,7 @@ import threading
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libexcalibur_gb300.so")
 
-EXC_ABI_VERSION = 1
+EXC_ABI_VERSION = 2
 EXC_MAX_FIELDS = 32
 
 # return codes
@@ -47,7 +47,7 @@ OBS_N = 20
 class ExcField(C.Structure):
     _fields_ = [("data", C.c_void_p), ("dtype", C.c_int32), ("ndim", C.c_int32),
                 ("boundary", C.c_int32), ("grad_mode", C.c_int32), ("n", C.c_int64 * 4),
-                ("origin", C.c_double * 4), ("spacing", C.c_double * 4)]
+                ("origin", C.c_double * 4), ("spacing", C.c_double * 4), ("shift", C.c_double * 3)]
 
 
 class ExcMetric(C.Structure):
@@ -133,6 +133,9 @@ EXPORTS = {
                                  C.c_int64, C.c_void_p]),
     "exc_trace_noalloc": (C.c_int, [C.POINTER(ExcMetric), C.POINTER(ExcTraceArgs), C.c_void_p]),
     "exc_gen_count": (C.c_int64, [C.POINTER(ExcPhotonGen)]),
+    "exc_spherical_mass_grid": (C.c_int, [C.POINTER(C.c_int64), C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                          C.POINTER(C.c_double), C.c_double, C.c_double, C.c_double, C.c_double,
+                                          C.c_void_p, C.c_void_p]),
     "exc_generate_photons": (C.c_int, [C.POINTER(ExcMetric), C.POINTER(ExcPhotonGen), C.c_void_p, C.c_void_p,
                                        C.c_void_p]),
     "exc_autotune": (C.c_int, [C.POINTER(ExcMetric), C.POINTER(ExcTraceArgs), C.c_void_p,

@@ -166,7 +166,7 @@ extern "C" int exc_born_patch(const ExcMetric* metric, const ExcBornArgs* a, voi
     F.n[d] = (int)f.n[d];
     F.s[d] = (float)f.spacing[d];
     F.inv_s[d] = (float)(1.0 / f.spacing[d]);
-    F.o[d] = (float)f.origin[d];
+    F.o[d] = (float)(f.origin[d] - f.shift[d]);   // a shifted grid is queried at x + shift
   }
   const int64_t blocks = (a->n + 127) / 128;
   born_kernel<<<(unsigned)blocks, 128, 0, (cudaStream_t)stream>>>(F, *a);

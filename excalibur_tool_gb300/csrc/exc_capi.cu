@@ -57,6 +57,8 @@ int check_field(const ExcField& f, int idx) {
       return fail(EXC_ERR_INVALID, "field %d: spacing[%d] must be finite and > 0", idx, d);
     if (!std::isfinite(f.origin[d])) return fail(EXC_ERR_INVALID, "field %d: origin[%d] not finite", idx, d);
   }
+  for (int d = 0; d < 3; ++d)
+    if (!std::isfinite(f.shift[d])) return fail(EXC_ERR_INVALID, "field %d: shift[%d] not finite", idx, d);
   if (f.grad_mode != EXC_GRAD_BASE_NODE && f.grad_mode != EXC_GRAD_TRILINEAR)
     return fail(EXC_ERR_INVALID, "field %d: unknown grad_mode %d", idx, f.grad_mode);
   if (f.grad_mode == EXC_GRAD_TRILINEAR) {

@@ -275,6 +275,9 @@ __device__ __forceinline__ void slow_gradient(const ExcField& f, const double* f
 template <class FT>
 __device__ __forceinline__ int slow_value3(const ExcField& f, double x, double y, double z, double& val) {
   const FT* d = (const FT*)f.data;
+  x += f.shift[0];
+  y += f.shift[1];
+  z += f.shift[2];
   const int64_t nx = f.n[0], ny = f.n[1], nz = f.n[2];
   const double rx = (x - f.origin[0]) / f.spacing[0];
   const double ry = (y - f.origin[1]) / f.spacing[1];
@@ -376,6 +379,10 @@ template <class FT, bool SLOW = true>
 __device__ __forceinline__ int interp_field(const ExcField& f, const double* fi, double x, double y, double z,
                                             double t, InterpOut& o) {
   const FT* d = (const FT*)f.data;
+  // a shifted interpolator queries x + shift (ExcField.shift; zero = none)
+  x += f.shift[0];
+  y += f.shift[1];
+  z += f.shift[2];
   if constexpr (SLOW) {
     if (f.grad_mode == EXC_GRAD_TRILINEAR) return interp_slow<FT>(f, fi, d, x, y, z, t, o);
   }

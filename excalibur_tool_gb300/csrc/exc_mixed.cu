@@ -468,9 +468,12 @@ __device__ __forceinline__ void photon_begin(const MixParams& Pm, const ExcTrace
   const double* s = A.state + p * 8;
   double btol = 0.0;
   for (int d = 0; d < 3; ++d) {
-    P.P[d] = df_of((s[1 + d] - f.origin[d]) / f.spacing[d]);   // the reference's cell coordinate
-    P.lc[d] = (float)((A.lens_center[d] - f.origin[d]) / f.spacing[d]);
-    const double blo = (A.box_lo[d] - f.origin[d]) / f.spacing[d], bhi = (A.box_hi[d] - f.origin[d]) / f.spacing[d];
+    // the reference's cell coordinate of the (shifted) query point; the lens and box are
+    // given in the state's coordinates and take the same shift
+    const double o = f.origin[d], sh = f.shift[d];
+    P.P[d] = df_of(((s[1 + d] + sh) - o) / f.spacing[d]);
+    P.lc[d] = (float)(((A.lens_center[d] + sh) - o) / f.spacing[d]);
+    const double blo = ((A.box_lo[d] + sh) - o) / f.spacing[d], bhi = ((A.box_hi[d] + sh) - o) / f.spacing[d];
     P.box[d] = (float)blo;
     P.box[3 + d] = (float)bhi;
     btol = fmax(btol, fmax(fabs((double)P.box[d] - blo), fabs((double)P.box[3 + d] - bhi)));
@@ -663,7 +666,7 @@ __device__ __forceinline__ void photon_finish(const MixParams& Pm, const ExcTrac
   for (int i = 0; i < 8; ++i) s0[i] = s[i];         // the photon's initial state (not yet overwritten)
   double x[4];
   x[0] = dbl(P.eta);
-  for (int d = 0; d < 3; ++d) x[1 + d] = f.origin[d] + dbl(P.P[d]) * f.spacing[d];
+  for (int d = 0; d < 3; ++d) x[1 + d] = (f.origin[d] + dbl(P.P[d]) * f.spacing[d]) - f.shift[d];
   const bool failed = P.status >= EXC_PH_OUTSIDE_GRID;
   double a_em = NAN, phi_em = NAN;
   if (!failed) {

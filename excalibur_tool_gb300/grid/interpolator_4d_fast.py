@@ -17,6 +17,7 @@ from .. import _native as N
 
 class InterpolatorFast:
     gradient_mode = "base_node"   # central difference at the cell's base node
+    shift = None                  # query offset (shifted_interpolator); None = query x itself
 
     def __init__(self, grid, boundary: str = "periodic", field_dtype=None):
         if boundary not in ("error", "clamp", "periodic"):
@@ -46,10 +47,10 @@ class InterpolatorFast:
         if split and str(t.dtype) == "torch.float64":
             planes = self.grid.device_field_split(field, device)
             f = field_struct(planes, self.shape[:nd], self.spacing[:nd], self.origin[:nd], self.boundary,
-                             split=True, gradient=self.gradient_mode)
+                             split=True, gradient=self.gradient_mode, shift=self.shift)
             return f, planes
         return field_struct(t, self.shape[:nd], self.spacing[:nd], self.origin[:nd], self.boundary,
-                            gradient=self.gradient_mode), t
+                            gradient=self.gradient_mode, shift=self.shift), t
 
     # ---- batched evaluation ----------------------------------------------
     def evaluate(self, points, field="Phi", device="cuda"):
@@ -96,3 +97,21 @@ class InterpolatorFast:
             raise ValueError("4D grid: you must pass t to value_and_gradient")
         v, g, _ = self.value_gradient_and_time_derivative(x, field, t if self.is_4d else 0.0)
         return v, g
+
+
+def shifted_interpolator(base, shift):
+    """`base` queried at x + shift: the comparison runners' _ShiftedInterpolator
+    (_excalibur_runs/excalibur_run_compare_schwarzschild_vs_flrw.py:39-56), which lets them
+    integrate in observer-local coordinates against a grid laid out in absolute ones.
+
+    Returns a copy of `base` sharing its grid (and the grid's device copy); the offset
+    travels in ExcField.shift, so the tracer and `evaluate` both add it on the device with
+    one float64 addition per component, as the reference's wrapper does on the host."""
+    import copy
+
+    ip = copy.copy(base)
+    sh = np.asarray(shift, dtype=np.float64).reshape(-1)
+    if sh.shape[0] != 3 or not np.all(np.isfinite(sh)):
+        raise ValueError("shift must be three finite numbers")
+    ip.shift = sh.copy()
+    return ip

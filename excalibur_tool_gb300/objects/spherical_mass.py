@@ -35,6 +35,30 @@ class spherical_mass:
         pot[~inside] = -self.G * self.mass / r[~inside]
         return pot
 
+    def potential_grid(self, shape, spacing, origin=(0.0, 0.0, 0.0), device="cuda"):
+        """`potential` on the nodes origin + i * spacing of a C-order grid, built on the GPU
+        (exc_spherical_mass_grid): the same values, bit for bit, as
+        potential(*np.meshgrid(*[np.linspace(o, o + n * s, n, endpoint=False)], indexing="ij"))
+        whenever s is the linspace step (stop - start) / n. Returns a float64 tensor."""
+        import ctypes as C
+
+        import torch
+
+        from .. import _native as N
+
+        n = (C.c_int64 * 3)(*[int(v) for v in shape])
+        dbl3 = lambda v: (C.c_double * 3)(*[float(x) for x in v])
+        out = torch.empty(tuple(int(v) for v in shape), dtype=torch.float64, device=device)
+        # the reference's scalar subexpressions, in its own (Python float) arithmetic
+        neg_gm = -self.G * self.mass
+        three_r2 = 3 * self.radius ** 2
+        two_r3 = 2 * self.radius ** 3
+        N.check(N.load().exc_spherical_mass_grid(n, dbl3(origin), dbl3(spacing),
+                                                 dbl3((self.x0, self.y0, self.z0)), float(self.radius),
+                                                 float(neg_gm), float(three_r2), float(two_r3), N.ptr(out),
+                                                 N.stream_handle(device)), "exc_spherical_mass_grid")
+        return out
+
 
 class spherical_mass_nfw:
     def __init__(self, mass, radius, concentration, center=np.array([0.5, 0.5, 0.5])):

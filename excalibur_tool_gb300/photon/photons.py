@@ -39,15 +39,28 @@ def rotate_to_direction(vectors, target_direction):
 
 
 class Photons:
-    def __init__(self, metric):
+    def __init__(self, metric, *, defer_checks: bool = False):
+        """`defer_checks=True` keeps generated states on the device and postpones the check of
+        the null-condition solve (the ValueError the generators raise for an origin where the
+        metric cannot be evaluated) to `check_generated()` or the first host access, so that a
+        generator call does not wait for the GPU."""
         self.metric = metric
         self._batch = []          # list of [n, 8] arrays (host) or tensors (device)
         self._photons = None
         self.field_index = None
+        self.defer_checks = bool(defer_checks)
+        self._pending = []        # device status tensors of deferred null-condition solves
+
+    def check_generated(self):
+        pending, self._pending = self._pending, []
+        for status in pending:
+            if int((status != 0).sum()) != 0:
+                raise ValueError("metric evaluation failed at a photon origin (outside the grid?)")
 
     # ---- storage ---------------------------------------------------------
     @property
     def photons(self):
+        self.check_generated()
         if self._photons is None:
             st = self.states_numpy()
             self._photons = [Photon(s[:4].copy(), s[4:].copy()) for s in st]
@@ -56,6 +69,7 @@ class Photons:
     def states_numpy(self):
         import torch
 
+        self.check_generated()
         if self._photons is not None:
             return np.array([np.concatenate([p.x, p.u]) for p in self._photons]).reshape(-1, 8)
         if not self._batch:
@@ -110,6 +124,10 @@ class Photons:
         st[:, 5:8] = u_spatial
         t = torch.as_tensor(st, dtype=torch.float64, device="cuda")
         status = null_init(self.metric, t, sign)
+        if self.defer_checks:
+            self._pending.append(status)
+            self._append_batch(t)
+            return t
         if int((status != 0).sum()) != 0:
             raise ValueError("metric evaluation failed at a photon origin (outside the grid?)")
         self._append_batch(t.cpu().numpy())

@@ -105,7 +105,7 @@ def base_metric_struct(kind: int) -> N.ExcMetric:
 
 
 def field_struct(data, shape, spacing, origin, boundary: str, split: bool = False,
-                 gradient: str = "base_node") -> N.ExcField:
+                 gradient: str = "base_node", shift=None) -> N.ExcField:
     import torch
 
     f = N.ExcField()
@@ -133,6 +133,9 @@ def field_struct(data, shape, spacing, origin, boundary: str, split: bool = Fals
         f.n[d] = int(shape[d])
         f.spacing[d] = float(spacing[d])
         f.origin[d] = float(origin[d])
+    if shift is not None:
+        for d in range(3):
+            f.shift[d] = float(shift[d])
     return f
 
 
@@ -152,11 +155,14 @@ def _check_device_tensor(t, dtype, shape_tail, name):
 
 
 def trace_batch(metric, states, cfg: TraceConfig, *, field_index=None, dt=None, out=None,
-                queue=None, abort_flag=None, stream=None) -> TraceResult:
+                queue=None, abort_flag=None, stream=None, check_field_index=True) -> TraceResult:
     """Trace every photon of `states` ([N, 8] float64 on a CUDA device) in one launch.
 
     `metric` is any of the package's metric classes (it provides `descriptor(device)`).
     `states` is not modified; the result holds fresh tensors (or `out`'s).
+    `check_field_index=False` skips the range check of `field_index` (a device reduction and
+    a host synchronisation) for callers that built it in range; the kernel still gives an
+    out-of-range photon the status EXC_PH_BAD_FIELD.
     """
     import torch
 
@@ -188,7 +194,7 @@ def trace_batch(metric, states, cfg: TraceConfig, *, field_index=None, dt=None, 
         if field_index.dtype != torch.int32 or field_index.device != dev or field_index.shape != (n,):
             raise ValueError("field_index must be an int32 [N] tensor on the states' device")
         nf = desc.struct.n_fields
-        if n and (int(field_index.min()) < 0 or int(field_index.max()) >= nf):
+        if check_field_index and n and (int(field_index.min()) < 0 or int(field_index.max()) >= nf):
             raise ValueError(f"field_index values must lie in [0, {nf})")
     res = TraceResult(st, status, nsteps, niter, dts, obs, records, nrec)
     res.field_index = field_index

@@ -39,7 +39,7 @@
 extern "C" {
 #endif
 
-#define EXC_ABI_VERSION 1
+#define EXC_ABI_VERSION 2
 #define EXC_MAX_FIELDS 32
 
 /* ---- return codes of every entry point ---------------------------------- */
@@ -147,6 +147,12 @@ typedef struct ExcField {
   int64_t n[4];
   double origin[4];
   double spacing[4];
+  /* Query offset added to a position before every lookup in this grid: the
+   * comparison runners integrate in observer-local coordinates and wrap their
+   * interpolator so that it queries x + shift (_ShiftedInterpolator,
+   * _excalibur_runs/excalibur_run_compare_schwarzschild_vs_flrw.py:39-56).
+   * All zero = no shift (x + 0.0 leaves every position unchanged). */
+  double shift[3];
 } ExcField;
 
 /* Spacetime: metric parameters, cosmology table and potential grids. */
@@ -308,6 +314,18 @@ int64_t exc_gen_count(const ExcPhotonGen* gen);
 /* states: [exc_gen_count(gen)][8] float64, device. */
 int exc_generate_photons(const ExcMetric* metric, const ExcPhotonGen* gen, double* states, int32_t* status,
                          void* stream);
+
+/* ---- lens potential on a grid: replaces the host-side field construction of
+ * spherical_mass(M, R, center).potential(X, Y, Z) (objects/spherical_mass.py:29-49)
+ * on the meshgrid of numpy.linspace(origin, origin + n * spacing, n, endpoint=False)
+ * that the comparison runners build before every run
+ * (_excalibur_runs/excalibur_run_compare_schwarzschild_vs_flrw.py:474-479).
+ * out: [n0][n1][n2] float64, device. neg_gm, three_r2, two_r3 are the reference's
+ * scalar subexpressions -G*M, 3*R**2 and 2*R**3, evaluated by the caller with the
+ * reference's own (Python) arithmetic; the grid is then bit-identical to numpy's. */
+int exc_spherical_mass_grid(const int64_t n[3], const double origin[3], const double spacing[3],
+                            const double center[3], double radius, double neg_gm, double three_r2,
+                            double two_r3, double* out, void* stream);
 
 /* ---- launch-schedule autotuner (no reference counterpart: the reference has no
  * GPU schedule). Runs exc_trace on a sample batch for each candidate (block size

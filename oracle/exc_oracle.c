@@ -260,6 +260,11 @@ static int slow_interp(const ExcField* f, double x, double y, double z, double t
 int oracle_interp_one(const ExcField* f, double x, double y, double z, double t, double out[5]) {
   Interp o;
   int st;
+  /* _ShiftedInterpolator (excalibur_run_compare_schwarzschild_vs_flrw.py:50-52):
+   * the query point is x + shift, one float64 addition per component */
+  x = x + f->shift[0];
+  y = y + f->shift[1];
+  z = z + f->shift[2];
   if (f->grad_mode == EXC_GRAD_TRILINEAR) {
     st = slow_interp(f, x, y, z, t, &o);
   } else if (f->ndim != 4) {

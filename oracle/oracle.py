@@ -51,6 +51,7 @@ class FieldSpec:
     origin: tuple
     boundary: str = "periodic"
     gradient: str = "base_node"         # "base_node" | "trilinear" (the slow Interpolator)
+    shift: tuple = (0.0, 0.0, 0.0)      # query offset of a shifted interpolator (runner local coords)
 
 
 @dataclasses.dataclass
@@ -93,13 +94,15 @@ class Spacetime:
         for i, f in enumerate(self.fields):
             arr = np.ascontiguousarray(f.data)
             self._fields.append(arr)
-            m.fields[i] = field_struct(arr, f.spacing, f.origin, f.boundary, f.gradient)
+            m.fields[i] = field_struct(arr, f.spacing, f.origin, f.boundary, f.gradient, f.shift)
         m.n_fields = len(self.fields)
         return m
 
 
-def field_struct(arr, spacing, origin, boundary, gradient="base_node"):
+def field_struct(arr, spacing, origin, boundary, gradient="base_node", shift=(0.0, 0.0, 0.0)):
     fs = N.ExcField()
+    for d in range(3):
+        fs.shift[d] = float(shift[d])
     fs.data = arr.ctypes.data
     fs.dtype = N.DTYPE_F32 if arr.dtype == np.float32 else N.DTYPE_F64
     fs.ndim = arr.ndim
@@ -114,7 +117,7 @@ def field_struct(arr, spacing, origin, boundary, gradient="base_node"):
 
 def interp(field: FieldSpec, pts4):
     arr = np.ascontiguousarray(field.data)
-    fs = field_struct(arr, field.spacing, field.origin, field.boundary, field.gradient)
+    fs = field_struct(arr, field.spacing, field.origin, field.boundary, field.gradient, field.shift)
     pts = np.ascontiguousarray(pts4, dtype=np.float64)
     n = pts.shape[0]
     out = np.empty((n, 5))

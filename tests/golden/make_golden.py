@@ -527,17 +527,117 @@ def gen_observables(cz):
          stats_sph=stats(sphs), path=path, delay=delay, theory=theory)
 
 
+# --------------------------------------------- comparison runner (one sweep job)
+# The job behind the reference's committed per-run table results_test/per_run/job_00001.csv,
+# whose command line is in results_test/logs/job_00001_runner.log.
+COMPARE_JOB_ARGV = ["--mass-msun", "20000000000000.0", "--distance-mpc", "500.0", "--flrw-grid-N", "128",
+                    "--progress-every", "0", "--record-every", "4", "--sampling", "cone", "--n-photons", "400",
+                    "--cone-angle-deg", "10.0", "--static", "--flrw-local-coords"]
+COMPARE_KEEP = [1, 40, 97, 190, 300, 380]     # photons whose whole trajectories are kept
+
+
+def gen_compare_job():
+    """Run the reference's comparison runner (excalibur_run_compare_schwarzschild_vs_flrw.py) on
+    job 1's command line, capture each photon's initial state as the runner hands it to
+    integrate_single, and reduce both trajectory files with the reference's analyzer
+    (analyze_compare_trajectories._trajectory_stats). Also keeps the reference's committed CSV
+    of the same job (produced on the author's machine with numba's fastmath) for comparison."""
+    import contextlib
+    import hashlib
+    import io
+    import tempfile
+
+    pp = _load_postprocessing()
+    runner = _load_file("compare_runner", "_excalibur_runs", "excalibur_run_compare_schwarzschild_vs_flrw.py")
+    inits, phis = {}, []
+    orig_integrate_all, orig_add = runner._integrate_all, runner.Grid.add_field
+
+    def capture(photons, integrator, n_steps, **kw):
+        inits[kw["label"]] = np.array([np.concatenate([p.x, p.u]) for p in photons.photons])
+        return orig_integrate_all(photons, integrator, n_steps, **kw)
+
+    def add_field(self, name, data):
+        phis.append(np.asarray(data))
+        return orig_add(self, name, data)
+
+    runner._integrate_all = capture
+    runner.Grid.add_field = add_field
+    with tempfile.TemporaryDirectory() as tmp:
+        old = sys.argv
+        sys.argv = ["runner", *COMPARE_JOB_ARGV, "--output-dir", tmp]
+        out = io.StringIO()
+        try:
+            with contextlib.redirect_stdout(out):
+                runner.main()
+        finally:
+            sys.argv = old
+            runner._integrate_all, runner.Grid.add_field = orig_integrate_all, orig_add
+        text = out.getvalue()
+        s_h5 = text.split("Schwarzschild ->")[1].splitlines()[0].strip()
+        f_h5 = text.split("FLRW          ->")[1].splitlines()[0].strip()
+        s_tr, _ = pp._load_trajectories(s_h5.replace(".h5", ".npz"))
+        f_tr, _ = pp._load_trajectories(f_h5.replace(".h5", ".npz"))
+    lens = np.asarray(pp.parse_trajectory_filename(s_h5)["mass_position_m"], dtype=float)
+
+    def stats(tr, sph):
+        rows = []
+        for i in range(tr.shape[0]):
+            st = pp._trajectory_stats(tr[i], lens, is_spherical=sph)
+            rows.append([st.n_records, st.finite_fraction, st.path_length, st.min_r, st.final_r,
+                         st.bending_angle_rad, st.speed_mean, st.speed_max])
+        return np.array(rows)
+
+    csv_ref = np.loadtxt(os.path.join(REF, "results_test", "per_run", "job_00001.csv"), delimiter=",", skiprows=1)
+    phi = phis[0]
+    save("compare_job1.npz", argv=np.array(COMPARE_JOB_ARGV), lens_center=lens,
+         schw_init=inits["Schwarzschild"], flrw_init=inits["FLRW"],
+         schw_stats=stats(s_tr, True), flrw_stats=stats(f_tr, False),
+         keep=np.array(COMPARE_KEEP), schw_traj=s_tr[COMPARE_KEEP], flrw_traj=f_tr[COMPARE_KEEP],
+         n_records=np.array(s_tr.shape[1]), phi_sha256=np.array(hashlib.sha256(phi.tobytes()).hexdigest()),
+         phi_shape=np.array(phi.shape), csv_author=csv_ref)
+
+
+def gen_manifest():
+    """The reference's manifest writer (make_manifest.py) on a small sweep, both sampling modes."""
+    import subprocess
+    import tempfile
+
+    script = os.path.join(REF, "_simulations", "_schwarzschild_vs_flrw", "make_manifest.py")
+    runs = {
+        "manifest_cone.csv": ["--masses", "1e13,2e13", "--distances", "300,500", "--Ns", "64,128",
+                              "--sampling", "cone", "--cone-nphotons", "100", "--cone-angle-deg", "5",
+                              "--integrators", "rk4,leapfrog4", "--seed0", "7"],
+        "manifest_impact.csv": ["--masses", "1e14", "--distances", "200,400", "--Ns", "96",
+                                "--b-min", "0.5", "--b-max", "2.5", "--b-nbins", "4", "--b-nperbin", "30",
+                                "--radii-mpc", "2,3", "--static", "0", "--record-every", "8"],
+    }
+    for name, argv in runs.items():
+        with tempfile.TemporaryDirectory() as tmp:
+            out = os.path.join(tmp, name)
+            subprocess.run([sys.executable, script, "--out", out, *argv], check=True, capture_output=True)
+            with open(out) as f, open(os.path.join(HERE, name), "w") as g:
+                g.write(f.read())
+        print(f"wrote {name}")
+    with open(os.path.join(HERE, "manifest_args.txt"), "w") as g:
+        for name, argv in runs.items():
+            g.write(name + " " + " ".join(argv) + "\n")
+
+
+GENERATORS = ["cosmology", "interp", "interp_slow", "rhs", "steps", "integrate", "generators", "observables",
+              "cfg2_small", "cfg1", "compare_job", "manifest"]
+
 if __name__ == "__main__":
     if not os.path.isdir(REF):
         sys.exit(f"reference checkout not found at {REF}")
     np.seterr(all="ignore")
-    cz = gen_cosmology()
-    gen_interp()
-    gen_interp_slow(cz)
-    gen_rhs(cz)
-    gen_steps(cz)
-    gen_integrate(cz)
-    gen_generators(cz)
-    gen_observables(cz)
-    gen_cfg2_small(cz)
-    gen_cfg1()
+    which = sys.argv[1:] or GENERATORS
+    cz = gen_cosmology() if "cosmology" in which else None
+    if cz is None and set(which) & {"interp_slow", "rhs", "steps", "integrate", "generators", "observables",
+                                    "cfg2_small"}:
+        cz = LCDM_Cosmology(70, 0.3, 0.0, 0.7)
+    for name in which:
+        if name == "cosmology":
+            continue
+        fn = globals()["gen_" + name]
+        fn(cz) if name in ("interp_slow", "rhs", "steps", "integrate", "generators", "observables",
+                           "cfg2_small") else fn()
