@@ -69,7 +69,7 @@ def parse():
                    help="only time the surrogate's tensor-core GEMM on M rows (for profiling) and exit")
     p.add_argument("--map-side", type=int, default=4096)
     p.add_argument("--train-steps", type=int, default=8000)
-    p.add_argument("--smooth-train-steps", type=int, default=24000,
+    p.add_argument("--smooth-train-steps", type=int, default=16000,
                    help="training steps of the surrogate on the slow-Interpolator field")
     return p.parse_args()
 
@@ -652,7 +652,7 @@ def gemm_tflops(dev, stream, m=1 << 20, members=4):
     return flops / sec / 1e12, sec, flops
 
 
-def _surrogate_map(args, metric, patch, cfg, fp64_rays_s, train_steps):
+def _surrogate_map(args, metric, patch, cfg, fp64_rays_s, train_steps, lr=2e-3):
     """Train the BF16 ensemble on 1,048,576 rays traced with `cfg`, fill an n x n map with
     ensemble-spread fallback and a seeded 1 % audit (both traced with `cfg`), and compare
     the map time with tracing every pixel."""
@@ -666,7 +666,7 @@ def _surrogate_map(args, metric, patch, cfg, fp64_rays_s, train_steps):
     uv, y, _, info = training_set(metric, patch, n_train, cfg, seed=1)
     tracer_rays_s = n_train / info["trace_s"]
     model = SkySurrogate(n_members=4, n_out=y.shape[1], seed=0, device=torch_device())
-    rep = model.fit(uv, y, steps=train_steps, batch=8192, lr=2e-3, log_every=1000)
+    rep = model.fit(uv, y, steps=train_steps, batch=8192, lr=lr, log_every=1000)
     fill_sky_map(model, metric, patch, cfg, n_side=128, std_threshold=1e-7, audit_fraction=0.01, audit_seed=6)
     _, mrep = fill_sky_map(model, metric, patch, cfg, n_side=args.map_side, std_threshold=1e-7,
                            audit_fraction=0.01, audit_seed=5)
@@ -781,7 +781,7 @@ def run_surrogate_smooth(args, dev):
            "fp64_parity_status_counts": np.bincount(r.status.cpu().numpy(), minlength=12).tolist(),
            "mixed_on_sample": {"rays_per_s": mixed_rays_s, "speedup_vs_fp64": mixed_rays_s / fp64_rays_s,
                                "retrace_fraction": retrace, **errors_vs(r, rm)}}
-    out.update(_surrogate_map(args, metric, patch, cfg, fp64_rays_s, args.smooth_train_steps))
+    out.update(_surrogate_map(args, metric, patch, cfg, fp64_rays_s, args.smooth_train_steps, lr=3e-3))
     return out
 
 

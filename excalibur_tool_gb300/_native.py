@@ -114,6 +114,13 @@ class ExcBornArgs(C.Structure):
                 ("e1", C.c_double * 3), ("e2", C.c_double * 3), ("half", C.c_double), ("box_lo", C.c_double * 3),
                 ("box_hi", C.c_double * 3), ("step", C.c_double), ("c", C.c_double), ("out", C.c_void_p)]
 
+class ExcAdamTensor(C.Structure):
+    _fields_ = [("p", C.c_void_p), ("grad", C.c_void_p), ("m1", C.c_void_p), ("m2", C.c_void_p), ("n", C.c_int64),
+                ("p_bf16", C.c_void_p), ("pt_bf16", C.c_void_p), ("rows", C.c_int32), ("cols", C.c_int32)]
+
+
+EXC_ADAM_MAX_TENSORS = 16
+
 _V = C.c_void_p
 EXPORTS = {
     "exc_abi_version": (C.c_int, []),
@@ -152,6 +159,8 @@ EXPORTS = {
     "exc_mlp_row_sums": (C.c_int, [_V, C.c_int64, C.c_int64, C.c_int64, _V, _V]),
     "exc_mlp_adam": (C.c_int, [_V, _V, _V, _V, C.c_int64, C.c_float, C.c_float, C.c_float, C.c_float, C.c_int32,
                                _V, _V, C.c_int32, C.c_int32, _V]),
+    "exc_mlp_adam_multi": (C.c_int, [C.POINTER(ExcAdamTensor), C.c_int32, _V, C.c_float, C.c_float, C.c_float,
+                                     _V]),
     "exc_mlp_error_count": (C.c_int, [C.POINTER(C.c_uint32)]),
     "exc_born_patch": (C.c_int, [C.POINTER(ExcMetric), C.POINTER(ExcBornArgs), _V]),
 }

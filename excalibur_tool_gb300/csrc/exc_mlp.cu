@@ -387,93 +387,132 @@ __global__ void features_kernel(const double* dirs, int64_t n, int64_t n_pad, in
 }
 
 // ---------------------------------------------------------------------- head
-// One warp per row; lane l holds columns 8l .. 8l+7 of the 256-wide hidden row.
+// A block walks tiles of kHeadRows consecutive rows; in a tile each warp takes kHeadRows / 8
+// rows, one at a time, lane l holding columns 8l .. 8l+7 of the 256-wide hidden row. The
+// transposed output dHt is staged in shared memory and written column by column, a warp
+// storing 64 consecutive rows of one column as bf16 pairs (128 contiguous bytes), instead of
+// every lane scattering eight 2-byte stores one matrix row apart.
+constexpr int kHeadRows = 64;
+constexpr int kHeadStride = 258;   // bf16 per staged row: 129 words, odd, so column reads do not conflict
+
+// Two blocks per SM (at most 128 registers a thread): the grid of a training step is about two
+// blocks per SM, and one block a SM would leave eight warps to hide every load.
 template <int NOUT>
-__global__ void __launch_bounds__(256) head_kernel(const __nv_bfloat16* H, int64_t m, int n_members,
-                                                   const float* W, const float* bias, float* Y, const float* T,
-                                                   const __nv_bfloat16* Z, __nv_bfloat16* dH, __nv_bfloat16* dHt,
-                                                   int64_t ldt, float* dW, float* db, float* loss) {
+__global__ void __launch_bounds__(256, 2) head_kernel(const __nv_bfloat16* H, int64_t m, int n_members,
+                                                      const float* W, const float* bias, float* Y, const float* T,
+                                                      const __nv_bfloat16* Z, __nv_bfloat16* dH, __nv_bfloat16* dHt,
+                                                      int64_t ldt, float* dW, float* db, float* loss) {
   constexpr int width = 256;
+  static_assert(NOUT * width * 2 <= kHeadRows * kHeadStride, "sdw must fit in the staging tile");
   __shared__ float sw[NOUT * width];
-  __shared__ float sdw[NOUT * width];
   __shared__ float sdb[NOUT], sloss;
+  // the staging tile of dHt during the row loop; afterwards the block's weight-gradient sums
+  __shared__ __align__(16) __nv_bfloat16 tile[kHeadRows * kHeadStride];
+  float* sdw = reinterpret_cast<float*>(tile);
   const int e = blockIdx.y;
   const float* We = W + (int64_t)e * NOUT * width;
-  for (int i = threadIdx.x; i < NOUT * width; i += blockDim.x) { sw[i] = We[i]; sdw[i] = 0.0f; }
+  for (int i = threadIdx.x; i < NOUT * width; i += blockDim.x) sw[i] = We[i];
   if (threadIdx.x < NOUT) sdb[threadIdx.x] = 0.0f;
   if (threadIdx.x == 0) sloss = 0.0f;
   __syncthreads();
   const int lane = threadIdx.x & 31;
-  const int wpb = blockDim.x >> 5;
-  const int64_t wid = (int64_t)blockIdx.x * wpb + (threadIdx.x >> 5);
-  const int64_t nw = (int64_t)gridDim.x * wpb;
+  const int warp = threadIdx.x >> 5;
+  constexpr int rows_per_warp = kHeadRows / 8;
   float gw[NOUT][8];
   float gb[NOUT];
 #pragma unroll
   for (int j = 0; j < NOUT; ++j) { gb[j] = 0.0f; for (int q = 0; q < 8; ++q) gw[j][q] = 0.0f; }
   float lsum = 0.0f;
   const float inv = 2.0f / ((float)m * (float)NOUT);
-  for (int64_t row = wid; row < m; row += nw) {
-    const int64_t off = ((int64_t)e * m + row) * width + lane * 8;
-    const uint4 raw = *reinterpret_cast<const uint4*>(H + off);
-    const __nv_bfloat16* hb = reinterpret_cast<const __nv_bfloat16*>(&raw);
-    float h[8];
+  const int64_t n_tiles = (m + kHeadRows - 1) / kHeadRows;
+  for (int64_t tile_i = blockIdx.x; tile_i < n_tiles; tile_i += gridDim.x) {
+    const int64_t r0 = tile_i * kHeadRows;
+    for (int k = 0; k < rows_per_warp; ++k) {
+      const int jr = warp * rows_per_warp + k;
+      const int64_t row = r0 + jr;
+      if (row >= m) break;
+      const int64_t off = ((int64_t)e * m + row) * width + lane * 8;
+      const uint4 raw = *reinterpret_cast<const uint4*>(H + off);
+      const __nv_bfloat16* hb = reinterpret_cast<const __nv_bfloat16*>(&raw);
+      float h[8];
 #pragma unroll
-    for (int q = 0; q < 8; ++q) h[q] = __bfloat162float(hb[q]);
-    float y[NOUT];
-#pragma unroll
-    for (int j = 0; j < NOUT; ++j) {
-      float acc = 0.0f;
-#pragma unroll
-      for (int q = 0; q < 8; ++q) acc = fmaf(h[q], sw[j * width + lane * 8 + q], acc);
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-      y[j] = acc + __ldg(bias + (int64_t)e * NOUT + j);
-    }
-    if (Y && lane < NOUT) {
-#pragma unroll
-      for (int j = 0; j < NOUT; ++j)
-        if (lane == j) Y[((int64_t)e * m + row) * NOUT + j] = y[j];
-    }
-    if (!T) continue;
-    float dy[NOUT];
-#pragma unroll
-    for (int j = 0; j < NOUT; ++j) {
-      const float d = y[j] - __ldg(T + row * NOUT + j);
-      lsum += lane == 0 ? d * d : 0.0f;
-      dy[j] = inv * d;
-      gb[j] += lane == 0 ? dy[j] : 0.0f;
-    }
-    float zf[8];
-    if (Z) {
-      const uint4 zr = *reinterpret_cast<const uint4*>(Z + off);
-      const __nv_bfloat16* zb = reinterpret_cast<const __nv_bfloat16*>(&zr);
-#pragma unroll
-      for (int q = 0; q < 8; ++q) zf[q] = __bfloat162float(zb[q]);
-    }
-    __nv_bfloat16 out[8];
-#pragma unroll
-    for (int q = 0; q < 8; ++q) {
-      float g = 0.0f;
+      for (int q = 0; q < 8; ++q) h[q] = __bfloat162float(hb[q]);
+      float y[NOUT];
 #pragma unroll
       for (int j = 0; j < NOUT; ++j) {
-        g = fmaf(dy[j], sw[j * width + lane * 8 + q], g);
-        gw[j][q] = fmaf(dy[j], h[q], gw[j][q]);
-      }
-      if (Z) {
-        const float sg = sigmoid(zf[q]);
-        g *= sg * (1.0f + zf[q] * (1.0f - sg));
-      }
-      out[q] = __float2bfloat16_rn(g);
-    }
-    if (dH) *reinterpret_cast<uint4*>(dH + off) = *reinterpret_cast<uint4*>(out);
-    if (dHt) {
-      __nv_bfloat16* Tt = dHt + (int64_t)e * width * ldt + row;
+        float acc = 0.0f;
 #pragma unroll
-      for (int q = 0; q < 8; ++q) Tt[(int64_t)(lane * 8 + q) * ldt] = out[q];
+        for (int q = 0; q < 8; ++q) acc = fmaf(h[q], sw[j * width + lane * 8 + q], acc);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        y[j] = acc + __ldg(bias + (int64_t)e * NOUT + j);
+      }
+      if (Y && lane < NOUT) {
+#pragma unroll
+        for (int j = 0; j < NOUT; ++j)
+          if (lane == j) Y[((int64_t)e * m + row) * NOUT + j] = y[j];
+      }
+      if (!T) continue;
+      float dy[NOUT];
+#pragma unroll
+      for (int j = 0; j < NOUT; ++j) {
+        const float d = y[j] - __ldg(T + row * NOUT + j);
+        lsum += lane == 0 ? d * d : 0.0f;
+        dy[j] = inv * d;
+        gb[j] += lane == 0 ? dy[j] : 0.0f;
+      }
+      float zf[8];
+      if (Z) {
+        const uint4 zr = *reinterpret_cast<const uint4*>(Z + off);
+        const __nv_bfloat16* zb = reinterpret_cast<const __nv_bfloat16*>(&zr);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) zf[q] = __bfloat162float(zb[q]);
+      }
+      __nv_bfloat16 out[8];
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        float g = 0.0f;
+#pragma unroll
+        for (int j = 0; j < NOUT; ++j) {
+          g = fmaf(dy[j], sw[j * width + lane * 8 + q], g);
+          gw[j][q] = fmaf(dy[j], h[q], gw[j][q]);
+        }
+        if (Z) {
+          const float sg = sigmoid(zf[q]);
+          g *= sg * (1.0f + zf[q] * (1.0f - sg));
+        }
+        out[q] = __float2bfloat16_rn(g);
+      }
+      if (dH) *reinterpret_cast<uint4*>(dH + off) = *reinterpret_cast<uint4*>(out);
+      if (dHt) {
+#pragma unroll
+        for (int q = 0; q < 8; ++q) tile[jr * kHeadStride + lane * 8 + q] = out[q];
+      }
+    }
+    if (dHt) {
+      // tile[jr][c] -> dHt[e][c][r0 + jr]: warp w writes columns w, w + 8, ...; lane l the rows
+      // 2l and 2l + 1 as one bf16 pair (ldt is even, r0 a multiple of 64: 4-byte aligned)
+      __syncthreads();
+      const int64_t rows_here = (m - r0) < kHeadRows ? (m - r0) : kHeadRows;
+      const int ja = 2 * lane, jb = 2 * lane + 1;
+      for (int c = warp; c < width; c += 8) {
+        __nv_bfloat16* dst = dHt + ((int64_t)e * width + c) * ldt + r0;
+        if (jb < rows_here) {
+          __nv_bfloat162 v;
+          v.x = tile[ja * kHeadStride + c];
+          v.y = tile[jb * kHeadStride + c];
+          *reinterpret_cast<__nv_bfloat162*>(dst + ja) = v;
+        } else if (ja < rows_here) {
+          dst[ja] = tile[ja * kHeadStride + c];
+        }
+      }
+      __syncthreads();   // the tile is rewritten by the next one
     }
   }
   if (T) {
+    __syncthreads();   // every warp is done with the staging tile
+    for (int i = threadIdx.x; i < NOUT * width; i += blockDim.x) sdw[i] = 0.0f;
+    __syncthreads();
 #pragma unroll
     for (int j = 0; j < NOUT; ++j) {
 #pragma unroll
@@ -534,6 +573,35 @@ __global__ void adam_kernel(float* p, const float* g, float* m1, float* m2, int6
       const int64_t e = i / per, w = i - e * per;
       const int r = (int)(w / cols), c = (int)(w - (int64_t)r * cols);
       pt[e * per + (int64_t)c * rows + r] = bv;
+    }
+  }
+}
+
+struct AdamMulti {
+  ExcAdamTensor t[EXC_ADAM_MAX_TENSORS];
+};
+
+// blockIdx.y selects the tensor; the schedule {lr, c1, c2} is read once per thread.
+__global__ void adam_multi_kernel(const AdamMulti P, const float* sched, float b1, float b2, float eps) {
+  const ExcAdamTensor& T = P.t[blockIdx.y];
+  const float lr = sched[0], c1 = sched[1], c2 = sched[2];
+  __nv_bfloat16* pb = (__nv_bfloat16*)T.p_bf16;
+  __nv_bfloat16* pt = (__nv_bfloat16*)T.pt_bf16;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < T.n; i += (int64_t)gridDim.x * blockDim.x) {
+    const float gi = T.grad[i];
+    const float a = b1 * T.m1[i] + (1.0f - b1) * gi;
+    const float v = b2 * T.m2[i] + (1.0f - b2) * gi * gi;
+    T.m1[i] = a;
+    T.m2[i] = v;
+    const float pi = T.p[i] - lr * (a * c1) / (sqrtf(v * c2) + eps);
+    T.p[i] = pi;
+    const __nv_bfloat16 bv = __float2bfloat16_rn(pi);
+    if (pb) pb[i] = bv;
+    if (pt) {
+      const int64_t per = (int64_t)T.rows * T.cols;
+      const int64_t e = i / per, w = i - e * per;
+      const int r = (int)(w / T.cols), c = (int)(w - (int64_t)r * T.cols);
+      pt[e * per + (int64_t)c * T.rows + r] = bv;
     }
   }
 }
@@ -664,8 +732,22 @@ int exc_mlp_head(const void* h, int64_t m, int32_t width, int32_t n_out, int32_t
   if (targets && (!dw || !db || !loss)) return mlp_fail(EXC_ERR_INVALID, "head: training needs dw, db, loss");
   if ((z && !aligned16(z)) || (dh && !aligned16(dh)) || (dht && ldt < m))
     return mlp_fail(EXC_ERR_INVALID, "head: z/dh must be 16-byte aligned, ldt >= m");
+  if (dht && (ldt & 1)) return mlp_fail(EXC_ERR_INVALID, "head: ldt must be even");
   const int block = 256;
-  int64_t blocks = (m + 7) / 8;
+  const int64_t n_tiles = (m + kHeadRows - 1) / kHeadRows;
+  int64_t blocks = n_tiles;
+  if (targets) {
+    // Training: each block adds its partial weight and bias gradients (NOUT x 257 floats) into
+    // dw/db with one global atomic per entry, all blocks of a member on the same few addresses,
+    // so the block count sets that serialised atomic traffic. About two blocks per SM over all
+    // members keep the row loads in flight; the tiles are then shared out evenly.
+    const int64_t per_member = (2 * 152 + n_members - 1) / n_members;
+    const int64_t cap = per_member < 16 ? 16 : per_member;
+    if (blocks > cap) {
+      const int64_t tiles_per_block = (n_tiles + cap - 1) / cap;
+      blocks = (n_tiles + tiles_per_block - 1) / tiles_per_block;
+    }
+  }
   if (blocks > 152 * 8) blocks = 152 * 8;
   dim3 grid((unsigned)blocks, (unsigned)n_members);
   cudaStream_t s = (cudaStream_t)stream;
@@ -711,6 +793,29 @@ int exc_mlp_adam(float* p, const float* grad, float* m1, float* m2, int64_t n, f
   adam_kernel<<<grid_for(n, 256), 256, 0, (cudaStream_t)stream>>>(p, grad, m1, m2, n, lr, beta1, beta2, eps, c1, c2,
                                                                  (__nv_bfloat16*)p_bf16, (__nv_bfloat16*)pt_bf16,
                                                                  rows, cols);
+  return mlp_cuda(cudaGetLastError());
+}
+
+int exc_mlp_adam_multi(const ExcAdamTensor* tensors, int32_t n_tensors, const float* sched, float beta1,
+                       float beta2, float eps, void* stream) {
+  if (!tensors || !sched || n_tensors < 1 || n_tensors > EXC_ADAM_MAX_TENSORS)
+    return mlp_fail(EXC_ERR_INVALID, "adam_multi: 1..EXC_ADAM_MAX_TENSORS tensors and a schedule are required");
+  AdamMulti P;
+  int64_t nmax = 0;
+  for (int k = 0; k < n_tensors; ++k) {
+    const ExcAdamTensor& T = tensors[k];
+    if (!T.p || !T.grad || !T.m1 || !T.m2 || T.n < 1)
+      return mlp_fail(EXC_ERR_INVALID, "adam_multi: every tensor needs p, grad, m1, m2 and n >= 1");
+    if (T.pt_bf16 && (T.rows < 1 || T.cols < 1 || T.n % ((int64_t)T.rows * T.cols)))
+      return mlp_fail(EXC_ERR_INVALID, "adam_multi: n must be a multiple of rows*cols for a transposed copy");
+    P.t[k] = T;
+    if (T.n > nmax) nmax = T.n;
+  }
+  int64_t bx = (nmax + 255) / 256;
+  const int64_t cap = (152 * 16 + n_tensors - 1) / n_tensors;
+  if (bx > cap) bx = cap;
+  dim3 grid((unsigned)(bx < 1 ? 1 : bx), (unsigned)n_tensors);
+  adam_multi_kernel<<<grid, 256, 0, (cudaStream_t)stream>>>(P, sched, beta1, beta2, eps);
   return mlp_cuda(cudaGetLastError());
 }
 

@@ -107,6 +107,23 @@ def adam(p, g, m1, m2, *, lr, beta1, beta2, eps, t, p_bf16=None, pt_bf16=None, s
                              _p(pt_bf16), rows, cols, _stream(p)), "exc_mlp_adam")
 
 
+def adam_multi(tensors, sched, *, beta1, beta2, eps):
+    """One Adam step over every (p, g, m1, m2, p_bf16, pt_bf16, shape) in `tensors` in a single
+    launch, {lr, 1/(1-beta1^t), 1/(1-beta2^t)} read from the float32 device tensor `sched`.
+    """
+    arr = (N.ExcAdamTensor * len(tensors))()
+    for k, (p, g, m1, m2, pb, pt, shape) in enumerate(tensors):
+        a = arr[k]
+        a.p, a.grad, a.m1, a.m2 = p.data_ptr(), g.data_ptr(), m1.data_ptr(), m2.data_ptr()
+        a.n = p.numel()
+        a.p_bf16 = pb.data_ptr() if pb is not None else None
+        a.pt_bf16 = pt.data_ptr() if pt is not None else None
+        a.rows, a.cols = (shape if shape is not None else (0, 0))
+    lib = N.load()
+    N.check(lib.exc_mlp_adam_multi(arr, len(tensors), _p(sched), beta1, beta2, eps, _stream(sched)),
+            "exc_mlp_adam_multi")
+
+
 def error_count() -> int:
     v = C.c_uint32(0)
     N.check(N.load().exc_mlp_error_count(C.byref(v)), "exc_mlp_error_count")

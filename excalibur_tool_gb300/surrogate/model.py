@@ -157,12 +157,34 @@ class SkySurrogate:
             if l > 0:
                 K.gemm(dZ[l], self.wtb[l], epilogue="dsilu", z_in=Z[l - 1], c=dZ[l - 1], ct=dZT[l - 1])
 
+    def _schedule(self, steps, lr, lr_final, beta1=0.9, beta2=0.999):
+        """[steps, 3] float32 {lr_t, 1/(1-beta1^t), 1/(1-beta2^t)}: the values the eager step
+        passes to exc_mlp_adam (lr_t rounded to float32; the corrections in float32 powf, as
+        the library computes them)."""
+        out = np.empty((steps, 3), dtype=np.float32)
+        one, b1, b2 = np.float32(1.0), np.float32(beta1), np.float32(beta2)
+        for step in range(steps):
+            t = np.float32(self._t + 1 + step)
+            out[step, 0] = np.float32(lr_final + 0.5 * (lr - lr_final) * (1 + math.cos(math.pi * step / max(1, steps - 1))))
+            out[step, 1] = one / (one - np.power(b1, t))
+            out[step, 2] = one / (one - np.power(b2, t))
+        return out
+
     def fit(self, uv: np.ndarray, targets: np.ndarray, steps: int = 3000, batch: int = 8192, lr: float = 2e-3,
-            lr_final: float = 2e-5, seed: int = 1, k_splits: int = 32, log_every: int = 100,
-            extra: Optional[np.ndarray] = None) -> TrainReport:
+            lr_final: float = 2e-5, seed: int = 1, k_splits: int = 16, log_every: int = 100,
+            extra: Optional[np.ndarray] = None, graph: bool = True, graph_steps: int = 16) -> TrainReport:
         """Train every member on (uv [n, 2] in [-1, 1]^2, targets [n, n_out]) with Adam and a cosine
         schedule; `extra` [n, k] are per-direction baseline features (the same must be given to
-        prediction)."""
+        prediction).
+
+        With `graph` (default), `graph_steps` consecutive training steps -- forward, backward and
+        Adam, about forty kernels each -- are captured once in a CUDA graph and replayed: the host
+        fills a chunk of batches and the steps' learning rates and bias corrections into static
+        device buffers, then issues one graph launch, so the step time is the GPU's and not the
+        host's launch rate. The steps are the eager loop's, batch for batch and value for value."""
+        if graph:
+            return self._fit_graphed(uv, targets, steps, batch, lr, lr_final, seed, k_splits, log_every, extra,
+                                     graph_steps)
         import time
 
         import torch
@@ -203,6 +225,89 @@ class SkySurrogate:
                     K.adam(p, g, m1, m2, lr=lr_t, beta1=0.9, beta2=0.999, eps=1e-8, t=self._t)
             if log_every and (step % log_every == 0 or step == steps - 1):
                 curve.append((step, (buf["loss"] / (B * self.n_out)).cpu().tolist()))
+        torch.cuda.synchronize(dev)
+        secs = time.perf_counter() - t0
+        return TrainReport(steps, B, curve[-1][1] if curve else [], secs, curve)
+
+    def _fit_graphed(self, uv, targets, steps, batch, lr, lr_final, seed, k_splits, log_every, extra, K_steps):
+        import time
+
+        import torch
+
+        if batch % 128:
+            raise ValueError("batch must be a multiple of 128")
+        if K_steps < 1:
+            raise ValueError("graph_steps must be >= 1")
+        n = uv.shape[0]
+        self.set_normalisation(uv, targets, extra)
+        dev = self.device
+        uv_d = torch.as_tensor(np.ascontiguousarray(uv, dtype=np.float64), device=dev)
+        t_d = torch.as_tensor(self._normalise(uv, targets, extra), device=dev)
+        B = batch
+        buf = self._buffers(B, k_splits)
+        if self._adam is None:
+            self._adam = [(torch.zeros_like(p), torch.zeros_like(p)) for p in self.params()]
+        sched_all = torch.as_tensor(self._schedule(steps, lr, lr_final), device=dev)
+        K_steps = min(K_steps, max(1, steps))
+        uv_c = torch.empty((K_steps * B, 2), dtype=torch.float64, device=dev)
+        t_c = torch.empty((K_steps * B, t_d.shape[1]), dtype=torch.float32, device=dev)
+        sched_c = torch.empty((K_steps, 3), dtype=torch.float32, device=dev)
+        gen = torch.Generator(device="cpu").manual_seed(seed)
+        state = {"perm": torch.randperm(n, generator=gen).to(dev), "pos": 0}
+
+        def batch_index():   # the eager loop's batch order
+            if state["pos"] + B > n:
+                state["perm"] = torch.randperm(n, generator=gen).to(dev)
+                state["pos"] = 0
+            idx = state["perm"][state["pos"]:state["pos"] + B]
+            state["pos"] += B
+            return idx
+
+        def fill(step0, k):
+            idx = torch.cat([batch_index() for _ in range(k)])
+            torch.index_select(uv_d, 0, idx, out=uv_c[:k * B])
+            torch.index_select(t_d, 0, idx, out=t_c[:k * B])
+            sched_c[:k].copy_(sched_all[step0:step0 + k])
+
+        grads = buf["gw"] + buf["gb"] + [buf["gwh"], buf["gbh"]]
+        groups = []
+        for i, (p, g) in enumerate(zip(self.params(), grads)):
+            m1, m2 = self._adam[i]
+            if i < self.depth:
+                groups.append((p, g, m1, m2, self.wb[i], self.wtb[i], (p.shape[1], p.shape[2])))
+            else:
+                groups.append((p, g, m1, m2, None, None, None))
+
+        def one_step(j):
+            self.forward_backward(uv_c[j * B:(j + 1) * B], t_c[j * B:(j + 1) * B], buf)
+            K.adam_multi(groups, sched_c[j], beta1=0.9, beta2=0.999, eps=1e-8)   # every tensor, one launch
+
+        curve = []
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        step, g = 0, None
+        while step < steps:
+            k = min(K_steps, steps - step)
+            fill(step, k)
+            if k == K_steps and g is None and step > 0:
+                # captured after one eager chunk has run (kernels loaded, attributes set)
+                g = torch.cuda.CUDAGraph()
+                side = torch.cuda.Stream(dev)
+                side.wait_stream(torch.cuda.current_stream(dev))
+                with torch.cuda.graph(g, stream=side):
+                    for j in range(K_steps):
+                        one_step(j)
+            if k == K_steps and g is not None:
+                g.replay()
+            else:
+                for j in range(k):
+                    one_step(j)
+                    if log_every and step == 0 and j == 0:
+                        curve.append((0, (buf["loss"] / (B * self.n_out)).cpu().tolist()))
+            self._t += k
+            step += k
+            if log_every and (step // log_every != (step - k) // log_every or step == steps):
+                curve.append((step - 1, (buf["loss"] / (B * self.n_out)).cpu().tolist()))
         torch.cuda.synchronize(dev)
         secs = time.perf_counter() - t0
         return TrainReport(steps, B, curve[-1][1] if curve else [], secs, curve)

@@ -92,6 +92,27 @@ int exc_mlp_row_sums(const void* x, int64_t rows, int64_t m, int64_t ld, float* 
 int exc_mlp_adam(float* p, const float* grad, float* m1, float* m2, int64_t n, float lr, float beta1, float beta2,
                  float eps, int32_t t, void* p_bf16, void* pt_bf16, int32_t rows, int32_t cols, void* stream);
 
+/* One parameter tensor of a multi-tensor Adam step (fields as in exc_mlp_adam). */
+typedef struct ExcAdamTensor {
+  float* p;
+  const float* grad;
+  float* m1;
+  float* m2;
+  int64_t n;
+  void* p_bf16;      /* optional bf16 copy */
+  void* pt_bf16;     /* optional transposed bf16 copy ([cols][rows] per matrix) */
+  int32_t rows, cols;
+} ExcAdamTensor;
+#define EXC_ADAM_MAX_TENSORS 16
+
+/* exc_mlp_adam over up to EXC_ADAM_MAX_TENSORS tensors in one launch (the network's weights,
+ * biases and head of every ensemble member in a training step), with the step's learning rate
+ * and bias corrections read on the device from sched = {lr, 1 / (1 - beta1^t),
+ * 1 / (1 - beta2^t)} (float32): a training step captured once in a CUDA graph can then be
+ * replayed with a schedule that changes every step. */
+int exc_mlp_adam_multi(const ExcAdamTensor* tensors, int32_t n_tensors, const float* sched, float beta1,
+                       float beta2, float eps, void* stream);
+
 /* First-order (Born) line integrals along the straight rays of a tangent-plane
  * patch, the baseline features of the sky-map surrogate. For ray i, d = unit(axis
  * + uv[i][0] half e1 + uv[i][1] half e2) from origin (x, y, z) to the first face of

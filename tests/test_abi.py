@@ -116,11 +116,12 @@ def test_struct_layout_matches_c():
 #include "excalibur_gb300.h"
 #include "excalibur_mlp.h"
 int main(void) {
-  printf("%zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu\n", sizeof(ExcField), sizeof(ExcMetric),
+  printf("%zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu\n", sizeof(ExcField), sizeof(ExcMetric),
          sizeof(ExcTraceArgs), offsetof(ExcMetric, fields), offsetof(ExcTraceArgs, dt), offsetof(ExcTraceArgs, queue),
          offsetof(ExcTraceArgs, deadline_cycles), sizeof(ExcGemm), offsetof(ExcGemm, bias),
          offsetof(ExcGemm, stride_ct), sizeof(ExcPhotonGen), offsetof(ExcPhotonGen, uv), sizeof(ExcLaunchPlan),
-         offsetof(ExcLaunchPlan, trial_rate));
+         offsetof(ExcLaunchPlan, trial_rate), offsetof(ExcField, shift), sizeof(ExcAdamTensor),
+         offsetof(ExcAdamTensor, rows));
   return 0;
 }
 '''
@@ -133,5 +134,6 @@ int main(void) {
     want = [C.sizeof(N.ExcField), C.sizeof(N.ExcMetric), C.sizeof(N.ExcTraceArgs), N.ExcMetric.fields.offset,
             N.ExcTraceArgs.dt.offset, N.ExcTraceArgs.queue.offset, N.ExcTraceArgs.deadline_cycles.offset,
             C.sizeof(N.ExcGemm), N.ExcGemm.bias.offset, N.ExcGemm.stride_ct.offset, C.sizeof(N.ExcPhotonGen),
-            N.ExcPhotonGen.uv.offset, C.sizeof(N.ExcLaunchPlan), N.ExcLaunchPlan.trial_rate.offset]
+            N.ExcPhotonGen.uv.offset, C.sizeof(N.ExcLaunchPlan), N.ExcLaunchPlan.trial_rate.offset,
+            N.ExcField.shift.offset, C.sizeof(N.ExcAdamTensor), N.ExcAdamTensor.rows.offset]
     assert got == want
