@@ -67,6 +67,11 @@ def parse():
     p.add_argument("--no-sweep", action="store_true", help="skip the comparison-sweep leg")
     p.add_argument("--profile-gemm", type=int, default=0, metavar="M",
                    help="only time the surrogate's tensor-core GEMM on M rows (for profiling) and exit")
+    p.add_argument("--profile-training", type=int, default=0, metavar="STEPS",
+                   help="only run STEPS graph-captured surrogate training steps (batch 8192, 4 members, 6 "
+                        "outputs, synthetic targets) and exit")
+    p.add_argument("--profile-sweep", action="store_true",
+                   help="only run the 32-row comparison sweep of the sweep leg once and exit")
     p.add_argument("--map-side", type=int, default=4096)
     p.add_argument("--train-steps", type=int, default=8000)
     p.add_argument("--smooth-train-steps", type=int, default=16000,
@@ -688,6 +693,21 @@ def _surrogate_map(args, metric, patch, cfg, fp64_rays_s, train_steps, lr=2e-3):
     }
 
 
+def profile_training(steps):
+    """`steps` graph-captured training steps of the surrogate (4 members, 6 outputs, batch 8192)
+    on 1,048,576 synthetic smooth targets, after a 32-step warm-up fit."""
+    from excalibur_tool_gb300.surrogate.model import SkySurrogate
+
+    rng = np.random.default_rng(4)
+    uv = rng.uniform(-1, 1, (1 << 20, 2))
+    y = np.stack([np.sin(3 * uv[:, 0]) * uv[:, 1], uv[:, 0] ** 2, np.cos(2 * uv[:, 1]), uv[:, 0] * uv[:, 1],
+                  uv[:, 1], uv[:, 0]], 1)
+    SkySurrogate(n_members=4, n_out=6, seed=0, device=torch_device()).fit(uv, y, steps=32, batch=8192, log_every=0)
+    m = SkySurrogate(n_members=4, n_out=6, seed=0, device=torch_device())
+    rep = m.fit(uv, y, steps=steps, batch=8192, log_every=0)
+    return {"training_steps": steps, "ms_per_step": 1e3 * rep.seconds / steps, "batch": 8192, "members": 4}
+
+
 def torch_device():
     import torch
 
@@ -913,6 +933,22 @@ def main():
         dev = torch.device("cuda", 0)
         tf, sec, fl = gemm_tflops(dev, torch.cuda.current_stream(dev), m=args.profile_gemm)
         print(json.dumps({"gemm_tflops": tf, "ms": sec * 1e3, "flops": fl, "rows": args.profile_gemm}), flush=True)
+        return
+    if args.profile_training:
+        print(json.dumps(profile_training(args.profile_training)), flush=True)
+        return
+    if args.profile_sweep:
+        import torch
+        from excalibur_tool_gb300.runners import sweep as S
+
+        with tempfile.TemporaryDirectory() as tmp:
+            path = os.path.join(tmp, "manifest.csv")
+            S.make_manifest(path, **SWEEP_MANIFEST)
+            jobs = S.read_jobs(path)
+        t0 = time.perf_counter()
+        res = S.run_jobs(jobs)
+        torch.cuda.synchronize()
+        print(json.dumps({"sweep_rows": len(res), "seconds": time.perf_counter() - t0}), flush=True)
         return
     rank, world, local = dist_setup(args.gpus)
     if args.impl == "reference":

@@ -177,3 +177,27 @@ def test_sweep_rows_match_oracle(cuda):
             assert _scaled_err(gs[ok], os_[ok][:, : gs.shape[1]]) <= 1e-12
         else:
             assert np.all(ost == 6) and got[j.jobid].error.startswith("every photon of the Schwarzschild leg")
+
+
+def test_impact_runner_matches_oracle(cuda):
+    """The impact-parameter runner (sampling "impact": impact-parameter bins, seed 0; a photon
+    that fails keeps its history up to the failure) against the oracle fed the same states."""
+    cfg = R.run_config(mass_msun=1e14, distance_mpc=300.0, flrw_grid_N=64, record_every=8, sampling="impact",
+                       b_min_mpc=0.5, b_max_mpc=3.0, b_nbins=3, b_nperbin=20, n_photons=20, static=True,
+                       flrw_local_coords=True, progress_every=0)
+    geo = R.geometry(cfg)
+    res = R.run(cfg)
+    assert res.flrw.trajectories.shape[0] == 60 and res.schwarzschild.trajectories.shape[0] == 60
+    _, fs, _ = R.flrw_setup(cfg, geo, impact_runner=True)
+    _, ss, _, _ = R.schwarzschild_setup(cfg, geo, impact_runner=True)
+    of, fst = _oracle_leg(cfg, geo, fs.cpu().numpy(), "flrw", R.flrw_potential(cfg, geo))
+    assert np.array_equal(res.flrw.trajectories, of, equal_nan=True) and np.all(fst == 0)
+    os_, sst = _oracle_leg(cfg, geo, ss.cpu().numpy(), "schwarzschild")
+    assert np.array_equal(res.schwarzschild.status, sst)
+    ok = sst == 0
+    gs = res.schwarzschild.trajectories
+    if ok.any():
+        assert _scaled_err(gs[ok], os_[ok][:, : gs.shape[1]]) <= 1e-12
+    # failed photons keep their records up to the failure (not emptied, unlike the plain runner)
+    for i in np.flatnonzero(~ok):
+        assert np.isfinite(gs[i, 0]).all()
