@@ -113,6 +113,12 @@ __device__ __forceinline__ double trilinear(double c000, double c100, double c01
          c111 * dx * dy * dz;
 }
 
+// True when the field carries a query offset (any non-zero bit in ExcField.shift).
+__device__ __forceinline__ bool has_shift(const ExcField& f) {
+  return (__double_as_longlong(f.shift[0]) | __double_as_longlong(f.shift[1]) |
+          __double_as_longlong(f.shift[2])) != 0;
+}
+
 // One spatial snapshot `it` (of nt, innermost index) of a 3-D/4-D field.
 // Returns an EXC_PH_* failure code, or 0 with `o` filled (o.dtd = 0).
 // The cell coordinate rel = (x - origin) / spacing is an IEEE division in
@@ -275,9 +281,11 @@ __device__ __forceinline__ void slow_gradient(const ExcField& f, const double* f
 template <class FT>
 __device__ __forceinline__ int slow_value3(const ExcField& f, double x, double y, double z, double& val) {
   const FT* d = (const FT*)f.data;
-  x += f.shift[0];
-  y += f.shift[1];
-  z += f.shift[2];
+  if (has_shift(f)) {
+    x += f.shift[0];
+    y += f.shift[1];
+    z += f.shift[2];
+  }
   const int64_t nx = f.n[0], ny = f.n[1], nz = f.n[2];
   const double rx = (x - f.origin[0]) / f.spacing[0];
   const double ry = (y - f.origin[1]) / f.spacing[1];
@@ -379,10 +387,13 @@ template <class FT, bool SLOW = true>
 __device__ __forceinline__ int interp_field(const ExcField& f, const double* fi, double x, double y, double z,
                                             double t, InterpOut& o) {
   const FT* d = (const FT*)f.data;
-  // a shifted interpolator queries x + shift (ExcField.shift; zero = none)
-  x += f.shift[0];
-  y += f.shift[1];
-  z += f.shift[2];
+  // a shifted interpolator queries x + shift (ExcField.shift; zero = none). The test is on the
+  // bit patterns (integer pipe, uniform per launch): an unshifted grid costs no FP64 operation.
+  if (has_shift(f)) {
+    x += f.shift[0];
+    y += f.shift[1];
+    z += f.shift[2];
+  }
   if constexpr (SLOW) {
     if (f.grad_mode == EXC_GRAD_TRILINEAR) return interp_slow<FT>(f, fi, d, x, y, z, t, o);
   }

@@ -198,6 +198,7 @@ def test_impact_runner_matches_oracle(cuda):
     gs = res.schwarzschild.trajectories
     if ok.any():
         assert _scaled_err(gs[ok], os_[ok][:, : gs.shape[1]]) <= 1e-12
-    # failed photons keep their records up to the failure (not emptied, unlike the plain runner)
+    # failed photons keep their records up to the failure (not emptied, unlike the plain runner);
+    # the state columns of the first record are finite (its quantity columns lag one record)
     for i in np.flatnonzero(~ok):
-        assert np.isfinite(gs[i, 0]).all()
+        assert np.isfinite(gs[i, 0, :8]).all()
