@@ -70,7 +70,6 @@ def test_stats_edge_cases():
 
 
 def _oracle_leg(cfg, geo, states, kind, phi=None):
-    from excalibur_tool_gb300.core.constants import c
     from excalibur_tool_gb300.trace import TraceConfig
     from oracle import oracle as O
     from oracle.oracle import FieldSpec, Spacetime

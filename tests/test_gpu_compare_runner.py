@@ -8,7 +8,6 @@ import pytest
 from conftest import golden
 from helpers import rel_err
 from test_compare_runner import _oracle_leg, job1_config
-from excalibur_tool_gb300.runners import analyze as A
 from excalibur_tool_gb300.runners import compare as R
 
 pytestmark = pytest.mark.gpu
