@@ -297,6 +297,8 @@ def run_jobs(jobs: Iterable[Job], *, runner: str = "plain", max_fields: int = N.
     if not 1 <= max_fields <= N.EXC_MAX_FIELDS:
         raise ValueError(f"max_fields must be in [1, {N.EXC_MAX_FIELDS}]")
     jobs = list(jobs)
+    if not jobs:
+        return {}
     # launch groups from the row parameters alone (no device work yet)
     groups = {}
     for job in jobs:

@@ -137,3 +137,34 @@ int main(void) {
             N.ExcPhotonGen.uv.offset, C.sizeof(N.ExcLaunchPlan), N.ExcLaunchPlan.trial_rate.offset,
             N.ExcField.shift.offset, C.sizeof(N.ExcAdamTensor), N.ExcAdamTensor.rows.offset]
     assert got == want
+
+
+def test_new_entry_points_validate_before_any_launch(lib):
+    """Argument checks of the lens-grid, multi-tensor Adam and shifted-field paths run on the
+    host: the invalid calls below return an error without touching a device."""
+    L = N.load()
+    n = (C.c_int64 * 3)(0, 4, 4)
+    d3 = (C.c_double * 3)(0.0, 0.0, 0.0)
+    assert L.exc_spherical_mass_grid(n, d3, d3, d3, 1.0, -1.0, 3.0, 2.0, C.c_void_p(4096), None) == N.EXC_ERR_INVALID
+    assert b"n must be" in L.exc_last_error()
+    n_ok = (C.c_int64 * 3)(4, 4, 4)
+    assert L.exc_spherical_mass_grid(n_ok, d3, d3, d3, 1.0, -1.0, 3.0, 2.0, None, None) == N.EXC_ERR_INVALID
+    arr = (N.ExcAdamTensor * 1)()
+    assert L.exc_mlp_adam_multi(arr, 0, C.c_void_p(4096), 0.9, 0.999, 1e-8, None) == N.EXC_ERR_INVALID
+    assert L.exc_mlp_adam_multi(arr, N.EXC_ADAM_MAX_TENSORS + 1, C.c_void_p(4096), 0.9, 0.999, 1e-8,
+                                None) == N.EXC_ERR_INVALID
+    assert L.exc_mlp_adam_multi(arr, 1, C.c_void_p(4096), 0.9, 0.999, 1e-8, None) == N.EXC_ERR_INVALID  # p NULL
+    # a non-finite query offset is refused by the trace's field validation
+    m = N.ExcMetric()
+    m.kind = N.METRIC_FLRW
+    m.c, m.c2, m.c4 = 299792458.0, 299792458.0 ** 2, 299792458.0 ** 4
+    m.n_fields = 1
+    f = m.fields[0]
+    f.data = 4096
+    f.dtype = N.DTYPE_F64
+    f.ndim = 3
+    for d in range(3):
+        f.n[d], f.spacing[d] = 8, 1.0
+    f.shift[1] = float("nan")
+    assert L.exc_trace(C.byref(m), C.byref(_args()), None) == N.EXC_ERR_INVALID
+    assert b"shift" in L.exc_last_error()

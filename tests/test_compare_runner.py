@@ -197,3 +197,13 @@ def test_manifest_rows_to_runner_configs():
     assert geo.n_photons_effective == 30 and len(geo.b_edges) == 2
     with pytest.raises(SystemExit):
         S.read_job(runs["manifest_impact.csv"], 99)
+
+
+def test_empty_inputs():
+    from excalibur_tool_gb300.runners import sweep as S
+
+    st = A.trajectory_stats(np.zeros((0, 5, 14)), np.zeros(3), is_spherical=False)
+    assert st.table().shape == (0, 8)
+    st = A.trajectory_stats(np.zeros((0, 5, 12)), np.zeros(3), is_spherical=True)
+    assert st.table().shape == (0, 8)
+    assert S.run_jobs([]) == {}
