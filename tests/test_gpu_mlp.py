@@ -83,6 +83,45 @@ def test_gemm_dsilu(cuda):
     assert torch.equal(dt[:, :, :M], d.transpose(1, 2))
 
 
+@pytest.mark.parametrize("K,N,shared_a", [(256, 256, False), (256, 256, True), (128, 48, False)])
+def test_gemm_many_tiles(cuda, K, N, shared_a):
+    """More row tiles than the GPU holds at once (3 members x 313 tiles, the last one ragged),
+    every epilogue against torch, and an A shared by the members (the first inference layer)."""
+    import torch
+    from excalibur_tool_gb300.surrogate import kernels as Kn
+
+    E, M = 3, 40_000                                    # 3 x 313 tiles >= 4 x 152
+    a = _rand((M, K), 11) if shared_a else _rand((E, M, K), 11)
+    b = _rand((E, N, K), 12, 0.1)
+    af = a.float().expand(E, M, K) if shared_a else a.float()
+    acc = torch.bmm(af, b.float().transpose(1, 2))
+    c = torch.full((E, M, N), float("nan"), device="cuda")
+    Kn.gemm(a, b, epilogue="f32", c=c)
+    torch.cuda.synchronize()
+    assert torch.isfinite(c).all() and float((c - acc).abs().max()) <= 1e-5 * float(acc.abs().max())
+    bias = torch.randn(E, N, device="cuda") * 0.1
+    z = torch.empty((E, M, N), dtype=torch.bfloat16, device="cuda")
+    h = torch.empty_like(z)
+    ht = torch.zeros((E, N, M + 64), dtype=torch.bfloat16, device="cuda")
+    Kn.gemm(a, b, epilogue="bias_silu", bias=bias, c=z, c2=h, ct=ht)
+    torch.cuda.synchronize()
+    _close_bf16(z, acc + bias[:, None, :])
+    zq = z.float()
+    _close_bf16(h, zq * torch.sigmoid(zq))
+    assert torch.equal(ht[:, :, :M], h.transpose(1, 2)) and not bool(ht[:, :, M:].any())
+    if not shared_a:
+        zin = _rand((E, M, N), 13)
+        d = torch.empty((E, M, N), dtype=torch.bfloat16, device="cuda")
+        dt = torch.zeros((E, N, M), dtype=torch.bfloat16, device="cuda")
+        Kn.gemm(a, b, epilogue="dsilu", z_in=zin, c=d, ct=dt)
+        zf = zin.float()
+        sg = torch.sigmoid(zf)
+        torch.cuda.synchronize()
+        _close_bf16(d, acc * (sg * (1 + zf * (1 - sg))))
+        assert torch.equal(dt, d.transpose(1, 2))
+    assert Kn.error_count() == 0
+
+
 def test_gemm_split_k_weight_gradient(cuda):
     """dW = dZ^T . X with K = batch rows, split over CTAs and reduced."""
     import torch
