@@ -194,10 +194,12 @@ __device__ __forceinline__ void epilogue(const ExcGemm& g, uint32_t tmem, int64_
           const float zr = __bfloat162float(zb[i]);   // the value the backward pass will see
           hb[i] = __float2bfloat16_rn(zr * sigmoid(zr));
         }
-        uint4* d1 = reinterpret_cast<uint4*>(t1 + r * kPitchH + c0);
+        if (g.c) {   // the pre-activation is staged only when it is an output (training)
+          uint4* d1 = reinterpret_cast<uint4*>(t1 + r * kPitchH + c0);
+          d1[0] = *reinterpret_cast<uint4*>(&zb[0]);
+          d1[1] = *reinterpret_cast<uint4*>(&zb[8]);
+        }
         uint4* d2 = reinterpret_cast<uint4*>(t2 + r * kPitchH + c0);
-        d1[0] = *reinterpret_cast<uint4*>(&zb[0]);
-        d1[1] = *reinterpret_cast<uint4*>(&zb[8]);
         d2[0] = *reinterpret_cast<uint4*>(&hb[0]);
         d2[1] = *reinterpret_cast<uint4*>(&hb[8]);
       } else {  // EXC_EPI_DSILU
