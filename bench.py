@@ -360,12 +360,19 @@ def fp64_pipe_roofline(dev, stream, photon_steps_per_s):
 
     rates = fp64_pipe_rates(dev, stream)
     ops = roofline.OPS_PER_RK4_STEP_FLRW
-    slots = roofline.fp64_pipe_slots(ops, rates)
+    slots_ieee = roofline.fp64_pipe_slots(ops, rates)
+    slots = roofline.fp64_pipe_slots_executed(ops, rates)
     achieved = photon_steps_per_s * slots
-    return {"ops_per_photon_step": ops, "measured_ops_per_s": rates,
-            "slot_cost": {k: rates["addmul"] / rates[k] for k in ("div", "fmod", "sqrt")},
+    return {"ops_per_photon_step": {**ops, "div_by_launch_constant": roofline.DIV_CONST_PER_RK4_STEP_FLRW},
+            "measured_ops_per_s": rates,
+            "slot_cost": {**{k: rates["addmul"] / rates[k] for k in ("div", "fmod", "sqrt")},
+                          "div_by_launch_constant": roofline.CONST_DIV_SLOTS},
             "slots_per_photon_step": slots, "achieved_slots_per_s": achieved,
             "peak_slots_per_s": rates["addmul"], "frac": achieved / rates["addmul"],
+            "frac_if_every_division_were_ieee": photon_steps_per_s * slots_ieee / rates["addmul"],
+            "note": "the parity build takes its divisions by launch constants as correctly rounded FMA "
+                    "quotients from host reciprocals (1 multiply + 2 FMA, bit-identical to IEEE division, "
+                    "checked by exc_probe_div_rn); frac counts them at 3 slots",
             "source": "exc_probe_fp64_rates (multiply/add, IEEE division, sqrt, fmod throughput, --fmad=false)"}
 
 

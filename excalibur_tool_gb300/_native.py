@@ -149,6 +149,7 @@ EXPORTS = {
                                C.POINTER(ExcLaunchPlan), C.c_void_p]),
     "exc_probe_scratch_len": (C.c_int64, []),
     "exc_probe_fp64_rates": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(C.c_double), C.c_void_p]),
+    "exc_probe_div_rn": (C.c_int, [C.c_void_p, C.c_int32, C.c_int64, C.c_uint64, C.c_void_p, C.c_void_p]),
     # surrogate kernels (include/excalibur_mlp.h)
     "exc_gemm_bf16": (C.c_int, [C.POINTER(ExcGemm), _V]),
     "exc_mlp_features": (C.c_int, [_V, C.c_int64, C.c_int64, C.c_int32, C.POINTER(C.c_double),

@@ -3,11 +3,12 @@
 // Every function restates one reference routine in the reference's own
 // operation order (C and Python share left-to-right associativity for
 // + - * /), so the translation unit compiled without FMA contraction
-// (EXC_FAST == 0) reproduces the reference's IEEE double arithmetic. The unit
-// compiled with contraction (EXC_FAST == 1) also replaces divisions by launch
-// constants (c^2, c^4, grid spacings, table step, 1/a) with multiplications by
-// reciprocals: GB300's FP64 pipe is narrow and each IEEE division costs about
-// ten FP64 pipe slots.
+// (EXC_FAST == 0) reproduces the reference's IEEE double arithmetic; its divisions by
+// launch constants (c^2, c^4, grid spacings, table step) take the correctly rounded
+// quotient from a host reciprocal (div_rn), identical to the IEEE division at a third of
+// its FP64 pipe cost. The unit compiled with contraction (EXC_FAST == 1) replaces those
+// divisions, and 1/a, with plain multiplications by reciprocals: GB300's FP64 pipe is
+// narrow and each IEEE division costs about eight FP64 pipe slots.
 //
 // Reference quirks kept on purpose (parity):
 //  * gradient = central difference at the base node, piecewise constant per
@@ -21,6 +22,7 @@
 #include <cstdint>
 #include <cmath>
 #include "exc_devmetric.h"
+#include "exc_divrn.cuh"
 
 #ifndef EXC_FAST
 #error "EXC_FAST must be defined (0 = exact reference order, 1 = fast)"
@@ -88,14 +90,14 @@ struct InterpOut {
   double val, gx, gy, gz, dtd;
 };
 
-// x / c on the parity path; x * (1/c) on the fast path.
+// x / c by a launch constant: the correctly rounded quotient on the parity path (div_rn,
+// bit-identical to an IEEE division), x * (1/c) on the fast path.
 __device__ __forceinline__ double div_c(double x, double c, double inv_c) {
 #if EXC_FAST
   (void)c;
   return x * inv_c;
 #else
-  (void)inv_c;
-  return x / c;
+  return ::div_rn(x, c, inv_c);
 #endif
 }
 
@@ -121,8 +123,8 @@ __device__ __forceinline__ bool has_shift(const ExcField& f) {
 
 // One spatial snapshot `it` (of nt, innermost index) of a 3-D/4-D field.
 // Returns an EXC_PH_* failure code, or 0 with `o` filled (o.dtd = 0).
-// The cell coordinate rel = (x - origin) / spacing is an IEEE division in
-// every build: the base-node gradient is discontinuous across cell faces, and
+// The cell coordinate rel = (x - origin) / spacing is the correctly rounded quotient in
+// every build (div_rn): the base-node gradient is discontinuous across cell faces, and
 // positions that sit exactly on a node plane (an observer placed on a grid
 // node, as the reference runner does) must select the reference's cell.
 template <class FT>
@@ -139,7 +141,7 @@ __device__ __forceinline__ int interp_snapshot(const ExcField& f, const double* 
     x = ox + py_fmod(x - ox, Lx);
     y = oy + py_fmod(y - oy, Ly);
     z = oz + py_fmod(z - oz, Lz);
-    const double rx = (x - ox) / sx, ry = (y - oy) / sy, rz = (z - oz) / sz;
+    const double rx = div_rn(x - ox, sx, fi[0]), ry = div_rn(y - oy, sy, fi[1]), rz = div_rn(z - oz, sz, fi[2]);
     if (!isfinite(rx) || !isfinite(ry) || !isfinite(rz)) return EXC_PH_NONFINITE;
     int64_t i0 = (int64_t)floor(rx), j0 = (int64_t)floor(ry), k0 = (int64_t)floor(rz);
     const double dx = rx - (double)i0, dy = ry - (double)j0, dz = rz - (double)k0;
@@ -166,7 +168,7 @@ __device__ __forceinline__ int interp_snapshot(const ExcField& f, const double* 
     if (x < ox) x = ox; else if (x > hx) x = hx;
     if (y < oy) y = oy; else if (y > hy) y = hy;
     if (z < oz) z = oz; else if (z > hz) z = hz;
-    const double rx = (x - ox) / sx, ry = (y - oy) / sy, rz = (z - oz) / sz;
+    const double rx = div_rn(x - ox, sx, fi[0]), ry = div_rn(y - oy, sy, fi[1]), rz = div_rn(z - oz, sz, fi[2]);
     if (!isfinite(rx) || !isfinite(ry) || !isfinite(rz)) return EXC_PH_NONFINITE;
     int64_t i0 = (int64_t)floor(rx), j0 = (int64_t)floor(ry), k0 = (int64_t)floor(rz);
     if (i0 < 0) i0 = 0;
@@ -191,7 +193,7 @@ __device__ __forceinline__ int interp_snapshot(const ExcField& f, const double* 
   // EXC_BOUNDARY_ERROR: fused_interpolation_gradient_3d_error,
   // interpolator_4d_fast.py:50-91 (same arithmetic as the legacy strict
   // interpolator, grid/interpolator_fast.py:119-192)
-  const double rx = (x - ox) / sx, ry = (y - oy) / sy, rz = (z - oz) / sz;
+  const double rx = div_rn(x - ox, sx, fi[0]), ry = div_rn(y - oy, sy, fi[1]), rz = div_rn(z - oz, sz, fi[2]);
   if (rx < 1.0 || rx >= (double)nx - 2.0 || ry < 1.0 || ry >= (double)ny - 2.0 ||
       rz < 1.0 || rz >= (double)nz - 2.0)
     return EXC_PH_OUTSIDE_GRID;
@@ -314,9 +316,9 @@ __device__ __forceinline__ int interp_slow(const ExcField& f, const double* fi, 
                                            double x, double y, double z, double t, InterpOut& o) {
   const int64_t nx = f.n[0], ny = f.n[1], nz = f.n[2];
   // _index_and_weights (:13-44): bounds rel in [0, n-1), no clipping needed after it
-  const double rx = (x - f.origin[0]) / f.spacing[0];
-  const double ry = (y - f.origin[1]) / f.spacing[1];
-  const double rz = (z - f.origin[2]) / f.spacing[2];
+  const double rx = div_rn(x - f.origin[0], f.spacing[0], fi[0]);
+  const double ry = div_rn(y - f.origin[1], f.spacing[1], fi[1]);
+  const double rz = div_rn(z - f.origin[2], f.spacing[2], fi[2]);
   if (rx < 0.0 || rx >= (double)(nx - 1) || ry < 0.0 || ry >= (double)(ny - 1) || rz < 0.0 ||
       rz >= (double)(nz - 1))
     return EXC_PH_OUTSIDE_GRID;
@@ -338,7 +340,7 @@ __device__ __forceinline__ int interp_slow(const ExcField& f, const double* fi, 
   }
   const int64_t nt = f.n[3];
 #define EXC_IDX(i, j, k, l) ((((int64_t)(i) * ny + (j)) * nz + (k)) * nt + (l))
-  const double rt = (t - f.origin[3]) / f.spacing[3];
+  const double rt = div_rn(t - f.origin[3], f.spacing[3], fi[3]);
   if (!isfinite(rt)) return EXC_PH_NONFINITE;
   const double flt = floor(rt);
   const double wt = rt - flt;
@@ -410,9 +412,9 @@ __device__ __forceinline__ int interp_field(const ExcField& f, const double* fi,
     const double et = 1e-12 * stp;
     const double ht = ot + (double)(nt - 1) * stp - et;
     if (t < ot) t = ot; else if (t > ht) t = ht;
-    rt = (t - ot) / stp;
+    rt = div_rn(t - ot, stp, fi[3]);
   } else {
-    rt = (t - ot) / stp;
+    rt = div_rn(t - ot, stp, fi[3]);
     if (rt < 0.0 || rt >= (double)nt - 1.0) return EXC_PH_OUTSIDE_GRID;
   }
   if (!isfinite(rt)) return EXC_PH_NONFINITE;

@@ -7,6 +7,7 @@
 #include <cstdint>
 
 #include "excalibur_gb300.h"
+#include "exc_divrn.cuh"
 
 namespace exc {
 void set_last_error(const char* msg);
@@ -73,9 +74,60 @@ cudaError_t time_op(double* out, int64_t n, double b, double y, cudaStream_t s, 
   return err;
 }
 
+__device__ __forceinline__ uint64_t mix64(uint64_t x) {
+  x += 0x9E3779B97F4A7C15ull;
+  x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+  x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+  return x ^ (x >> 31);
+}
+
+// div_rn(x, c, RN(1/c)) against the IEEE quotient x / c, bit for bit. Even samples: x with a
+// random sign and significand and an exponent in 2^-200 .. 2^200. Odd samples: x = RN(c m)
+// for m = y + ulp(y)/2 a rounding midpoint (one FMA), so that x / c falls next to a midpoint
+// -- the quotients hardest to round.
+__global__ void div_probe_kernel(const double* divs, int nd, int64_t n, uint64_t seed, unsigned long long* bad) {
+  unsigned long long local = 0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double c = divs[i % nd];
+    const double rc = 1.0 / c;
+    const uint64_t h = mix64(seed ^ (uint64_t)i), h2 = mix64(h);
+    const uint64_t expo = 823 + (h2 % 401);                     // biased exponent: 2^-200 .. 2^200
+    double x = __longlong_as_double((long long)((h & 0x800FFFFFFFFFFFFFull) | (expo << 52)));
+    if (i & 1) {
+      const double y = fabs(x);
+      const double half_ulp = __longlong_as_double((long long)((expo - 53) << 52));   // ulp(y) / 2
+      x = fma(c, y, c * half_ulp);
+    }
+    const double a = x / c, b = div_rn(x, c, rc);
+    if (__double_as_longlong(a) != __double_as_longlong(b)) ++local;
+  }
+  if (local) atomicAdd(bad, local);
+}
+
 }  // namespace
 
 extern "C" {
+
+int exc_probe_div_rn(const double* divisors, int32_t n_div, int64_t n_samples, uint64_t seed,
+                     unsigned long long* mismatches, void* stream) {
+  if (!divisors || !mismatches || n_div < 1 || n_samples < 1) {
+    exc::set_last_error("exc_probe_div_rn: divisors, mismatches, n_div >= 1 and n_samples >= 1 required");
+    return EXC_ERR_INVALID;
+  }
+  const int n = sm_count();
+  if (n < 0) { exc::set_last_error("no CUDA device"); return EXC_ERR_NO_DEVICE; }
+  cudaStream_t s = (cudaStream_t)stream;
+  cudaError_t err = cudaMemsetAsync(mismatches, 0, sizeof(unsigned long long), s);
+  if (err == cudaSuccess) {
+    div_probe_kernel<<<n * 8, 256, 0, s>>>(divisors, n_div, n_samples, seed, mismatches);
+    err = cudaGetLastError();
+  }
+  if (err != cudaSuccess) {
+    exc::set_last_error(cudaGetErrorString(err));
+    return EXC_ERR_CUDA;
+  }
+  return EXC_SUCCESS;
+}
 
 int64_t exc_probe_scratch_len(void) {
   const int n = sm_count();

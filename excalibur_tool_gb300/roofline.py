@@ -13,6 +13,11 @@ SQRT_PER_RK4_STEP_FLRW = 4
 # the same, by kind (a division or fmod costs several multiply/add slots of the FP64
 # pipe; exc_probe_fp64_rates measures how many)
 OPS_PER_RK4_STEP_FLRW = {"add": 228, "sub": 128, "mul": 492, "div": 149, "fmod": 12, "sqrt": 4}
+# of those divisions, the ones by a launch constant (c^2, c^4, grid spacings, the a(eta) table
+# step): the parity build takes them as correctly rounded FMA quotients from host reciprocals
+# (one multiply and two FMAs, bit-identical to the IEEE division)
+DIV_CONST_PER_RK4_STEP_FLRW = 129
+CONST_DIV_SLOTS = 3
 
 
 def fp64_pipe_slots(ops: dict, rates: dict) -> float:
@@ -21,6 +26,14 @@ def fp64_pipe_slots(ops: dict, rates: dict) -> float:
     base = rates["addmul"]
     return (ops["add"] + ops["sub"] + ops["mul"] + ops["div"] * base / rates["div"] +
             ops["fmod"] * base / rates["fmod"] + ops["sqrt"] * base / rates["sqrt"])
+
+
+def fp64_pipe_slots_executed(ops: dict, rates: dict, div_const: int = DIV_CONST_PER_RK4_STEP_FLRW) -> float:
+    """fp64_pipe_slots with the divisions by launch constants at CONST_DIV_SLOTS slots each
+    (how the parity build executes them) instead of an IEEE division's measured cost."""
+    return fp64_pipe_slots(ops, rates) - div_const * (rates["addmul"] / rates["div"] - CONST_DIV_SLOTS)
+
+
 # bytes gathered per RK4 photon-step: 4 RHS x (11 distinct grid nodes + 2 a(eta) table entries)
 NODES_PER_RHS = 11
 TABLE_ENTRIES_PER_RHS = 2

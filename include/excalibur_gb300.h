@@ -367,6 +367,14 @@ enum { EXC_PROBE_ADDMUL = 0, EXC_PROBE_DIV = 1, EXC_PROBE_SQRT = 2, EXC_PROBE_FM
 int64_t exc_probe_scratch_len(void);
 int exc_probe_fp64_rates(double* scratch, int64_t n_scratch, double* rates_out, void* stream);
 
+/* Check of the parity build's division by launch constants (no reference counterpart): the
+ * quotient x * RN(1/c) with Markstein's FMA correction against the IEEE quotient x / c, bit for
+ * bit, over n_samples x (random signs and significands over 2^-200 .. 2^200, and every second
+ * one placed next to a rounding midpoint of x / c) for the divisors[k] (device, n_div of them,
+ * taken in turn). *mismatches (device) is zeroed, then counts the quotients that differ. */
+int exc_probe_div_rn(const double* divisors, int32_t n_div, int64_t n_samples, uint64_t seed,
+                     unsigned long long* mismatches, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

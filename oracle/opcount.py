@@ -42,7 +42,10 @@ class F:
     def __rsub__(self, o): return self._op("sub", self._v(o) - self.v)
     def __mul__(self, o): return self._op("mul", self.v * self._v(o))
     def __rmul__(self, o): return self._op("mul", self._v(o) * self.v)
-    def __truediv__(self, o): return self._op("div", self.v / self._v(o))
+    def __truediv__(self, o):
+        if not isinstance(o, F) or isinstance(o, Const):
+            COUNTS["div_const"] += 1      # divisor fixed for the launch (c^2, c^4, spacing, table step)
+        return self._op("div", self.v / self._v(o))
     def __rtruediv__(self, o): return self._op("div", self._v(o) / self.v)
     def __mod__(self, o): return self._op("fmod", math.fmod(self.v, self._v(o)) % self._v(o))
     def __neg__(self): return F(-self.v)
@@ -57,6 +60,24 @@ class F:
     def __gt__(self, o): return self.v > self._v(o)
     def __ge__(self, o): return self.v >= self._v(o)
     def __float__(self): return self.v
+
+
+class Const(F):
+    """A launch constant (grid spacing, table step): a division by it, or by a plain Python
+    number such as c**2, is counted as a division by a constant as well. Products and sums of
+    constants stay constants (2.0 * spacing)."""
+    __slots__ = ()
+
+    def _op(self, kind, val):
+        COUNTS[kind] += 1
+        return F(val)
+
+    def __mul__(self, o):
+        COUNTS["mul"] += 1
+        v = self.v * self._v(o)
+        return Const(v) if not isinstance(o, F) or isinstance(o, Const) else F(v)
+
+    __rmul__ = __mul__
 
 
 def fsqrt(x):
@@ -131,11 +152,11 @@ def count_rk4_flrw_step():
         return field[i % n, j % n, k % n]
 
     tab = [F(v) for v in np.linspace(0.1, 2.0, 5000)]
-    s = [F(2.5e22)] * 3
+    s = [Const(2.5e22)] * 3
     o = [F(0.0)] * 3
     state = [F(1.4e18), F(1.0e23), F(2.0e23), F(3.0e23), F(-1.0), F(2e8), F(1e8), F(1.5e8)]
     dt = F(5e13)
-    args = (fg, o, s, n, tab, F(0.0), F(3.5e14), F(2.27e-18), 0.3, 0.0, 0.0, 0.7, 299792458)
+    args = (fg, o, s, n, tab, F(0.0), Const(3.5e14), F(2.27e-18), 0.3, 0.0, 0.0, 0.7, 299792458)
     k1 = rhs(state, *args)
     k2 = rhs([state[i] + 0.5 * dt * k1[i] for i in range(8)], *args)
     k3 = rhs([state[i] + 0.5 * dt * k2[i] for i in range(8)], *args)
@@ -143,7 +164,7 @@ def count_rk4_flrw_step():
     d6 = dt / 6
     _ = [state[i] + d6 * (k1[i] + 2 * k2[i] + 2 * k3[i] + k4[i]) for i in range(8)]
     counts = dict(COUNTS)
-    flops = sum(v for k, v in counts.items() if k != "sqrt")
+    flops = sum(v for k, v in counts.items() if k not in ("sqrt", "div_const"))
     return flops, counts.get("sqrt", 0), counts
 
 

@@ -336,3 +336,31 @@ def test_abort_flag_and_deadline(cuda):
     r = trace_batch(m, s, cfg)
     torch.cuda.synchronize()
     assert (r.status.cpu().numpy() == N.PH_LEFT_BOX).all()
+
+
+def test_division_by_launch_constants_is_ieee(cuda):
+    """The parity build divides by launch constants (c^2, c^4, grid spacings and their
+    doubles, the a(eta) table step) with x * RN(1/c) and Markstein's FMA correction; over
+    2^32 quotients per run -- random operands over 2^-200 .. 2^200 and operands placed next to
+    rounding midpoints -- it must equal the IEEE quotient bit for bit."""
+    import ctypes as C
+
+    import torch
+    from excalibur_tool_gb300 import _native as N
+    from excalibur_tool_gb300.core import constants as K
+
+    cz = golden("cosmology.npz")
+    divs = [K.C2_F64, K.C4_F64, float(cz["eta_step"])]
+    for n in (32, 64, 96, 128, 256, 512):
+        h = 1000 * K.one_Mpc / n
+        divs += [h, 2.0 * h]
+    rng = np.random.default_rng(8)
+    divs += list(rng.uniform(1.0, 2.0, 16) * 2.0 ** rng.integers(-60, 90, 16))
+    d = torch.as_tensor(np.array(divs), device=cuda)
+    bad = torch.zeros(1, dtype=torch.int64, device=cuda)
+    L = N.load()
+    for seed in (1, 2):
+        N.check(L.exc_probe_div_rn(N.ptr(d), len(divs), 1 << 32, seed, N.ptr(bad), N.stream_handle(cuda)),
+                "exc_probe_div_rn")
+        torch.cuda.synchronize()
+        assert int(bad.item()) == 0
