@@ -516,8 +516,11 @@ __device__ __forceinline__ void flrw_accel_tensorial(const DevMetric& D, double 
   const double adot_a = adot * inv_a;
   const double ia2 = inv_a * inv_a;
 #else
+  // a and a^2 divide several terms: one IEEE reciprocal each, then correctly rounded
+  // quotients from it (div_rn), identical to the reference's divisions
   (void)inv_a;
-  const double adot_a = adot / a;
+  const double ra = 1.0 / a, ra2 = 1.0 / a2;
+  const double adot_a = ::div_rn(adot, a, ra);
 #endif
   const double usq = u1 * u1 + u2 * u2 + u3 * u3;
   const double psi = phi;
@@ -534,9 +537,9 @@ __device__ __forceinline__ void flrw_accel_tensorial(const DevMetric& D, double 
   const double G200 = gy * ia2 * u0 * u0;
   const double G300 = gz * ia2 * u0 * u0;
 #else
-  const double G100 = gx / a2 * u0 * u0;
-  const double G200 = gy / a2 * u0 * u0;
-  const double G300 = gz / a2 * u0 * u0;
+  const double G100 = ::div_rn(gx, a2, ra2) * u0 * u0;
+  const double G200 = ::div_rn(gy, a2, ra2) * u0 * u0;
+  const double G300 = ::div_rn(gz, a2, ra2) * u0 * u0;
 #endif
   const double G1ii = -gxc * u1 * u1 + gxc * (u2 * u2 + u3 * u3) + (-gyc) * u1 * u2 + (-gzc) * u1 * u3;
   du[1] = -(G100 + hub * u0 * u1 + G1ii);
@@ -560,8 +563,9 @@ __device__ __forceinline__ void flrw_accel_analytical(const DevMetric& D, double
   const double aa2 = 2.0 * adot * inv_a;
 #else
   (void)inv_a;
-  const double aa = adot / a;
-  const double aa2 = 2.0 * adot / a;
+  const double ra = 1.0 / a;
+  const double aa = ::div_rn(adot, a, ra);
+  const double aa2 = ::div_rn(2.0 * adot, a, ra);
 #endif
   const double pdc2 = div_c(phi_dot, c2, ic2);
   du[0] = -(aa + pdc2) * (u0 * u0) - tc2 * u0 * dphidl -

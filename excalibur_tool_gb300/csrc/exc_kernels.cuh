@@ -142,7 +142,7 @@ struct Tracer {
     for (int i = 0; i < 8; ++i) { acc[i] = acc[i] + 2.0 * k[i]; tmp[i] = s[i] + dt * k[i]; }
     st = rhs(tmp, k);
     if (st) return st;
-    const double d6 = dt / 6.0;
+    const double d6 = ::div_rn(dt, 6.0, 1.0 / 6.0);   // dt / 6, correctly rounded (1/6 folded at compile time)
 #pragma unroll
     for (int i = 0; i < 8; ++i) out[i] = s[i] + d6 * (acc[i] + k[i]);
     return 0;
