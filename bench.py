@@ -74,7 +74,7 @@ def parse():
                    help="only run the 32-row comparison sweep of the sweep leg once and exit")
     p.add_argument("--map-side", type=int, default=4096)
     p.add_argument("--train-steps", type=int, default=8000)
-    p.add_argument("--smooth-train-steps", type=int, default=16000,
+    p.add_argument("--smooth-train-steps", type=int, default=12000,
                    help="training steps of the surrogate on the slow-Interpolator field")
     return p.parse_args()
 
@@ -808,7 +808,7 @@ def run_surrogate_smooth(args, dev):
            "fp64_parity_status_counts": np.bincount(r.status.cpu().numpy(), minlength=12).tolist(),
            "mixed_on_sample": {"rays_per_s": mixed_rays_s, "speedup_vs_fp64": mixed_rays_s / fp64_rays_s,
                                "retrace_fraction": retrace, **errors_vs(r, rm)}}
-    out.update(_surrogate_map(args, metric, patch, cfg, fp64_rays_s, args.smooth_train_steps, lr=3e-3))
+    out.update(_surrogate_map(args, metric, patch, cfg, fp64_rays_s, args.smooth_train_steps, lr=3.5e-3))
     return out
 
 
