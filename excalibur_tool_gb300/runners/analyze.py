@@ -128,18 +128,19 @@ def trajectory_stats(trajs, lens_center=None, *, is_spherical: bool) -> Trajecto
             path = np.full(n_ph, np.nan)
         rr = _row_norm(xyz_path)
         rr = np.where(np.isfinite(rr), rr, np.nan)
-        import warnings
-
-        with warnings.catch_warnings():
-            warnings.simplefilter("ignore", RuntimeWarning)
-            min_r = np.nanmin(rr, axis=1) if n_rec else np.full(n_ph, np.nan)
-            final_r = rr[:, -1] if n_rec else np.full(n_ph, np.nan)
-            vmag = _row_norm(v)
-            detadl = u[..., 0]
-            denom = np.where(np.abs(detadl) > 0, np.abs(detadl), np.nan)
-            speed = vmag / denom
-            speed_mean = np.nanmean(speed, axis=1)
-            speed_max = np.nanmax(speed, axis=1)
+        # numpy's nanmin / nanmax / nanmean, computed as numpy computes them (fmin/fmax
+        # reductions; sum of the non-NaN values over their count) but without the warnings
+        # those emit for all-NaN rows: the warnings filters are process-wide, and rows are
+        # reduced on several threads at once
+        min_r = np.fmin.reduce(rr, axis=1) if n_rec else np.full(n_ph, np.nan)
+        final_r = rr[:, -1] if n_rec else np.full(n_ph, np.nan)
+        vmag = _row_norm(v)
+        detadl = u[..., 0]
+        denom = np.where(np.abs(detadl) > 0, np.abs(detadl), np.nan)
+        speed = vmag / denom
+        nan = np.isnan(speed)
+        speed_mean = np.where(nan, 0.0, speed).sum(axis=1) / (~nan).sum(axis=1)
+        speed_max = np.fmax.reduce(speed, axis=1) if n_rec else np.full(n_ph, np.nan)
     bend = _bend(v)
     return TrajectoryStats(n_records=np.full(n_ph, n_rec, dtype=np.int64), finite_fraction=finite_fraction,
                            path_length=path, min_r=min_r, final_r=final_r, bending_angle_rad=bend,
