@@ -69,7 +69,9 @@ def test_stats_edge_cases():
     assert np.all(np.isnan(one.path_length))
 
 
-def _oracle_leg(cfg, geo, states, kind, phi=None):
+def _oracle_leg(cfg, geo, states, kind, phi=None, dt_bounds=None):
+    """The oracle's records [n, n_rec, 12] and statuses of one runner leg; `dt_bounds` =
+    (dt_min, dt_max) of the leg (default both |dlambda|, the fixed-step integrators' bounds)."""
     from excalibur_tool_gb300.trace import TraceConfig
     from oracle import oracle as O
     from oracle.oracle import FieldSpec, Spacetime
@@ -85,7 +87,8 @@ def _oracle_leg(cfg, geo, states, kind, phi=None):
                        fields=[FieldSpec(phi, (d, d, d), (0.0, 0.0, 0.0), "periodic",
                                          shift=tuple(shift) if shift is not None else (0.0, 0.0, 0.0))])
     dl = geo.dlambda
-    tc = TraceConfig(stepper=cfg.integrator, dt=dl, dt_min=abs(dl), dt_max=abs(dl), max_steps=geo.n_steps,
+    dt_min, dt_max = dt_bounds if dt_bounds is not None else (abs(dl), abs(dl))
+    tc = TraceConfig(stepper=cfg.integrator, dt=dl, dt_min=dt_min, dt_max=dt_max, max_steps=geo.n_steps,
                      record_every=cfg.record_every, observables=False)
     r = O.trace(st, states, tc, threads=4)
     tr = r.records[:, : int(r.n_records.max())].copy()

@@ -8,6 +8,7 @@ import pytest
 from conftest import golden
 from helpers import rel_err
 from test_compare_runner import _oracle_leg, job1_config
+from excalibur_tool_gb300 import _native as N
 from excalibur_tool_gb300.runners import compare as R
 
 pytestmark = pytest.mark.gpu
@@ -201,3 +202,47 @@ def test_impact_runner_matches_oracle(cuda):
     # the state columns of the first record are finite (its quantity columns lag one record)
     for i in np.flatnonzero(~ok):
         assert np.isfinite(gs[i, 0, :8]).all()
+
+
+def test_rk45_row_matches_oracle(cuda):
+    """A manifest row run with the runner's RK45 (rtol 1e-9, atol 1e-13; the Schwarzschild step
+    free in [|dl| / 1e6, |dl|], the FLRW step pinned to |dl|) against the oracle fed the same
+    states and bounds. On this row the reference's controller accepts no trial step, down to the
+    floor: every photon of both legs stops at the 10,000-iteration cap with its initial state,
+    here and in the oracle alike. Statuses and accepted steps agree; records to a few ulps on
+    the FLRW leg and to 1e-6 (1e-10 on most photons) on the Schwarzschild one, the tolerances
+    a run that does take steps needs (one RK45 step differs from the oracle's by <= 4.5e-16; a
+    free step control can turn a sin/cos ulp into another step sequence)."""
+    import dataclasses
+    import os
+
+    from conftest import GOLDEN
+    from excalibur_tool_gb300.runners import sweep as S
+
+    job = dataclasses.replace(S.read_jobs(os.path.join(GOLDEN, "manifest_cone.csv"))[0], integrator="rk45")
+    got = S.run_jobs([job])[job.jobid]
+    cfg = S.job_config(job)
+    geo = R.geometry(cfg)
+    _, fs, _ = R.flrw_setup(cfg, geo)
+    _, ss, dmin, dmax = R.schwarzschild_setup(cfg, geo)
+    assert dmin == abs(geo.dlambda) / 1e6 and dmax == abs(geo.dlambda)
+    of, fst = _oracle_leg(cfg, geo, fs.cpu().numpy(), "flrw", R.flrw_potential(cfg, geo))
+    assert np.array_equal(got.flrw.status, fst)
+    gf = got.flrw.trajectories
+    assert gf.shape == of.shape and np.array_equal(np.isnan(gf), np.isnan(of))
+    assert _scaled_err(gf, of) <= 1e-13
+    os_, sst = _oracle_leg(cfg, geo, ss.cpu().numpy(), "schwarzschild", dt_bounds=(dmin, dmax))
+    assert np.array_equal(got.schwarzschild.status, sst)
+    for leg in (got.flrw, got.schwarzschild):
+        assert np.all(leg.status == N.PH_MAX_ITER) and np.all(leg.n_steps == 0)
+    failed = np.isin(sst, (N.PH_HORIZON, N.PH_NONFINITE, N.PH_OUTSIDE_GRID))
+    if failed.all():
+        assert got.error.startswith("every photon of the Schwarzschild leg")
+        return
+    ok = np.flatnonzero(~failed)
+    gs = got.schwarzschild.trajectories
+    n = min(gs.shape[1], os_.shape[1])
+    scale = np.nanmax(np.abs(os_[ok][:, :n]), axis=(0, 1))
+    scale = np.where(scale > 0, scale, 1.0)
+    per_photon = np.array([np.nanmax(np.abs(gs[i, :n] - os_[i, :n]) / scale) for i in ok])
+    assert per_photon.max() <= 1e-6 and (per_photon <= 1e-10).mean() >= 0.9
