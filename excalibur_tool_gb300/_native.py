@@ -33,6 +33,9 @@ COSMO_STATIC, COSMO_TABLE, COSMO_TABLE_FD = 0, 1, 2
 BOUNDARY = {"periodic": 0, "clamp": 1, "error": 2}
 GRAD = {"base_node": 0, "trilinear": 1}
 PROBE = {"addmul": 0, "div": 1, "sqrt": 2, "fmod": 3}
+# exc_record_redshift output columns (EXC_RS_*)
+RS_COLUMNS = ("z_H", "z_SW", "z_ISW", "z_D", "z_total", "z_total_exact", "Phi_obs", "Phi_em", "a_obs", "a_em",
+              "eta_obs", "eta_em", "x_obs0", "x_obs1", "x_obs2", "x_em0", "x_em1", "x_em2", "n_rows")
 DTYPE_F64, DTYPE_F32, DTYPE_F32X2 = 0, 1, 2
 STEPPER = {"rk4": 0, "rk45": 1, "leapfrog4": 2}
 TABLEAU = {"reference": 0, "fehlberg": 1}
@@ -150,6 +153,13 @@ EXPORTS = {
     "exc_probe_scratch_len": (C.c_int64, []),
     "exc_probe_fp64_rates": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(C.c_double), C.c_void_p]),
     "exc_probe_div_rn": (C.c_int, [C.c_void_p, C.c_int32, C.c_int64, C.c_uint64, C.c_void_p, C.c_void_p]),
+    # redshift maps from recorded trajectories
+    "exc_record_redshift": (C.c_int, [_V, C.c_int64, C.c_int32, C.c_int32, C.c_double, _V, _V, _V, _V, _V]),
+    "exc_sky_directions": (C.c_int, [_V, C.c_int64, C.c_int32, C.c_int32, _V, _V]),
+    "exc_sky_project": (C.c_int, [_V, C.c_int64, C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                  C.POINTER(C.c_double), _V, _V, _V]),
+    "exc_sky_bin": (C.c_int, [_V, _V, _V, C.c_int64, C.c_int32, C.c_int32, C.POINTER(C.c_double), _V, _V, _V,
+                              _V]),
     # surrogate kernels (include/excalibur_mlp.h)
     "exc_gemm_bf16": (C.c_int, [C.POINTER(ExcGemm), _V]),
     "exc_mlp_features": (C.c_int, [_V, C.c_int64, C.c_int64, C.c_int32, C.POINTER(C.c_double),

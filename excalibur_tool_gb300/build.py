@@ -34,6 +34,7 @@ UNITS = {
     "exc_gen.cu": ["--fmad=false"],
     "exc_born.cu": [],
     "exc_probe.cu": ["--fmad=false"],
+    "exc_maps.cu": ["--fmad=false"],
 }
 
 

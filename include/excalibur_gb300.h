@@ -375,6 +375,55 @@ int exc_probe_fp64_rates(double* scratch, int64_t n_scratch, double* rates_out, 
 int exc_probe_div_rn(const double* divisors, int32_t n_div, int64_t n_samples, uint64_t seed,
                      unsigned long long* mismatches, void* stream);
 
+/* ---- redshift maps from recorded trajectories ---------------------------
+ * Replace the host loop of _postprocessing/compute_redshift_map.py:98-171
+ * (compute_redshift_map: per photon, the rows holding a NaN dropped as
+ * load_trajectories does at :47-48, then RedshiftCalculator(...)
+ * .compute_all_components(), excalibur/observables/redshift.py:340-399) and
+ * extract_sky_positions (:54-95); the maps are pixel means (exc_sky_bin) in place
+ * of create_2d_map's scipy griddata (_postprocessing/compute_time_delay_map.py:313-357).
+ * records: [n_photons][n_rows][n_cols] float64, device, NaN-padded (the runners'
+ * trajectory-file layout; FLRW rows [eta, x, y, z, u0..u3, a, Phi, dPhi/dx,
+ * dPhi/dy, dPhi/dz, dPhi/deta], n_cols >= 14). */
+enum {
+  EXC_RS_Z_H = 0,
+  EXC_RS_Z_SW = 1,
+  EXC_RS_Z_ISW = 2,          /* -simpson(Phi_dot c^2, eta) / c^2, scipy's irregular-spacing rule */
+  EXC_RS_Z_D = 3,            /* Doppler; 0 without endpoint velocities */
+  EXC_RS_Z_TOTAL = 4,
+  EXC_RS_Z_TOTAL_EXACT = 5,
+  EXC_RS_PHI_OBS = 6,        /* columns 6..17: NaN for a photon without clean rows */
+  EXC_RS_PHI_EM = 7,
+  EXC_RS_A_OBS = 8,
+  EXC_RS_A_EM = 9,
+  EXC_RS_ETA_OBS = 10,
+  EXC_RS_ETA_EM = 11,
+  EXC_RS_X_OBS = 12,         /* 3 columns */
+  EXC_RS_X_EM = 15,          /* 3 columns */
+  EXC_RS_N_ROWS = 18,        /* clean rows; components stay 0 below 2, as in compute_redshift_map */
+  EXC_RS_NCOLS = 19
+};
+/* out: [n_photons][EXC_RS_NCOLS] float64, device. scratch: n_photons * n_rows int32,
+ * device. v_obs, v_em: [n_photons][3] float64 peculiar velocities at the first and
+ * last clean row (the reference's velocity_func evaluated there), or both NULL. */
+int exc_record_redshift(const double* records, int64_t n_photons, int32_t n_rows, int32_t n_cols, double c,
+                        const double* v_obs, const double* v_em, int32_t* scratch, double* out, void* stream);
+/* dirs: [n_photons][3], the unit spatial velocity (columns 5..7) of each photon's first clean
+ * row; NaN for a photon without one. */
+int exc_sky_directions(const double* records, int64_t n_photons, int32_t n_rows, int32_t n_cols, double* dirs,
+                       void* stream);
+/* x_proj, y_proj: [n] tangent-plane coordinates of dirs about mean_dir with the in-plane basis
+ * (basis_x, basis_y): the angle from mean_dir along the in-plane unit vector, 0 within 1e-10
+ * rad of it, NaN for a NaN direction. The three host vectors are passed by value. */
+int exc_sky_project(const double* dirs, int64_t n, const double mean_dir[3], const double basis_x[3],
+                    const double basis_y[3], double* x_proj, double* y_proj, void* stream);
+/* Pixel means of scattered samples over extent = {x0, x1, y0, y1} (host): pixel
+ * (iy, ix) with ix = min(floor((x - x0) / (x1 - x0) * nx), nx - 1), iy likewise; samples
+ * outside the extent or with a non-finite x, y or value are skipped. sum [ny][nx] float64 and
+ * count [ny][nx] uint64 are zeroed first; mean [ny][nx] = sum / count, NaN where count = 0. */
+int exc_sky_bin(const double* x, const double* y, const double* values, int64_t n, int32_t nx, int32_t ny,
+                const double extent[4], double* sum, unsigned long long* count, double* mean, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -168,3 +168,27 @@ def test_new_entry_points_validate_before_any_launch(lib):
     f.shift[1] = float("nan")
     assert L.exc_trace(C.byref(m), C.byref(_args()), None) == N.EXC_ERR_INVALID
     assert b"shift" in L.exc_last_error()
+
+
+def test_map_entry_points_validate_before_any_launch(lib):
+    """The redshift-map entry points refuse bad shapes and half-given inputs on the host."""
+    L = N.load()
+    P = C.c_void_p(4096)
+    c = 299792458.0
+    # fewer than the 14 FLRW record columns; one velocity array without the other; c <= 0
+    assert L.exc_record_redshift(P, 4, 10, 8, c, None, None, P, P, None) == N.EXC_ERR_INVALID
+    assert b"n_cols >= 14" in L.exc_last_error()
+    assert L.exc_record_redshift(P, 4, 10, 14, c, P, None, P, P, None) == N.EXC_ERR_INVALID
+    assert L.exc_record_redshift(P, 4, 10, 14, 0.0, None, None, P, P, None) == N.EXC_ERR_INVALID
+    assert L.exc_record_redshift(None, 4, 10, 14, c, None, None, P, P, None) == N.EXC_ERR_INVALID
+    assert L.exc_record_redshift(None, 0, 10, 14, c, None, None, None, None, None) == N.EXC_SUCCESS
+    assert L.exc_sky_directions(P, 4, 10, 7, P, None) == N.EXC_ERR_INVALID
+    d3 = (C.c_double * 3)(1.0, 0.0, 0.0)
+    assert L.exc_sky_project(P, -1, d3, d3, d3, P, P, None) == N.EXC_ERR_INVALID
+    assert L.exc_sky_project(None, 4, d3, d3, d3, P, P, None) == N.EXC_ERR_INVALID
+    ext = (C.c_double * 4)(0.0, 1.0, 0.0, 1.0)
+    assert L.exc_sky_bin(P, P, P, 10, 0, 4, ext, P, P, P, None) == N.EXC_ERR_INVALID
+    bad = (C.c_double * 4)(1.0, 0.0, 0.0, 1.0)
+    assert L.exc_sky_bin(P, P, P, 10, 4, 4, bad, P, P, P, None) == N.EXC_ERR_INVALID
+    assert b"x1 > x0" in L.exc_last_error()
+    assert L.exc_sky_bin(None, P, P, 10, 4, 4, ext, P, P, P, None) == N.EXC_ERR_INVALID

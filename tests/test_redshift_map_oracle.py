@@ -1,0 +1,133 @@
+"""The redshift-map oracle (oracle/redshift_map.py) against scipy, numpy and the package's
+RedshiftCalculator (itself the reference's class on a trajectory's rows), bit for bit."""
+import numpy as np
+import pytest
+
+from oracle import redshift_map as O
+from excalibur_tool_gb300.core.constants import c
+from excalibur_tool_gb300.observables.redshift import RedshiftCalculator
+
+
+def _irregular(rng, n, dup=False):
+    x = np.cumsum(rng.uniform(0.1, 2.0, n)) * 1e14 + 4.6e17
+    if dup and n > 3:
+        x[n // 2] = x[n // 2 - 1]          # a zero-length interval (scipy's where= guards)
+    return x
+
+
+def test_np_sum_matches_numpy():
+    rng = np.random.default_rng(1)
+    for n in list(range(0, 140)) + [255, 256, 257, 1000, 1031, 4100]:
+        a = rng.standard_normal(n) * 10.0 ** rng.integers(-6, 6, n)
+        assert O.np_sum(a) == np.sum(a), n
+
+
+def test_simpson_matches_scipy():
+    from scipy.integrate import simpson
+
+    rng = np.random.default_rng(2)
+    for n in list(range(1, 70)) + [128, 129, 257, 258, 301, 1000]:
+        for dup in (False, True):
+            x = _irregular(rng, n, dup)
+            y = rng.standard_normal(n) * 1e-3
+            got, want = O.simpson(y, x), float(simpson(y, x=x))
+            if n % 2 == 1 or n == 2:
+                assert got == want, (n, dup, got, want)
+            else:
+                # the last interval's x**3: numpy's power against a double-double cube
+                scale = float(np.sum(np.abs(y) * np.gradient(x)))
+                assert abs(got - want) <= 4e-16 * scale, (n, dup, got, want)
+
+
+def test_cube_is_correctly_rounded_off_halfway():
+    from fractions import Fraction
+
+    rng = np.random.default_rng(6)
+    x = rng.uniform(1e13, 2e14, 3000)
+    bad = sum(O.cube(float(v)) != float(Fraction(float(v)) ** 3) for v in x)
+    assert bad <= 3
+
+
+def _records(rng, n_photons=40, n_rows=60, lag=True, lengths=None):
+    """NaN-padded FLRW record stacks: ragged lengths (0, 1, 2, 3, ... rows), the first row's
+    quantity columns NaN like the runners' histories (lag=True), a NaN row in the middle."""
+    rec = np.full((n_photons, n_rows, 14), np.nan)
+    for i in range(n_photons):
+        if lengths is not None:
+            m = lengths[i]
+        else:
+            m = i if i < 6 else int(rng.integers(2, n_rows + 1))
+        eta = 4.6e17 - np.cumsum(rng.uniform(0.5, 1.5, m)) * 1e14
+        rec[i, :m, 0] = eta
+        rec[i, :m, 1:4] = rng.uniform(0, 3e24, 3) + np.cumsum(rng.normal(0, 1e21, (m, 3)), axis=0)
+        rec[i, :m, 4] = -1.0
+        rec[i, :m, 5:8] = rng.normal(0, 1, 3) * 1e5 + np.array([-3e8, 0, 0])
+        rec[i, :m, 8] = 1.0 / (1.0 + np.linspace(0, 0.3, m))
+        rec[i, :m, 9] = rng.normal(0, 1e-6, m)
+        rec[i, :m, 10:13] = rng.normal(0, 1e-9, (m, 3))
+        rec[i, :m, 13] = rng.normal(0, 1e-24, m)
+        if lag and m > 0:
+            rec[i, 0, 8:] = np.nan
+        if m > 8 and i % 5 == 0:
+            rec[i, m // 2, 3] = np.nan
+    return rec
+
+
+def test_redshift_rows_match_the_calculator():
+    rng = np.random.default_rng(3)
+    rec = _records(rng)
+    rows = O.redshift_rows(rec, c)
+    for i in range(len(rec)):
+        tr = O.clean_rows(rec[i])
+        if len(tr) < 2:
+            assert np.all(rows[i, :6] == 0.0)
+            continue
+        r = RedshiftCalculator(tr).compute_all_components()
+        for k, name in enumerate(("z_H", "z_SW", "z_ISW", "z_D", "z_total", "z_total_exact")):
+            assert rows[i, k] == r[name], (i, name)
+        assert rows[i, -1] == len(tr)
+
+
+def test_doppler_matches_the_calculator():
+    rng = np.random.default_rng(4)
+    rec = _records(rng, n_photons=12, lag=False)
+    v = rng.normal(0, 3e5, (12, 2, 3))
+    rows = O.redshift_rows(rec, c, v[:, 0], v[:, 1])
+    for i in range(6, 12):
+        tr = O.clean_rows(rec[i])
+        calls = iter([v[i, 0], v[i, 1]])
+        r = RedshiftCalculator(tr, velocity_func=lambda *a: next(calls)).compute_all_components()
+        # np.dot and np.linalg.norm of 3-vectors go through BLAS, whose order may differ
+        assert abs(rows[i, 3] - r["z_D"]) <= 1e-15 * abs(r["z_D"]) + 1e-30
+        assert abs(rows[i, 4] - r["z_total"]) <= 1e-15 * abs(r["z_total"])
+
+
+def test_sky_positions_match_numpy():
+    rng = np.random.default_rng(5)
+    rec = _records(rng)
+    xp, yp, used = O.sky_positions(rec)
+    trajs = [O.clean_rows(r) for r in rec]
+    dirs = np.array([t[0, 5:8] / np.linalg.norm(t[0, 5:8]) for t in trajs if len(t)])
+    md = np.mean(dirs, axis=0)
+    md /= np.linalg.norm(md)
+    assert used.sum() == len(dirs)
+    ct = dirs @ md
+    th = np.arccos(np.clip(ct, -1, 1))
+    ip = dirs - ct[:, None] * md
+    ip /= np.linalg.norm(ip, axis=1)[:, None]
+    up = np.array([0.0, 0, 1])
+    bx = up - up @ md * md
+    bx /= np.linalg.norm(bx)
+    by = np.cross(md, bx)
+    # d - cos(theta) * mean cancels to |d| * theta: relative rounding ~1e-16 / theta**2
+    tol = 1e-15 / th
+    assert np.all(np.abs(xp - ip @ bx * th) <= tol) and np.all(np.abs(yp - ip @ by * th) <= tol)
+
+
+def test_bin_mean_small():
+    x = np.array([0.0, 0.5, 1.0, 0.99, np.nan, 2.0])
+    y = np.array([0.0, 0.5, 1.0, 0.0, 0.0, 0.0])
+    v = np.array([1.0, 2.0, 3.0, 4.0, 5.0, 6.0])
+    mean, cnt = O.bin_mean(x, y, v, 2, 2, (0.0, 1.0, 0.0, 1.0))
+    assert cnt.tolist() == [[1, 1], [0, 2]]
+    assert mean[1, 1] == 2.5 and np.isnan(mean[1, 0]) and mean[0, 1] == 4.0
