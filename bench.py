@@ -72,6 +72,8 @@ def parse():
                         "outputs, synthetic targets) and exit")
     p.add_argument("--profile-sweep", action="store_true",
                    help="only run the 32-row comparison sweep of the sweep leg once and exit")
+    p.add_argument("--profile-redshift-map", type=int, default=0, metavar="N",
+                   help="only time the redshift-map kernels on N synthetic 64-row FLRW histories and exit")
     p.add_argument("--map-side", type=int, default=4096)
     p.add_argument("--train-steps", type=int, default=8000)
     p.add_argument("--smooth-train-steps", type=int, default=12000,
@@ -932,6 +934,60 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def profile_redshift_map(n: int, n_rows: int = 64, reps: int = 5, host_sample: int = 2000) -> dict:
+    """The redshift-map kernels on n synthetic FLRW histories [n, 64, 14] (seeded; the first
+    row's quantity columns NaN, as the runners record them): device-resident table, sky
+    projection and a 512^2 binned map, timed with CUDA events (the stack is larger than L2 from
+    n = 40k on); beside them the host path the reference runs per photon
+    (RedshiftCalculator.compute_all_components, scipy's Simpson) on a sample of photons."""
+    import torch
+    from excalibur_tool_gb300.observables import maps
+    from excalibur_tool_gb300.observables.redshift import RedshiftCalculator
+
+    dev = torch.device("cuda", 0)
+    g = torch.Generator(device=dev).manual_seed(21)
+    f64 = dict(dtype=torch.float64, device=dev)
+    rec = torch.empty((n, n_rows, 14), **f64)
+    rec[..., 0] = 4.6e17 - torch.cumsum(torch.rand((n, n_rows), generator=g, **f64) * 1e14 + 5e13, dim=1)
+    rec[..., 1:4] = torch.rand((n, n_rows, 3), generator=g, **f64) * 3e24
+    rec[..., 4] = -1.0
+    rec[..., 5:8] = torch.randn((n, n_rows, 3), generator=g, **f64) * 1e5 + torch.tensor([-3e8, 0.0, 0.0], **f64)
+    rec[..., 8] = 1.0 / (1.0 + torch.linspace(0.0, 0.3, n_rows, **f64))
+    rec[..., 9] = torch.randn((n, n_rows), generator=g, **f64) * 1e-6
+    rec[..., 10:13] = torch.randn((n, n_rows, 3), generator=g, **f64) * 1e-9
+    rec[..., 13] = torch.randn((n, n_rows), generator=g, **f64) * 1e-24
+    rec[:, 0, 8:] = float("nan")
+
+    def timed(fn):
+        for _ in range(3):
+            fn()
+        torch.cuda.synchronize()
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(reps)]
+        for e0, e1 in evs:
+            e0.record()
+            fn()
+            e1.record()
+        torch.cuda.synchronize()
+        return sum(e0.elapsed_time(e1) for e0, e1 in evs) / reps / 1e3
+
+    t_table = timed(lambda: maps.redshift_table(rec))
+    t_sky = timed(lambda: maps.sky_projection(rec))
+    table = maps.redshift_table(rec)
+    xp, yp, _ = maps.sky_projection(rec)
+    ext = maps.square_extent(xp.cpu().numpy(), yp.cpu().numpy())
+    t_bin = timed(lambda: maps.bin_sky_map(xp, yp, table[:, 4], grid_resolution=512, extent=ext))
+    sample = rec[:host_sample].cpu().numpy()
+    t0 = time.perf_counter()
+    for tr in sample:
+        RedshiftCalculator(tr[~np.isnan(tr).any(axis=1)]).compute_all_components()
+    t_host = (time.perf_counter() - t0) / len(sample)
+    algo_bytes = n * (n_rows * 14 * 8 + len(maps.RS_COLUMNS) * 8)
+    return {"redshift_map_photons": n, "rows": n_rows, "table_ms": t_table * 1e3,
+            "table_photons_per_s": n / t_table, "table_algo_gbs": algo_bytes / t_table / 1e9,
+            "sky_projection_ms": t_sky * 1e3, "bin_512_ms_incl_host_copy": t_bin * 1e3,
+            "host_calculator_photons_per_s": 1.0 / t_host, "host_sample": len(sample)}
+
+
 def main():
     args = parse()
     if args.profile_gemm:
@@ -956,6 +1012,9 @@ def main():
         res = S.run_jobs(jobs)
         torch.cuda.synchronize()
         print(json.dumps({"sweep_rows": len(res), "seconds": time.perf_counter() - t0}), flush=True)
+        return
+    if args.profile_redshift_map:
+        print(json.dumps(profile_redshift_map(args.profile_redshift_map)), flush=True)
         return
     rank, world, local = dist_setup(args.gpus)
     if args.impl == "reference":
