@@ -131,3 +131,23 @@ def test_bin_mean_small():
     mean, cnt = O.bin_mean(x, y, v, 2, 2, (0.0, 1.0, 0.0, 1.0))
     assert cnt.tolist() == [[1, 1], [0, 2]]
     assert mean[1, 1] == 2.5 and np.isnan(mean[1, 0]) and mean[0, 1] == 4.0
+
+
+def test_map_frame_and_extent_follow_the_reference():
+    """The host pieces of observables.maps: the tangent-plane frame and create_2d_map's square
+    extent, against the reference's formulas (compute_redshift_map.py:68-80,
+    compute_time_delay_map.py:330-345)."""
+    from excalibur_tool_gb300.observables import maps
+
+    for mean in ([-1.0, 0.01, 0.02], [0.1, 0.2, 0.95]):
+        m, bx, by = maps.sky_frame(mean)
+        ref_m = np.asarray(mean) / np.linalg.norm(mean)
+        up = np.array([0.0, 0, 1]) if abs(ref_m[2]) < 0.9 else np.array([1.0, 0, 0])
+        ref_bx = up - np.dot(up, ref_m) * ref_m
+        ref_bx = ref_bx / np.linalg.norm(ref_bx)
+        assert np.array_equal(m, ref_m) and np.array_equal(bx, ref_bx)
+        assert np.array_equal(by, np.cross(ref_m, ref_bx))
+    x = np.array([-1.0, 3.0, 0.5])
+    y = np.array([2.0, 2.5, 2.2])
+    x0, x1, y0, y1 = maps.square_extent(x, y)
+    assert (x0, x1) == (1.0 - 2.4, 1.0 + 2.4) and (y0, y1) == (2.25 - 2.4, 2.25 + 2.4)
