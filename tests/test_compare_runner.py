@@ -89,7 +89,7 @@ def _oracle_leg(cfg, geo, states, kind, phi=None, dt_bounds=None):
     dl = geo.dlambda
     dt_min, dt_max = dt_bounds if dt_bounds is not None else (abs(dl), abs(dl))
     tc = TraceConfig(stepper=cfg.integrator, dt=dl, dt_min=dt_min, dt_max=dt_max, max_steps=geo.n_steps,
-                     record_every=cfg.record_every, observables=False)
+                     record_every=cfg.record_every, renormalize_every=cfg.renormalize_every, observables=False)
     r = O.trace(st, states, tc, threads=4)
     tr = r.records[:, : int(r.n_records.max())].copy()
     if shift is not None:
