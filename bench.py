@@ -65,6 +65,8 @@ def parse():
     p.add_argument("--no-batching", action="store_true", help="skip the multi-field RK45 batching leg")
     p.add_argument("--batching-scale", type=int, default=4, help="run 1/scale of the batching configuration")
     p.add_argument("--no-sweep", action="store_true", help="skip the comparison-sweep leg")
+    p.add_argument("--no-redshift-map", action="store_true",
+                   help="skip the redshift-map leg (262,144 recorded 64-row histories)")
     p.add_argument("--profile-gemm", type=int, default=0, metavar="M",
                    help="only time the surrogate's tensor-core GEMM on M rows (for profiling) and exit")
     p.add_argument("--profile-training", type=int, default=0, metavar="STEPS",
@@ -327,6 +329,13 @@ def run_ours(args, rank, world, local):
     if not args.no_sweep and world == 1:
         torch.cuda.empty_cache()
         line["sweep"] = run_sweep_leg(args, dev)
+    if not args.no_redshift_map and world == 1:
+        torch.cuda.empty_cache()
+        rm = profile_redshift_map(262144)
+        if peaks.get("hbm_gbs"):
+            rm["table_frac_of_measured_hbm"] = rm["table_algo_gbs"] / peaks["hbm_gbs"]
+        line["redshift_map"] = rm
+        torch.cuda.empty_cache()
     if not args.no_surrogate and world == 1:
         torch.cuda.empty_cache()
         line["surrogate"] = run_surrogate(args, dev, stream, peaks, rays_s)
