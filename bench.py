@@ -318,7 +318,8 @@ def run_ours(args, rank, world, local):
     if not args.no_variants and world == 1:
         line["variants"] = run_variants(args, wl, peaks, dev, stream, value)
     if not args.no_cpu_baseline and world == 1 and rank == 0:
-        line["cpu_baseline"] = cpu_baseline(wl, steps_per_batch)
+        line["cpu_baseline"] = cpu_baseline(wl, steps_per_batch, res)
+        line["parity"] = line["cpu_baseline"].pop("parity", None)
     if not args.no_precision and world == 1:
         del wl, metric, states, res
         torch.cuda.empty_cache()
@@ -887,31 +888,72 @@ def host_threads():
         return os.cpu_count() or 1
 
 
-def time_oracle(spec, states, cfg, threads, target_s=12.0):
-    """Oracle photon-steps/s on a bounded sample (about target_s of CPU work)."""
+def time_oracle(spec, states, cfg, threads, target_s=12.0, full=False, result=None):
+    """Oracle photon-steps/s on a bounded sample (about target_s of CPU work), or on the whole
+    batch (`full`). `result` (a dict) receives the traced sample and its indices."""
     from oracle import oracle as O
 
-    probe = states[:: max(1, len(states) // (threads * 8))][: threads * 8]
-    t0 = time.perf_counter()
-    r = O.trace(spec, probe, cfg, threads=threads)
-    dt = time.perf_counter() - t0
-    rate = r.n_steps.sum() / dt
-    per_photon = r.n_steps.mean()
-    n_sample = int(min(len(states), max(threads * 16, target_s * rate / max(per_photon, 1))))
+    if full:
+        n_sample = len(states)
+    else:
+        probe = states[:: max(1, len(states) // (threads * 8))][: threads * 8]
+        t0 = time.perf_counter()
+        r = O.trace(spec, probe, cfg, threads=threads)
+        dt = time.perf_counter() - t0
+        rate = r.n_steps.sum() / dt
+        per_photon = r.n_steps.mean()
+        n_sample = int(min(len(states), max(threads * 16, target_s * rate / max(per_photon, 1))))
     idx = np.linspace(0, len(states) - 1, n_sample).astype(int)
     t0 = time.perf_counter()
     r = O.trace(spec, states[idx], cfg, threads=threads)
     dt = time.perf_counter() - t0
+    if result is not None:
+        result["idx"], result["oracle"] = idx, r
     return float(r.n_steps.sum() / dt), n_sample, float(dt), int(r.n_steps.sum())
 
 
-def cpu_baseline(wl, steps_per_batch):
+def parity_vs_oracle(res, idx, o):
+    """The GPU batch against the oracle (the reference's arithmetic, libm pow) on photons idx:
+    statuses and step counts must agree; states and observables to the last digits."""
+    from excalibur_tool_gb300 import _native as N
+    from excalibur_tool_gb300.observables.lensing import deflection_angle, redshift_total
+
+    st = res.state.cpu().numpy()[idx]
+    ob = res.obs.cpu().numpy()[idx]
+
+    def rel(a, b):
+        den = np.maximum(np.abs(a), np.abs(b))
+        with np.errstate(invalid="ignore", divide="ignore"):
+            return float(np.nanmax(np.where(den > 0, np.abs(a - b) / den, 0.0)))
+
+    cols = ("a_obs", "a_em", "phi_obs", "phi_em", "path", "chord", "min_r", "v1x", "v1y", "v1z")
+    ie, ip = N.OBS_COLS.index("excess"), N.OBS_COLS.index("path")
+    return {"n_compared": int(len(idx)), "of": int(res.state.shape[0]),
+            "status_equal": bool(np.array_equal(res.status.cpu().numpy()[idx], o.status)),
+            "n_steps_equal": bool(np.array_equal(res.n_steps.cpu().numpy()[idx], o.n_steps)),
+            "bit_identical_states": int((st == o.state).all(axis=1).sum()),
+            "max_rel_state": rel(st, o.state),
+            "max_rel_obs": {c: rel(ob[:, N.OBS_COLS.index(c)], o.obs[:, N.OBS_COLS.index(c)]) for c in cols},
+            "max_abs_dz": float(np.nanmax(np.abs(redshift_total(ob) - redshift_total(o.obs)))),
+            "max_excess_diff_over_path": float(np.nanmax(np.abs(ob[:, ie] - o.obs[:, ie]) / o.obs[:, ip])),
+            "max_rel_excess": rel(ob[:, ie], o.obs[:, ie]),
+            "max_abs_deflection_rad": float(np.nanmax(np.abs(deflection_angle(ob) - deflection_angle(o.obs)))),
+            "oracle": "oracle/exc_oracle.c (reference operation order, glibc pow), every photon of the batch"}
+
+
+def cpu_baseline(wl, steps_per_batch, res=None):
+    """The oracle on the host cores over the whole batch (~8 s on 16 threads): its rate is the
+    CPU baseline, and its states are compared with the GPU's (`res`) photon for photon."""
     spec, states, cfg = _oracle_inputs(wl)
     threads = host_threads()
-    rate, n, dt, steps = time_oracle(spec, states, cfg, threads)
-    return {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"{n} of {len(states)} photons of the same batch ({steps} photon-steps, {dt:.1f} s), "
-                      f"C restatement of integrate_single (oracle/exc_oracle.c), {threads} threads"}
+    traced = {}
+    rate, n, dt, steps = time_oracle(spec, states, cfg, threads, full=True, result=traced)
+    out = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
+           "sample": f"{n} of {len(states)} photons of the same batch ({steps} photon-steps, {dt:.1f} s), "
+                     f"C restatement of integrate_single (oracle/exc_oracle.c), {threads} threads"}
+    if res is not None and res.obs is not None:
+        out["parity"] = parity_vs_oracle(res, traced["idx"], traced["oracle"])
+    return out
 
 
 def run_reference(args, rank, world):
@@ -993,7 +1035,7 @@ def profile_redshift_map(n: int, n_rows: int = 64, reps: int = 5, host_sample: i
     algo_bytes = n * (n_rows * 14 * 8 + len(maps.RS_COLUMNS) * 8)
     return {"redshift_map_photons": n, "rows": n_rows, "table_ms": t_table * 1e3,
             "table_photons_per_s": n / t_table, "table_algo_gbs": algo_bytes / t_table / 1e9,
-            "sky_projection_ms": t_sky * 1e3, "bin_512_ms_incl_host_copy": t_bin * 1e3,
+            "sky_projection_ms_incl_host_sync": t_sky * 1e3, "bin_512_ms_incl_host_copy": t_bin * 1e3,
             "host_calculator_photons_per_s": 1.0 / t_host, "host_sample": len(sample)}
 
 

@@ -31,7 +31,38 @@ namespace {
 constexpr size_t kQueueBytes = sizeof(unsigned long long);
 
 std::mutex g_mu;
-void* g_addr[EXC_NOALLOC_MAX_DEVICES] = {nullptr};
+
+// The array's address, looked up once per device and per CUDA context: a caller that makes
+// another context current on the same device (the array then lives at another address in it)
+// gets a fresh lookup instead of a stale pointer.
+struct Cached {
+  void* ctx;
+  void* addr;
+};
+Cached g_addr[EXC_NOALLOC_MAX_DEVICES] = {};
+
+// cuCtxGetCurrent through the runtime's driver entry-point query, so that the library does
+// not link the driver library itself (it loads on machines without one). NULL if unavailable:
+// the cache is then keyed on the device alone.
+typedef int (*CtxGetCurrentFn)(void**);
+CtxGetCurrentFn ctx_get_current() {
+  static CtxGetCurrentFn fn = [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      p = nullptr;
+    return reinterpret_cast<CtxGetCurrentFn>(p);
+  }();
+  return fn;
+}
+
+void* current_ctx() {
+  void* ctx = nullptr;
+  CtxGetCurrentFn fn = ctx_get_current();
+  if (!fn || fn(&ctx) != 0) return nullptr;
+  return ctx;
+}
 
 int reject(int code, const char* msg) {
   char buf[256];
@@ -54,16 +85,19 @@ int exc_trace_noalloc(const ExcMetric* metric, const ExcTraceArgs* args, void* s
   if (dev >= EXC_NOALLOC_MAX_DEVICES) return reject(EXC_ERR_INVALID, "device ordinal beyond EXC_NOALLOC_MAX_DEVICES");
   void* scratch = nullptr;
   {
-    // One-time set-up per device, with that device current: look up the
+    // One-time set-up per device (and per context), with that device current: look up the
     // array's device address (the first call on a device does this).
     std::lock_guard<std::mutex> lk(g_mu);
-    if (!g_addr[dev]) {
+    void* ctx = current_ctx();
+    Cached& c = g_addr[dev];
+    if (!c.addr || !ctx || ctx != c.ctx) {
       void* p = nullptr;
       cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
       if (e != cudaSuccess || !p) return reject(EXC_ERR_CUDA, cudaGetErrorString(e));
-      g_addr[dev] = p;
+      c.addr = p;
+      c.ctx = current_ctx();   // the lookup creates the device's primary context if need be
     }
-    scratch = g_addr[dev];
+    scratch = c.addr;
   }
   // exc_trace zeroes the queue head on the stream before the kernel starts,
   // so whatever the previous call left in the array does not matter.

@@ -6,17 +6,26 @@ runs: `Integrator.integrate` traces every photon in one persistent GPU launch
 `integrate_single`; `integrate_single` is the same launch with one photon.
 The steppers' `step()` run one step through the same kernel.
 
-Differences from the reference, all deliberate:
-* `mode` ("sequential" / "parallel" / "chunked") selects nothing: one GPU
-  launch replaces the process pools (integrator.py:443-473).
-* stop modes: "steps" as in the reference; "a" stops once a(eta) <= value,
-  and "box" at the first exit from the grid box (the reference's "a",
-  "redshift" and "chi" read attributes its Photon never sets,
-  integrator.py:204-211, so they cannot work there).
-* photons that the reference would abort with an exception (outside the
-  grid, horizon, non-finite state) get a failure status instead and are
-  counted as failures by `integrate`, like the reference's chunked mode
-  (integrator.py:414-429).
+`integrate` keeps the reference's per-mode contract (integrator.py:434-476):
+* "sequential": every photon is integrated as `integrate_single` with its
+  defaults (record_every=1: a history row per accepted step, the quantity
+  columns one record late, the final record) and updated in order; the first
+  photon that fails raises ValueError, as the reference's loop does, leaving
+  the photons after it untouched; returns len(photons).
+* "parallel" / "chunked": the same launch; a photon that succeeded is updated
+  in place, a photon that failed keeps its input state and history; returns
+  the number of successes. (The reference's chunked mode puts the integrated
+  copies back into the Photons container; its parallel mode discards the
+  pool's copies and only counts them.)
+The photons are traced together in persistent launches (chunked so that the
+recorded rows of one launch stay under 1 GiB of device memory) instead of one
+process per photon or chunk; `n_workers` and `chunk_size` are kept for the
+signature and select nothing.
+
+Other differences, deliberate: stop modes "steps" as in the reference; "a"
+stops once a(eta) <= value, and "box" at the first exit from the grid box (the
+reference's "a", "redshift" and "chi" read attributes its Photon never sets,
+integrator.py:204-211, so they cannot work there).
 """
 from __future__ import annotations
 
@@ -169,64 +178,110 @@ class Integrator:
         return out_host
 
     # ---------------------------------------------- reference-facing API
+    _RECORD_BYTES_PER_LAUNCH = 1 << 30
+
+    def _trace_recorded(self, plist, stop_mode, stop_value, record_every, renormalize_every):
+        """Trace `plist` with records; yields (photon, status, rows [n, cols], final [8]) in order,
+        in launches whose record buffers stay under _RECORD_BYTES_PER_LAUNCH."""
+        import torch
+
+        dev = self._device()
+        cfg = self.config(stop_mode, stop_value, record_every=record_every, renormalize_every=renormalize_every,
+                          observables=False)
+        from ..trace import _default_max_records
+
+        cols = 12 if getattr(self.metric, "internal_coords", None) == "spherical" else 14
+        per_photon = _default_max_records(cfg) * cols * 8
+        chunk = max(1, self._RECORD_BYTES_PER_LAUNCH // per_photon)
+        for lo in range(0, len(plist), chunk):
+            part = plist[lo:lo + chunk]
+            states = np.stack([self._prepare_state(np.concatenate([p.x, p.u])) for p in part])
+            res = trace_batch(self.metric, torch.as_tensor(states, device=dev), cfg)
+            status = res.status.cpu().numpy()
+            nrec = res.n_records.cpu().numpy()
+            final = res.state.cpu().numpy()
+            records = res.records.cpu().numpy()
+            for i, p in enumerate(part):
+                yield p, int(status[i]), records[i, :min(int(nrec[i]), records.shape[1])], final[i]
+
+    @staticmethod
+    def _apply(photon, rows, final):
+        """Update `photon` as integrate_single does: x, u, the history rows, the quantities.
+
+        A row recorded before the first quantity evaluation (the initial record, and the first
+        step's: the reference records before it evaluates, integrator.py:387-394) carries the
+        photon's quantities at call time -- none for a new photon (8 columns)."""
+        q0 = np.asarray(photon.quantities, dtype=float)
+        for row in rows:
+            if np.isnan(row[8:]).all():
+                photon.history.append(np.concatenate([row[:8], q0]))
+            else:
+                photon.history.append(row)
+        photon.x = final[:4].copy()
+        photon.u = final[4:].copy()
+
     def integrate_single(self, photon, stop_mode="steps", stop_value=100, *, record_every: int = 1,
                          trace_norm: bool = False, renormalize_every: int = 0):
         """Integrator.integrate_single (integrator.py:218-409): mutates `photon`
         (x, u, quantities, history) exactly as the reference does."""
-        import torch
         from .._evaluate import null_error
 
         if record_every < 0:
             raise ValueError("record_every must be >= 0")
         if renormalize_every < 0:
             raise ValueError("renormalize_every must be >= 0")
-        state = self._prepare_state(np.concatenate([photon.x, photon.u]))
-        dev = self._device()
+        if stop_mode not in self.STOP_MODES:
+            raise ValueError(f"stop_mode must be one of {self.STOP_MODES}")
         if trace_norm and not hasattr(photon, "norm_history"):
             photon.norm_history = []
-        s = torch.as_tensor(np.asarray(state, dtype=np.float64)[None], device=dev)
-        res = self.trace(s, stop_mode, stop_value, record_every=record_every,
-                         renormalize_every=renormalize_every, observables=False)
-        st = int(res.status[0])
-        nrec = int(res.n_records[0])
-        rows = res.records[0, :min(nrec, res.records.shape[1])].cpu().numpy()
-        final = res.state[0].cpu().numpy()
-        for i, row in enumerate(rows):
-            # the first record (and any recorded before quantities exist) has 8 columns
-            photon.history.append(row if not np.isnan(row[8:]).all() else row[:8])
-        photon.x = final[:4]
-        photon.u = final[4:]
+        _, st, rows, final = next(self._trace_recorded([photon], stop_mode, stop_value, record_every,
+                                                       renormalize_every))
+        self._finish_single(photon, st, rows, final, trace_norm, record_every)
+        return photon
+
+    def _finish_single(self, photon, st, rows, final, trace_norm=False, record_every=1):
+        from .._evaluate import null_error
+
+        self._apply(photon, rows, final)
         if st in N.FAILED_STATUSES:
+            # the reference evaluated the quantities at its last recorded state before it failed
+            # (integrator.py:387-394); they are in no record yet
+            if record_every and len(rows) > 1:
+                try:
+                    photon.quantities = np.asarray(self.metric.metric_physical_quantities(rows[-1][:4]))
+                except ValueError:
+                    pass
             raise ValueError(f"integration failed: {N.STATUS_NAMES.get(st, st)}")
         photon.quantities = rows[-1][8:] if len(rows) else np.array([])
         if trace_norm:
             rel, _ = null_error(self.metric, np.stack([rows[0][:8], final]))
             photon.norm_history.extend(rel.cpu().numpy().tolist())
-        return photon
 
     def integrate(self, photons, stop_mode="steps", stop_value=100, verbose=True):
-        """Integrator.integrate (integrator.py:434-476): all photons in one GPU launch.
-
-        Final states are written back into the Photon objects; returns the
-        number of photons that finished without a failure status."""
-        import torch
-
+        """Integrator.integrate (integrator.py:434-476), with the reference's per-mode results
+        (module docstring): "sequential" updates every photon like integrate_single, raises on
+        the first failure and returns len(photons); "parallel" / "chunked" update the photons
+        that succeeded and return their count."""
         if stop_mode not in self.STOP_MODES:
             raise ValueError(f"stop_mode must be one of {self.STOP_MODES}")
+        if self.mode not in ("sequential", "parallel", "chunked"):
+            raise ValueError("Unknown mode. Use 'sequential', 'parallel', or 'chunked'.")
         plist = list(photons)
-        if not plist:
-            return 0
-        states = np.stack([self._prepare_state(np.concatenate([p.x, p.u])) for p in plist])
-        out = self.integrate_batch(torch.from_numpy(states).pin_memory(), stop_mode, stop_value, observables=False)
-        final = out["state"].numpy()
-        status = out["status"].numpy()
-        ok = 0
-        for p, s, st in zip(plist, final, status):
-            p.x = s[:4].copy()
-            p.u = s[4:].copy()
-            p.history.append(s.copy())
-            if st not in N.FAILED_STATUSES:
-                ok += 1
+        traced = self._trace_recorded(plist, stop_mode, stop_value, 1, 0)
+        if self.mode == "sequential":
+            for p, st, rows, final in traced:
+                self._finish_single(p, st, rows, final)
+            return len(photons)
         if verbose:
-            print(f"GPU integration of {len(plist)} photons: {ok} succeeded")
+            if self.mode == "parallel":
+                print(f"Parallel integration with {self.n_workers} workers...")
+            else:
+                n_chunks = (len(plist) + self.chunk_size - 1) // self.chunk_size
+                print(f"Chunked mode: {n_chunks} chunks of size {self.chunk_size}")
+        ok = 0
+        for p, st, rows, final in traced:
+            if st in N.FAILED_STATUSES:
+                continue
+            self._finish_single(p, st, rows, final)
+            ok += 1
         return ok

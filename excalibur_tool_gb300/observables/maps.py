@@ -121,7 +121,9 @@ def sky_projection(trajectories):
     n_used = int(used.sum())
     if n_used == 0:
         return xp, yp, used
-    m, bx, by = sky_frame((dirs[used].sum(dim=0) / n_used).cpu().numpy())
+    # np.mean over axis 0 on the host, as the reference takes it (rows accumulated in order):
+    # the frame is then the reference's to the bit (3 doubles per photon copied back)
+    m, bx, by = sky_frame(np.mean(dirs[used].cpu().numpy(), axis=0))
     d3 = lambda v: (C.c_double * 3)(*[float(x) for x in v])
     N.check(lib.exc_sky_project(N.ptr(dirs), n, d3(m), d3(bx), d3(by), N.ptr(xp), N.ptr(yp), stream),
             "exc_sky_project")
@@ -150,8 +152,14 @@ def square_extent(x, y, pad: float = 1.2):
     ranges, padded by `pad`, about the centre of the samples."""
     x = np.asarray(x, dtype=np.float64)
     y = np.asarray(y, dtype=np.float64)
+    if x.size == 0 or y.size == 0:
+        raise ValueError("square_extent: no finite sky positions to map")
     xc, yc = (x.min() + x.max()) / 2, (y.min() + y.max()) / 2
     half = max(x.max() - x.min(), y.max() - y.min()) * pad / 2
+    if not half > 0.0:
+        # one sample, or samples on one point: a small square about it, so that the binning's
+        # extent has a width (the reference's griddata cannot interpolate such a set at all)
+        half = 1e-6 * max(1.0, abs(xc), abs(yc))
     return (xc - half, xc + half, yc - half, yc + half)
 
 

@@ -252,9 +252,14 @@ int exc_null_error(const ExcMetric* metric, const double* state, double* rel_err
  * EXC_NOALLOC_SCRATCH_BYTES per GPU, held until the process exits; a launch
  * uses 8 bytes of it (the queue head), on devices 0..EXC_NOALLOC_MAX_DEVICES-1.
  * The first call on a device looks up the array's address (with that device
- * current); make that first call before any stream capture. All calls share
- * the one array, so calls that overlap on the GPU (e.g. concurrent streams)
- * race on the queue: serialise them. Nothing here calls cudaMalloc/cudaFree. */
+ * current); make that first call before any stream capture. The address is
+ * cached per device and per CUDA context: a call from another context on the
+ * same device looks it up again. cudaDeviceReset unloads the library's device
+ * code; a later call may then reuse a stale address if the new primary context
+ * gets the old handle, so a process that resets a device must not call this
+ * entry point again afterwards. All calls share the one array, so calls that
+ * overlap on the GPU (e.g. concurrent streams) race on the queue: serialise
+ * them. Nothing here calls cudaMalloc/cudaFree. */
 #define EXC_NOALLOC_SCRATCH_BYTES 256
 #define EXC_NOALLOC_MAX_DEVICES 64
 int exc_trace_noalloc(const ExcMetric* metric, const ExcTraceArgs* args, void* stream);

@@ -25,6 +25,42 @@
 #include "../excalibur_tool_gb300/csrc/exc_stepctl.h"
 
 /* ------------------------------------------------------------ helpers */
+/* How x**3 and x**4 are evaluated (oracle_set_power_mode):
+ *   0 (default) glibc pow(), as the reference's Python/numpy `**` does;
+ *   1 the double-double power the CUDA library uses (csrc/exc_device.cuh pow3_cr /
+ *     pow4_cr): Dekker's exact square by FMA, the product's error term carried, one final
+ *     rounding. The two differ only where pow() misrounds a near-halfway case (by one ulp);
+ *     mode 1 lets a test show that such ulps are the only difference between the GPU and the
+ *     reference's arithmetic. */
+static int g_power_mode = 0;
+
+void oracle_set_power_mode(int mode) { g_power_mode = mode; }
+int oracle_power_mode(void) { return g_power_mode; }
+
+static double pow3_dd(double x) {
+  const double p = x * x;
+  const double e = fma(x, x, -p);
+  const double hi = p * x;
+  const double lo = fma(p, x, -hi) + e * x;
+  return hi + lo;
+}
+
+static double pow4_dd(double x) {
+  const double p = x * x;
+  const double e = fma(x, x, -p);
+  const double hi = p * p;
+  const double lo = fma(p, p, -hi) + 2.0 * p * e;
+  return hi + lo;
+}
+
+static double cube(double x) { return g_power_mode ? pow3_dd(x) : pow(x, 3.0); }
+static double fourth(double x) { return g_power_mode ? pow4_dd(x) : pow(x, 4.0); }
+
+/* x**3 (p == 3) or x**4 (p == 4) of n values under the current power mode. */
+void oracle_power(const double* x, double* out, int64_t n, int p) {
+  for (int64_t i = 0; i < n; ++i) out[i] = (p == 4) ? fourth(x[i]) : cube(x[i]);
+}
+
 static double py_fmod(double a, double b) { /* CPython float_rem */
   double m = fmod(a, b);
   if (m != 0.0) {
@@ -333,7 +369,7 @@ static int scale_factor(const ExcMetric* m, double eta, double* a_out, double* a
   } else if (m->cosmology == EXC_COSMO_TABLE) {
     a = a_interp(m, eta, &st);
     const double z = 1.0 / a - 1.0;
-    const double E = sqrt(m->omega_m * pow(1 + z, 3.0) + m->omega_r * pow(1 + z, 4.0) +
+    const double E = sqrt(m->omega_m * cube(1 + z) + m->omega_r * fourth(1 + z) +
                           m->omega_k * pow(1 + z, 2.0) + m->omega_lambda);
     adot = a * a * (m->H0 * E);
   } else {
@@ -431,7 +467,7 @@ static int schw_rhs(const ExcMetric* m, const double* s, double* out) {
       dte = -(1.0 / m->c) * sqrt(v);
       du0 = 0.0;
     }
-    const double r3 = pow(r, 3.0);
+    const double r3 = cube(r);
     if (isinf(r3)) return EXC_PH_NONFINITE; /* Python float ** int raises OverflowError */
     du1 = rs / (2.0 * r * (r - rs)) * u1 * u1 -
           (r - rs) / (2.0 * r3) * (m->c2 * rs * dte * dte - 2.0 * r3 * (u2 * u2 + (sn * sn) * u3 * u3));
@@ -658,16 +694,19 @@ static void cart_vel(const ExcMetric* m, const double* s, double* v) {
 
 static double norm3(const double* v) { return sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]); }
 
-/* |d| - d.e with the cross-product form (no cancellation); long double for headroom */
+/* |d| - d.e (e a unit vector) without cancellation: |d x e|^2 / (|d| + d.e), in double in
+ * this order, as the CUDA library evaluates the time-delay excess (csrc/exc_kernels.cuh). The
+ * reference itself has no such column: its time delay is path - chord over the recorded
+ * positions (_postprocessing/compute_time_delay_map.py:112-126), the PATH and CHORD columns. */
 static double excess_term(const double* d, const double* e) {
-  const long double nd = sqrtl((long double)d[0] * d[0] + (long double)d[1] * d[1] + (long double)d[2] * d[2]);
-  const long double de = (long double)d[0] * e[0] + (long double)d[1] * e[1] + (long double)d[2] * e[2];
-  if (de <= 0) return (double)(nd - de);
-  const long double cx = (long double)d[1] * e[2] - (long double)d[2] * e[1];
-  const long double cy = (long double)d[2] * e[0] - (long double)d[0] * e[2];
-  const long double cz = (long double)d[0] * e[1] - (long double)d[1] * e[0];
-  const long double den = nd + de;
-  return den > 0 ? (double)((cx * cx + cy * cy + cz * cz) / den) : 0.0;
+  const double nd = norm3(d);
+  const double de = d[0] * e[0] + d[1] * e[1] + d[2] * e[2];
+  if (de <= 0.0) return nd - de;
+  const double cx = d[1] * e[2] - d[2] * e[1];
+  const double cy = d[2] * e[0] - d[0] * e[2];
+  const double cz = d[0] * e[1] - d[1] * e[0];
+  const double den = nd + de;
+  return den > 0.0 ? (cx * cx + cy * cy + cz * cz) / den : 0.0;
 }
 
 static int quantities(const ExcMetric* m, int fi, const double* s, double* q) {

@@ -6,6 +6,7 @@ pointers, and run the C restatement of the reference (exc_oracle.c).
 """
 from __future__ import annotations
 
+import contextlib
 import ctypes as C
 import dataclasses
 import os
@@ -36,8 +37,33 @@ def lib():
         L.oracle_null_error.argtypes = [C.POINTER(N.ExcMetric), P, P, P, P, C.c_int64]
         L.oracle_step.argtypes = [C.POINTER(N.ExcMetric), C.c_int, C.c_int, P, C.c_double, C.c_double, C.c_double,
                                   P, P, P]
+        L.oracle_set_power_mode.argtypes = [C.c_int]
+        L.oracle_power.argtypes = [P, P, C.c_int64, C.c_int]
+        L.oracle_power_mode.restype = C.c_int
         _lib = L
     return _lib
+
+
+@contextlib.contextmanager
+def power_mode(mode):
+    """Evaluate x**3 and x**4 with glibc pow() ("libm", the reference's `**`, the default) or with
+    the CUDA library's double-double power ("dd") inside the block."""
+    L = lib()
+    prev = L.oracle_power_mode()
+    L.oracle_set_power_mode({"libm": 0, "dd": 1}[mode])
+    try:
+        yield
+    finally:
+        L.oracle_set_power_mode(prev)
+
+
+def power(x, p=3, mode="libm"):
+    """x**p (p = 3 or 4) elementwise with glibc pow() or the double-double power."""
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    out = np.empty_like(x)
+    with power_mode(mode):
+        lib().oracle_power(_p(x), _p(out), x.size, int(p))
+    return out
 
 
 def _p(a):

@@ -4,10 +4,10 @@ Runs lmagristella/excalibur-tool's own Python code (its numba-decorated
 kernels execute as plain Python through the test-only shim in
 oracle/shim/numba) on small seeded inputs and writes the results to
 tests/golden/*.npz. Only the machine that holds the reference checkout can
-run this (default path below, or EXCALIBUR_REF=<path>); the committed .npz
-files are what the tests read.
+run this (--ref <path> or EXCALIBUR_REF=<path>); the committed .npz files
+are what the tests read.
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py --ref <reference checkout> [generator ...]
 """
 from __future__ import annotations
 
@@ -19,7 +19,22 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
-REF = os.environ.get("EXCALIBUR_REF", "/root/reference")
+
+
+def _reference_path(argv):
+    """The reference checkout: `--ref PATH` or the EXCALIBUR_REF environment variable."""
+    if "--ref" in argv:
+        i = argv.index("--ref")
+        path = argv[i + 1]
+        del argv[i:i + 2]
+        return path
+    path = os.environ.get("EXCALIBUR_REF")
+    if not path:
+        sys.exit("usage: make_golden.py --ref PATH_TO_REFERENCE [generator ...] (or set EXCALIBUR_REF)")
+    return path
+
+
+REF = _reference_path(sys.argv)
 sys.path[:0] = [os.path.join(REPO, "oracle", "shim"), REF, REPO]
 
 from excalibur.core.constants import c, G, one_Mpc, one_Msun, one_Gpc  # noqa: E402
@@ -349,6 +364,65 @@ def gen_integrate(cz):
     save("integrate.npz", **out)
 
 
+# ------------------------------------------- Integrator.integrate (per mode)
+def _history_array(p, width=14):
+    hist = p.history.states
+    arr = np.full((len(hist), width), np.nan)
+    for i, h in enumerate(hist):
+        arr[i, :len(h)] = h
+    return arr
+
+
+def gen_integrate_modes(cz):
+    """Integrator.integrate on five photons through a strict ("error") grid, the fourth of
+    which leaves the grid's interior: sequential mode (records every step, raises at that
+    photon, the fifth never integrated) and chunked mode (two workers, chunks of two; the
+    failed photon left as it was)."""
+    g, data, ip = _flrw_setup(cz, seed=11, boundary="error")
+    box = 40 * one_Mpc
+    m = PerturbedFLRWMetricFast(cz.a_of_eta, g, ip, adot_of_eta=cz.adot_of_eta)
+    dt = 0.25 * one_Mpc / c
+    eta0 = cz._eta_at_a1
+    rng = np.random.default_rng(41)
+    inits = []
+    for k in range(5):
+        d = rng.standard_normal(3)
+        d /= np.linalg.norm(d)
+        x0 = np.array([eta0, *(rng.uniform(0.4, 0.6, 3) * box)])
+        if k == 3:      # starts next to the strict interior's edge, heading out
+            x0[1:4] = [0.85 * box, 0.5 * box, 0.5 * box]
+            d = np.array([1.0, 0.0, 0.0])
+        u0 = Photons(m)._solve_u0_from_null_condition(x0, d * c, sign=-1.0)
+        inits.append(np.concatenate([x0, [u0], d * c]))
+    out = {"field": data, "box": box, "dt": dt, "inits": np.array(inits), "n_steps": 40}
+
+    def make():
+        ph = Photons(m)
+        for s in inits:
+            ph.photons.append(Photon(s[:4].copy(), s[4:].copy()))
+        return ph
+
+    integ = Integrator(m, dt=dt, mode="sequential", integrator="rk4", dt_min=dt, dt_max=dt)
+    ph = make()
+    try:
+        integ.integrate(ph.photons, "steps", 40, verbose=False)
+        raised = 0
+    except ValueError:
+        raised = 1
+    out["seq_raised"] = raised
+    for k, p in enumerate(ph.photons):
+        out[f"seq{k}_history"] = _history_array(p)
+        out[f"seq{k}_final"] = np.concatenate([p.x, p.u])
+        out[f"seq{k}_quantities"] = np.asarray(p.quantities, dtype=float)
+    integ = Integrator(m, dt=dt, mode="chunked", integrator="rk4", dt_min=dt, dt_max=dt, n_workers=2, chunk_size=2)
+    ph = make()
+    out["chunked_ok"] = integ.integrate(ph, "steps", 40, verbose=False)
+    for k, p in enumerate(ph.photons):
+        out[f"chunked{k}_history"] = _history_array(p)
+        out[f"chunked{k}_final"] = np.concatenate([p.x, p.u])
+    save("integrate_modes.npz", **out)
+
+
 # ------------------------------------------------------------- cfg1 subset
 def cfg1_initial_states():
     """1024 photons: Schwarzschild lens (1e15 Msun at the box centre), observer at (0,500,500) Mpc,
@@ -623,8 +697,8 @@ def gen_manifest():
             g.write(name + " " + " ".join(argv) + "\n")
 
 
-GENERATORS = ["cosmology", "interp", "interp_slow", "rhs", "steps", "integrate", "generators", "observables",
-              "cfg2_small", "cfg1", "compare_job", "manifest"]
+GENERATORS = ["cosmology", "interp", "interp_slow", "rhs", "steps", "integrate", "integrate_modes", "generators",
+              "observables", "cfg2_small", "cfg1", "compare_job", "manifest"]
 
 if __name__ == "__main__":
     if not os.path.isdir(REF):
@@ -632,12 +706,12 @@ if __name__ == "__main__":
     np.seterr(all="ignore")
     which = sys.argv[1:] or GENERATORS
     cz = gen_cosmology() if "cosmology" in which else None
-    if cz is None and set(which) & {"interp_slow", "rhs", "steps", "integrate", "generators", "observables",
-                                    "cfg2_small"}:
+    if cz is None and set(which) & {"interp_slow", "rhs", "steps", "integrate", "integrate_modes", "generators",
+                                    "observables", "cfg2_small"}:
         cz = LCDM_Cosmology(70, 0.3, 0.0, 0.7)
     for name in which:
         if name == "cosmology":
             continue
         fn = globals()["gen_" + name]
-        fn(cz) if name in ("interp_slow", "rhs", "steps", "integrate", "generators", "observables",
-                           "cfg2_small") else fn()
+        fn(cz) if name in ("interp_slow", "rhs", "steps", "integrate", "integrate_modes", "generators",
+                           "observables", "cfg2_small") else fn()

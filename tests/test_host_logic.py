@@ -162,3 +162,17 @@ def test_trajectory_file_layout(tmp_path):
 
         with h5py.File(p) as f:
             assert np.array_equal(f["trajectories"][()], traj, equal_nan=True) and f.attrs["mass_kg"] == 1.5
+
+
+def test_square_extent_edge_cases():
+    """create_2d_map's square extent: padded larger range about the centre; a single sample gets
+    a small square about it, no sample at all a clear error."""
+    import pytest
+    from excalibur_tool_gb300.observables.maps import square_extent
+
+    x0, x1, y0, y1 = square_extent([0.0, 2.0], [1.0, 1.5])
+    assert (x0, x1) == (1.0 - 1.2, 1.0 + 1.2) and (y0 + y1) / 2 == 1.25 and y1 - y0 == x1 - x0
+    x0, x1, y0, y1 = square_extent([0.01], [-0.02])
+    assert x0 < 0.01 < x1 and y0 < -0.02 < y1
+    with pytest.raises(ValueError):
+        square_extent([], [])

@@ -40,7 +40,7 @@ def _workload():
     return m, states.contiguous(), 0.5 * one_Mpc / c, box
 
 
-def _args(n, states, dt, box, queue):
+def _args(n, states, dt, box, queue, precision="fp64"):
     import torch
     from excalibur_tool_gb300 import _native as N
 
@@ -50,7 +50,7 @@ def _args(n, states, dt, box, queue):
     a = N.ExcTraceArgs()
     a.n_photons = n
     a.state, a.status, a.n_steps = st.data_ptr(), status.data_ptr(), nsteps.data_ptr()
-    a.stepper, a.precision = N.STEPPER["rk4"], N.PRECISION["fp64"]
+    a.stepper, a.precision = N.STEPPER["rk4"], N.PRECISION[precision]
     a.dt = a.dt_min = a.dt_max = dt
     a.max_iter, a.max_steps = 100_000, 1 << 40
     a.stop_flags = N.STOP_BOX
@@ -90,6 +90,24 @@ def test_noalloc_trace_matches_trace_twice():
         assert np.array_equal(got[1], ref[1]), call
         assert np.array_equal(got[2], ref[2]), call
         assert np.array_equal(got[0], ref[0]), call
+
+    # the guarded mixed-precision trace uses the queue twice (the mixed pass, then the FP64
+    # re-trace of the rays it hands back, with the head cleared in between): the same bits as
+    # exc_trace with a caller-owned queue, on two calls in a row
+    mdesc = metric.descriptor(dev, split=True)
+    a, mref = _args(n, states, dt, box, queue, "mixed")
+    N.check(lib.exc_trace(C.byref(mdesc.struct), C.byref(a), stream), "exc_trace mixed")
+    torch.cuda.synchronize()
+    mref = [t.cpu().numpy() for t in mref]
+    assert (mref[1] == N.PH_LEFT_BOX).all()
+    for call in range(2):
+        b, out = _args(n, states, dt, box, None, "mixed")
+        rc = lib.exc_trace_noalloc(C.byref(mdesc.struct), C.byref(b), stream)
+        assert rc == 0, lib.exc_last_error()
+        torch.cuda.synchronize()
+        got = [t.cpu().numpy() for t in out]
+        for g_, r_ in zip(got, mref):
+            assert np.array_equal(g_, r_), call
 
     # a caller-supplied queue is refused with a message
     b, _ = _args(n, states, dt, box, queue)
