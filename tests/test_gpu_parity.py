@@ -145,7 +145,10 @@ def test_rk4_integrate_single_records(cuda):
         assert rel_err(r["state"][0], g[f"case{k}_final"]).max() <= 1e-14
         with O.power_mode("dd"):
             o = O.trace(spec, g[f"case{k}_init"][None], cfg)
-        assert np.array_equal(r["records"], o.records, equal_nan=True) and np.array_equal(r["state"], o.state)
+        assert r["n_records"][0] == o.n_records[0]
+        nr = int(o.n_records[0])
+        assert np.array_equal(r["records"][0, :nr], o.records[0, :nr], equal_nan=True)
+        assert np.array_equal(r["state"], o.state)
 
 
 def test_rk45_integrate_single(cuda):
@@ -161,7 +164,10 @@ def test_rk45_integrate_single(cuda):
     assert rel_err(r["state"][0], g["case4_final"]).max() <= 1e-12
     with O.power_mode("dd"):
         o = O.trace(spec, g["case4_init"][None], cfg)
-    assert np.array_equal(r["records"], o.records, equal_nan=True) and np.array_equal(r["state"], o.state)
+    assert r["n_records"][0] == o.n_records[0]
+    nr = int(o.n_records[0])
+    assert np.array_equal(r["records"][0, :nr], o.records[0, :nr], equal_nan=True)
+    assert np.array_equal(r["state"], o.state)
 
 
 def test_steppers_match_oracle(cuda):
