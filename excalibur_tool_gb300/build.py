@@ -63,8 +63,10 @@ def build(verbose: bool = False, force: bool = False) -> str:
         src = os.path.join(CSRC, unit)
         obj = os.path.join(BUILD, unit.replace(".cu", ".o"))
         objs.append(obj)
-        if force or _sources_newer(obj, [src] + headers):
-            cmd = [nvcc, *ARCH, *COMMON, *extra, "-c", src, "-o", obj]
+        cmd = [nvcc, *ARCH, *COMMON, *extra, "-c", src, "-o", obj]
+        stamp = obj + ".cmd"      # the command that built the object: a change of flags rebuilds it
+        same_cmd = os.path.exists(stamp) and open(stamp).read() == " ".join(cmd)
+        if force or not same_cmd or _sources_newer(obj, [src] + headers):
             jobs.append((unit, cmd))
 
     def run(job):
@@ -80,6 +82,8 @@ def build(verbose: bool = False, force: bool = False) -> str:
             if p.returncode != 0:
                 sys.stderr.write(p.stdout + p.stderr)
                 raise RuntimeError(f"nvcc failed for {unit} (see {log})")
+            with open(os.path.join(BUILD, unit.replace(".cu", ".o")) + ".cmd", "w") as fh:
+                fh.write(" ".join(cmd))
             if verbose:
                 sys.stderr.write(f"[build] {unit} ok\n")
     if force or jobs or not os.path.exists(LIB):
