@@ -941,6 +941,35 @@ def parity_vs_oracle(res, idx, o):
             "oracle": "oracle/exc_oracle.c (reference operation order, glibc pow), every photon of the batch"}
 
 
+def reference_pool(states, n_rays=2048, n_steps=200):
+    """The reference's own multiprocessing path (Integrator(mode="chunked") from the package
+    installed under baseline/_ref, one worker per host core) on a linspace sample of the batch's
+    initial states, n_steps RK4 steps each, in a process of its own (oracle/reference_pool.py).
+    Returns its measurement, or {"unavailable": why}."""
+    from excalibur_tool_gb300 import workloads
+    from excalibur_tool_gb300.core.constants import one_Mpc
+    from excalibur_tool_gb300.objects.fields import lens_plus_grf
+
+    if not os.path.isdir(os.path.join(ROOT, "baseline", "_ref", "excalibur")):
+        return {"unavailable": "the reference package is not installed under baseline/_ref"}
+    phi = lens_plus_grf(128, workloads.BOX, workloads.LENS_MASS, 5 * one_Mpc, workloads.LENS, seed=2)
+    idx = np.linspace(0, len(states) - 1, min(n_rays, len(states))).astype(int)
+    with tempfile.TemporaryDirectory() as tmp:
+        inp, out = os.path.join(tmp, "in.npz"), os.path.join(tmp, "out.json")
+        np.savez(inp, phi=phi, box=workloads.BOX, states=np.asarray(states)[idx], dt=workloads.DLAMBDA,
+                 n_steps=n_steps)
+        r = subprocess.run([sys.executable, os.path.join(ROOT, "oracle", "reference_pool.py"), "--inputs", inp,
+                            "--out", out], capture_output=True, text=True, timeout=600)
+        if r.returncode != 0:
+            return {"unavailable": "reference pool run failed: " + (r.stderr.strip().splitlines() or ["?"])[-1]}
+        with open(out) as f:
+            res = json.load(f)
+    res["unit"] = UNIT
+    res["sample"] = (f"{len(idx)} of {len(states)} initial states of the batch (linspace), {n_steps} RK4 steps "
+                     f"each (the reference has no box stop)")
+    return res
+
+
 def cpu_baseline(wl, steps_per_batch, res=None):
     """The oracle on the host cores over the whole batch (~8 s on 16 threads): its rate is the
     CPU baseline, and its states are compared with the GPU's (`res`) photon for photon."""
@@ -953,6 +982,7 @@ def cpu_baseline(wl, steps_per_batch, res=None):
                      f"C restatement of integrate_single (oracle/exc_oracle.c), {threads} threads"}
     if res is not None and res.obs is not None:
         out["parity"] = parity_vs_oracle(res, traced["idx"], traced["oracle"])
+    out["reference_pool"] = reference_pool(states)
     return out
 
 
@@ -982,6 +1012,8 @@ def run_reference(args, rank, world):
                                        f"(~10 s of CPU work), C restatement of integrate_single "
                                        f"(oracle/exc_oracle.c), {threads} threads"},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    # the reference's own Python path (its multiprocessing pool) beside the C restatement
+    line["cpu_baseline"]["reference_pool"] = reference_pool(states)
     print(json.dumps(line), flush=True)
 
 
@@ -1032,11 +1064,23 @@ def profile_redshift_map(n: int, n_rows: int = 64, reps: int = 5, host_sample: i
     for tr in sample:
         RedshiftCalculator(tr[~np.isnan(tr).any(axis=1)]).compute_all_components()
     t_host = (time.perf_counter() - t0) / len(sample)
+    # the time-delay script's per-photon loop (compute_time_delay_map.py:97-126, 275-297): a
+    # norm per recorded segment, then the chord
+    t0 = time.perf_counter()
+    for tr in sample:
+        pos = tr[~np.isnan(tr).any(axis=1)][:, 1:4]
+        path = 0.0
+        for i in range(len(pos) - 1):
+            path += np.linalg.norm(pos[i + 1] - pos[i])
+        _ = path / 299792458.0 - np.linalg.norm(pos[-1] - pos[0]) / 299792458.0
+    t_host_td = (time.perf_counter() - t0) / len(sample)
     algo_bytes = n * (n_rows * 14 * 8 + len(maps.RS_COLUMNS) * 8)
     return {"redshift_map_photons": n, "rows": n_rows, "table_ms": t_table * 1e3,
             "table_photons_per_s": n / t_table, "table_algo_gbs": algo_bytes / t_table / 1e9,
+            "table_columns": len(maps.RS_COLUMNS),
             "sky_projection_ms_incl_host_sync": t_sky * 1e3, "bin_512_ms_incl_host_copy": t_bin * 1e3,
-            "host_calculator_photons_per_s": 1.0 / t_host, "host_sample": len(sample)}
+            "host_calculator_photons_per_s": 1.0 / t_host,
+            "host_time_delay_photons_per_s": 1.0 / t_host_td, "host_sample": len(sample)}
 
 
 def main():

@@ -35,7 +35,8 @@ GRAD = {"base_node": 0, "trilinear": 1}
 PROBE = {"addmul": 0, "div": 1, "sqrt": 2, "fmod": 3}
 # exc_record_redshift output columns (EXC_RS_*)
 RS_COLUMNS = ("z_H", "z_SW", "z_ISW", "z_D", "z_total", "z_total_exact", "Phi_obs", "Phi_em", "a_obs", "a_em",
-              "eta_obs", "eta_em", "x_obs0", "x_obs1", "x_obs2", "x_em0", "x_em1", "x_em2", "n_rows")
+              "eta_obs", "eta_em", "x_obs0", "x_obs1", "x_obs2", "x_em0", "x_em1", "x_em2", "n_rows",
+              "path", "chord", "time_delay", "td_kept")
 DTYPE_F64, DTYPE_F32, DTYPE_F32X2 = 0, 1, 2
 STEPPER = {"rk4": 0, "rk45": 1, "leapfrog4": 2}
 TABLEAU = {"reference": 0, "fehlberg": 1}

@@ -7,10 +7,14 @@
 // scipy.integrate.simpson for the ISW integral; :54-95 for the sky positions) and grids them
 // with scipy's griddata. Here the NaN-padded record stack the tracer leaves in HBM
 // ([n_photons][n_rows][n_cols] float64, the runners' trajectory-file layout) is read in place:
-// one thread per photon compacts its clean rows into a scratch index list and evaluates every
-// component in the reference's operation order (compiled with --fmad=false, so no product is
-// contracted): the ISW Simpson sum follows scipy's irregular-spacing rule and numpy's pairwise
-// summation term for term. Sky positions are a per-photon projection; maps are pixel means by
+// one thread per photon scans its rows once and evaluates every component in the reference's
+// operation order (compiled with --fmad=false, so no product is contracted): the ISW Simpson sum
+// follows scipy's irregular-spacing rule and numpy's pairwise summation term for term, and the
+// time delay of _postprocessing/compute_time_delay_map.py:97-126,244-310 (path over the recorded
+// rows minus the chord) is summed in the same scan. numpy sums up to 128 terms as one block,
+// which a single scan can follow; longer histories (more than 257 rows, where the block split
+// depends on the clean-row count) compact their clean rows into a scratch index list first and
+// sum from it in a second pass. Sky positions are a per-photon projection; maps are pixel means by
 // atomics (binning in place of griddata's interpolation).
 #include <cuda_runtime.h>
 
@@ -26,6 +30,8 @@ void set_last_error(const char* msg);
 namespace {
 
 constexpr int kThreads = 128;
+// the most rows a history can have for its pair terms (at most (n - 1) / 2) to fit one numpy block
+constexpr int kOnePassRows = 257;
 
 __device__ __forceinline__ bool row_clean(const double* row, int n_cols) {
   for (int c = 0; c < n_cols; ++c)
@@ -54,19 +60,25 @@ struct Clean {
   double c2;
   __device__ __forceinline__ double eta(int k) const { return rows[(int64_t)idx[k] * n_cols]; }
   __device__ __forceinline__ double dphi(int k) const { return rows[(int64_t)idx[k] * n_cols + 13] * c2; }
-  // scipy's _basic_simpson term of the pair starting at sample 2j (irregular spacing)
-  __device__ double term(int j) const {
-    const int k = 2 * j;
-    const double x0 = eta(k), x1 = eta(k + 1), x2 = eta(k + 2);
-    const double h0 = x1 - x0, h1 = x2 - x1;
-    const double hsum = h0 + h1, hprod = h0 * h1;
-    const double h0divh1 = div0(h0, h1);
-    const double t0 = dphi(k) * (2.0 - div0(1.0, h0divh1));
-    const double t1 = dphi(k + 1) * (hsum * div0(hsum, hprod));
-    const double t2 = dphi(k + 2) * (2.0 - h0divh1);
-    return hsum / 6.0 * ((t0 + t1) + t2);
-  }
+  __device__ double term(int j) const;
 };
+
+// scipy's _basic_simpson term of the samples (x0, y0), (x1, y1), (x2, y2) (irregular spacing)
+__device__ __forceinline__ double simpson_term(double x0, double x1, double x2, double y0, double y1, double y2) {
+  const double h0 = x1 - x0, h1 = x2 - x1;
+  const double hsum = h0 + h1, hprod = h0 * h1;
+  const double h0divh1 = div0(h0, h1);
+  const double t0 = y0 * (2.0 - div0(1.0, h0divh1));
+  const double t1 = y1 * (hsum * div0(hsum, hprod));
+  const double t2 = y2 * (2.0 - h0divh1);
+  return hsum / 6.0 * ((t0 + t1) + t2);
+}
+
+// the term of the pair starting at clean sample 2j
+__device__ double Clean::term(int j) const {
+  const int k = 2 * j;
+  return simpson_term(eta(k), eta(k + 1), eta(k + 2), dphi(k), dphi(k + 1), dphi(k + 2));
+}
 
 // numpy's pairwise sum of the terms [lo, lo + n) of a block of at most 128: fewer than 8 in
 // order, else eight partial sums combined as a balanced tree, then the remainder in order.
@@ -131,28 +143,72 @@ __device__ double pairwise(const Clean& cl, int n) {
   }
 }
 
-// scipy.integrate.simpson(dphi, x=eta) over the m >= 2 clean samples.
-__device__ double simpson(const Clean& cl, int m) {
-  if (m % 2 == 1) return 0.0 + pairwise(cl, (m - 1) / 2);
+// scipy.integrate.simpson(dphi, x=eta) over m >= 2 clean samples, given the pairwise sum of the
+// pair terms (`pairs`) and the last three samples (x[2] the last; for m == 2, x[1] and x[2]).
+__device__ double simpson_finish(int m, double pairs, const double x[3], const double y[3]) {
+  if (m % 2 == 1) return 0.0 + pairs;
   if (m == 2) {
-    const double last_dx = cl.eta(1) - cl.eta(0);
-    return 0.0 + (0.0 + 0.5 * last_dx * (cl.dphi(1) + cl.dphi(0)));
+    const double last_dx = x[2] - x[1];
+    return 0.0 + (0.0 + 0.5 * last_dx * (y[2] + y[1]));
   }
-  double result = 0.0 + pairwise(cl, (m - 2) / 2);
-  const double h0 = cl.eta(m - 2) - cl.eta(m - 3);
-  const double h1 = cl.eta(m - 1) - cl.eta(m - 2);
+  double result = 0.0 + pairs;
+  const double h0 = x[1] - x[0];
+  const double h1 = x[2] - x[1];
   // Cartwright's correction of the last interval, with scipy's zero-denominator guards
   const double alpha = div0(2.0 * (h1 * h1) + (3.0 * h0) * h1, 6.0 * (h1 + h0));
   const double beta = div0(h1 * h1 + (3.0 * h0) * h1, 6.0 * h0);
   const double eta = div0(cube_dd(h1), (6.0 * h0) * (h0 + h1));
-  result += (alpha * cl.dphi(m - 1) + beta * cl.dphi(m - 2)) - eta * cl.dphi(m - 3);
+  result += (alpha * y[2] + beta * y[1]) - eta * y[0];
   return result + 0.0;
 }
 
-__device__ __forceinline__ double dot3(const double* a, const double* b) {
-  return (a[0] * b[0] + a[1] * b[1]) + a[2] * b[2];
+__device__ double simpson(const Clean& cl, int m) {
+  const int n_pairs = (m % 2 == 1) ? (m - 1) / 2 : (m - 2) / 2;
+  const double pairs = (m == 2) ? 0.0 : pairwise(cl, n_pairs);
+  double x[3], y[3];
+  for (int k = 0; k < 3; ++k) {
+    const int q = m - 3 + k;
+    x[k] = q >= 0 ? cl.eta(q) : 0.0;
+    y[k] = q >= 0 ? cl.dphi(q) : 0.0;
+  }
+  return simpson_finish(m, pairs, x, y);
 }
 
+// numpy's pairwise sum of a stream of at most 128 terms, fed in order: the first eight seed the
+// eight partial sums, each later complete group of eight adds into them, and the last incomplete
+// group is added in order after the partial sums are combined (fewer than eight terms in all:
+// added in order to -0.0).
+struct PairwiseStream {
+  double r[8], g[8];
+  int ng, groups;
+  __device__ __forceinline__ void init() { ng = 0; groups = 0; }
+  __device__ __forceinline__ void push(double t) {
+    g[ng++] = t;
+    if (ng == 8) {
+#pragma unroll
+      for (int j = 0; j < 8; ++j) r[j] = groups ? r[j] + g[j] : g[j];
+      ++groups;
+      ng = 0;
+    }
+  }
+  __device__ __forceinline__ double sum() const {
+    double res = groups ? ((r[0] + r[1]) + (r[2] + r[3])) + ((r[4] + r[5]) + (r[6] + r[7])) : -0.0;
+    for (int i = 0; i < ng; ++i) res += g[i];
+    return res;
+  }
+};
+
+// np.dot of two 3-vectors, and the square under np.linalg.norm of one: numpy hands both to BLAS
+// ddot, whose x86-64 kernel (OpenBLAS, FMA) forms the first product and fuses the other two
+// into it in order -- the same bits numpy returns there.
+__device__ __forceinline__ double dot3(const double* a, const double* b) {
+  return fma(a[2], b[2], fma(a[1], b[1], a[0] * b[0]));
+}
+
+// ONE_PASS: n_rows <= 257, so a photon has at most 128 pair terms (one numpy block): the scan
+// sums them as it goes and no scratch is used. Otherwise the scan writes the clean rows' indices
+// to scratch and the Simpson sum reads them back.
+template <bool ONE_PASS>
 __global__ void __launch_bounds__(kThreads) record_redshift_kernel(const double* __restrict__ records,
                                                                    int64_t n_photons, int32_t n_rows,
                                                                    int32_t n_cols, double c,
@@ -161,19 +217,46 @@ __global__ void __launch_bounds__(kThreads) record_redshift_kernel(const double*
                                                                    int32_t* __restrict__ scratch,
                                                                    double* __restrict__ out) {
   const double nan = __longlong_as_double(0x7ff8000000000000ll);
+  const double c2 = c * c;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n_photons;
        i += (int64_t)gridDim.x * blockDim.x) {
     const double* rows = records + i * (int64_t)n_rows * n_cols;
-    int32_t* idx = scratch + i * (int64_t)n_rows;
-    int m = 0;
-    for (int r = 0; r < n_rows; ++r)
-      if (row_clean(rows + (int64_t)r * n_cols, n_cols)) idx[m++] = r;
+    int32_t* idx = ONE_PASS ? nullptr : scratch + i * (int64_t)n_rows;
+    // the scan: first and last clean rows, the last three samples, the path, the largest |x|
+    // and |eta|, and (one pass) the Simpson pair terms
+    int m = 0, first = -1, last = -1;
+    double x3[3] = {0.0, 0.0, 0.0}, y3[3] = {0.0, 0.0, 0.0}, prev[3] = {0.0, 0.0, 0.0};
+    double path = 0.0, max_pos = 0.0, max_eta = 0.0;
+    PairwiseStream ps;
+    ps.init();
+    for (int r = 0; r < n_rows; ++r) {
+      const double* row = rows + (int64_t)r * n_cols;
+      if (!row_clean(row, n_cols)) continue;
+      if (!ONE_PASS) idx[m] = r;
+      if (first < 0) first = r;
+      last = r;
+      x3[0] = x3[1]; x3[1] = x3[2]; x3[2] = row[0];
+      y3[0] = y3[1]; y3[1] = y3[2]; y3[2] = row[13] * c2;
+      if (ONE_PASS && m >= 2 && (m % 2) == 0) ps.push(simpson_term(x3[0], x3[1], x3[2], y3[0], y3[1], y3[2]));
+      if (m >= 1) {
+        // compute_travel_time_deflected: path_length += norm(positions[i + 1] - positions[i])
+        double d[3];
+        for (int k = 0; k < 3; ++k) d[k] = row[1 + k] - prev[k];
+        path += sqrt(dot3(d, d));
+      }
+      for (int k = 0; k < 3; ++k) {
+        prev[k] = row[1 + k];
+        max_pos = fmax(max_pos, fabs(row[1 + k]));
+      }
+      max_eta = fmax(max_eta, fabs(row[0]));
+      ++m;
+    }
     double* o = out + i * EXC_RS_NCOLS;
     for (int k = 0; k < EXC_RS_NCOLS; ++k) o[k] = (k >= EXC_RS_PHI_OBS && k < EXC_RS_N_ROWS) ? nan : 0.0;
     o[EXC_RS_N_ROWS] = (double)m;
     if (m == 0) continue;
-    const double* f = rows + (int64_t)idx[0] * n_cols;
-    const double* l = rows + (int64_t)idx[m - 1] * n_cols;
+    const double* f = rows + (int64_t)first * n_cols;
+    const double* l = rows + (int64_t)last * n_cols;
     o[EXC_RS_PHI_OBS] = f[9];
     o[EXC_RS_PHI_EM] = l[9];
     o[EXC_RS_A_OBS] = f[8];
@@ -184,12 +267,26 @@ __global__ void __launch_bounds__(kThreads) record_redshift_kernel(const double*
       o[EXC_RS_X_OBS + k] = f[1 + k];
       o[EXC_RS_X_EM + k] = l[1 + k];
     }
-    if (m < 2) continue;  // compute_redshift_map leaves such photons at zero
-    const double c2 = c * c;
+    // compute_time_delay_map's loader keeps a photon whose clean rows stay below 1e26 m and 3e18 s
+    o[EXC_RS_TD_KEPT] = (max_pos < 1e26 && max_eta < 3e18) ? 1.0 : 0.0;
+    if (m < 2) continue;  // compute_redshift_map and compute_time_delays leave such photons at zero
+    {
+      double X[3];
+      for (int k = 0; k < 3; ++k) X[k] = l[1 + k] - f[1 + k];
+      const double chord = sqrt(dot3(X, X));
+      o[EXC_RS_PATH] = path;
+      o[EXC_RS_CHORD] = chord;
+      o[EXC_RS_TIME_DELAY] = path / c - chord / c;
+    }
     const double z_h = (f[8] / l[8]) - 1.0;
     const double z_sw = (f[9] - l[9]) / c2;
-    const Clean cl{rows, idx, n_cols, c2};
-    const double z_isw = -simpson(cl, m) / c2;
+    double z_isw;
+    if (ONE_PASS) {
+      z_isw = -simpson_finish(m, m == 2 ? 0.0 : ps.sum(), x3, y3) / c2;
+    } else {
+      const Clean cl{rows, idx, n_cols, c2};
+      z_isw = -simpson(cl, m) / c2;
+    }
     double z_d = 0.0;
     if (v_obs != nullptr && v_em != nullptr) {
       double d[3], nh[3];
@@ -320,8 +417,9 @@ extern "C" int exc_record_redshift(const double* records, int64_t n_photons, int
                n_photons, n_rows, n_cols, 14))
     return EXC_ERR_INVALID;
   if (n_photons == 0) return EXC_SUCCESS;
-  if (!records || !scratch || !out) {
-    exc::set_last_error("record_redshift: records, scratch and out are required");
+  const bool one_pass = n_rows <= kOnePassRows;
+  if (!records || !out || (!one_pass && !scratch)) {
+    exc::set_last_error("record_redshift: records and out are required, and scratch when n_rows > 257");
     return EXC_ERR_INVALID;
   }
   if ((v_obs == nullptr) != (v_em == nullptr)) {
@@ -332,8 +430,12 @@ extern "C" int exc_record_redshift(const double* records, int64_t n_photons, int
     exc::set_last_error("record_redshift: c must be finite and > 0");
     return EXC_ERR_INVALID;
   }
-  record_redshift_kernel<<<grid_for(n_photons, kThreads), kThreads, 0, (cudaStream_t)stream>>>(
-      records, n_photons, n_rows, n_cols, c, v_obs, v_em, scratch, out);
+  if (one_pass)
+    record_redshift_kernel<true><<<grid_for(n_photons, kThreads), kThreads, 0, (cudaStream_t)stream>>>(
+        records, n_photons, n_rows, n_cols, c, v_obs, v_em, nullptr, out);
+  else
+    record_redshift_kernel<false><<<grid_for(n_photons, kThreads), kThreads, 0, (cudaStream_t)stream>>>(
+        records, n_photons, n_rows, n_cols, c, v_obs, v_em, scratch, out);
   return launch_status();
 }
 

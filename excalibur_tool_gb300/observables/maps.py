@@ -8,9 +8,13 @@ _postprocessing/compute_time_delay_map.py:313-357). Here the NaN-padded record s
 leaves on the device (TraceConfig.record_every; records.trajectories_from_result's layout) is
 read in place by the kernels of csrc/exc_maps.cu:
 
-    table = redshift_table(records)                       # [n, 19] on the device (RS_COLUMNS)
+    table = redshift_table(records)                       # [n, 23] on the device (RS_COLUMNS)
     data, (x, y) = compute_redshift_map(records)          # the reference function's outputs
     X, Y, zmap, count = bin_sky_map(x, y, data["z_total"], grid_resolution=256)
+    delays, path, chord, (x, y) = compute_time_delays(records)   # compute_time_delay_map's
+
+The same table carries the time delay of _postprocessing/compute_time_delay_map.py (path over
+the recorded rows minus the chord, so it depends on record_every like the reference's).
 
 Maps are pixel means (binning) where the reference interpolates with griddata(method="cubic").
 Only trajectories that carry the recorded quantities (n_cols >= 14: a, Phi, grad Phi, Phi_dot)
@@ -28,6 +32,8 @@ from ..core.constants import c
 
 RS_COLUMNS = N.RS_COLUMNS
 _COL = {k: i for i, k in enumerate(RS_COLUMNS)}
+# the longest history exc_record_redshift reads in one pass, without scratch
+ONE_PASS_ROWS = 257
 
 
 def _as_stack(trajectories, device=None):
@@ -59,10 +65,12 @@ def _as_stack(trajectories, device=None):
 def redshift_table(trajectories, velocity_func=None):
     """Per-photon redshift components [n, len(RS_COLUMNS)] float64 on the device: the columns of
     RS_COLUMNS (z_H, z_SW, z_ISW, z_D, z_total, z_total_exact, the endpoint Phi, a, eta and x,
-    and the clean row count). Photons with fewer than two clean rows keep zero components, as
-    compute_redshift_map leaves them. `velocity_func(x, y, z, eta) -> (vx, vy, vz)` (the
-    reference's peculiar-velocity callable) adds the Doppler term: it is called on the host at
-    each photon's two endpoints, then the table is recomputed with those velocities."""
+    the clean row count, the recorded path, chord and time delay, and whether the time-delay
+    loader keeps the photon). Photons with fewer than two clean rows keep zero components and
+    delays, as compute_redshift_map and compute_time_delays leave them.
+    `velocity_func(x, y, z, eta) -> (vx, vy, vz)` (the reference's peculiar-velocity callable)
+    adds the Doppler term: it is called on the host at each photon's two endpoints, then the
+    table is recomputed with those velocities."""
     import torch
 
     rec = _as_stack(trajectories)
@@ -71,7 +79,9 @@ def redshift_table(trajectories, velocity_func=None):
         raise ValueError("the device redshift map needs the recorded quantities (n_cols >= 14); "
                          "use RedshiftCalculator with a_of_eta and potential_func for bare states")
     lib = N.load()
-    scratch = torch.empty((n, max(n_rows, 1)), dtype=torch.int32, device=rec.device)
+    # up to 257 rows the kernel reads each history once and needs no scratch; longer ones list
+    # their clean rows there for a second, recursive Simpson pass
+    scratch = torch.empty((n, n_rows), dtype=torch.int32, device=rec.device) if n_rows > ONE_PASS_ROWS else None
     out = torch.empty((n, len(RS_COLUMNS)), dtype=torch.float64, device=rec.device)
     stream = N.stream_handle(rec.device)
     N.check(lib.exc_record_redshift(N.ptr(rec), n, n_rows, n_cols, float(c), None, None, N.ptr(scratch),
@@ -90,19 +100,23 @@ def redshift_table(trajectories, velocity_func=None):
     return out
 
 
-def sky_frame(mean_dir):
+def sky_frame(mean_dir, normalize_y: bool = False):
     """The reference's tangent-plane frame about a mean direction (unnormalised input): the unit
     mean, basis_x from the z axis (or the x axis when the mean is within ~26 deg of z) with its
-    mean component removed, basis_y = mean x basis_x."""
+    mean component removed, basis_y = mean x basis_x (divided by its norm with `normalize_y`,
+    as the time-delay script's extract_initial_directions does, compute_time_delay_map.py:208)."""
     m = np.asarray(mean_dir, dtype=np.float64)
     m = m / np.linalg.norm(m)
     up = np.array([0.0, 0.0, 1.0]) if abs(m[2]) < 0.9 else np.array([1.0, 0.0, 0.0])
     bx = up - np.dot(up, m) * m
     bx = bx / np.linalg.norm(bx)
-    return m, bx, np.cross(m, bx)
+    by = np.cross(m, bx)
+    if normalize_y:
+        by = by / np.linalg.norm(by)
+    return m, bx, by
 
 
-def sky_projection(trajectories):
+def sky_projection(trajectories, normalize_y: bool = False):
     """(x_proj, y_proj, used) on the device for every photon: `used` marks the photons with at
     least one clean row (the only ones the reference's arrays hold); the others read NaN."""
     import torch
@@ -123,7 +137,7 @@ def sky_projection(trajectories):
         return xp, yp, used
     # np.mean over axis 0 on the host, as the reference takes it (rows accumulated in order):
     # the frame is then the reference's to the bit (3 doubles per photon copied back)
-    m, bx, by = sky_frame(np.mean(dirs[used].cpu().numpy(), axis=0))
+    m, bx, by = sky_frame(np.mean(dirs[used].cpu().numpy(), axis=0), normalize_y)
     d3 = lambda v: (C.c_double * 3)(*[float(x) for x in v])
     N.check(lib.exc_sky_project(N.ptr(dirs), n, d3(m), d3(bx), d3(by), N.ptr(xp), N.ptr(yp), stream),
             "exc_sky_project")
@@ -145,6 +159,27 @@ def compute_redshift_map(trajectories, a_of_eta=None, potential_func=None, veloc
     if verbose:
         print(f"redshift map: {len(table)} photons, {int((table[:, _COL['n_rows']] >= 2).sum())} with >= 2 rows")
     return data, extract_sky_positions(trajectories)
+
+
+def compute_time_delays(trajectories, metadata=None):
+    """compute_time_delay_map.py:244-310 on the device, over the photons its loader keeps
+    (load_trajectories, :76-92: a clean row, |x| < 1e26 m, |eta| < 3e18 s): (time_delays,
+    distances_deflected, distances_straight, (x_proj, y_proj)) numpy arrays. The delay is the
+    path summed over consecutive recorded rows minus the chord, over c; the sky positions are
+    extract_initial_directions' (:157-239) over the kept photons. `metadata` is accepted for the
+    reference's signature and not used."""
+    rec = _as_stack(trajectories)
+    table = redshift_table(rec)
+    kept = table[:, _COL["td_kept"]] == 1.0
+    t = table[kept].cpu().numpy()
+    delays = np.ascontiguousarray(t[:, _COL["time_delay"]])
+    path = np.ascontiguousarray(t[:, _COL["path"]])
+    chord = np.ascontiguousarray(t[:, _COL["chord"]])
+    if not bool(kept.any()):
+        return delays, path, chord, (np.array([]), np.array([]))
+    sub = rec[kept] if not bool(kept.all()) else rec
+    xp, yp, used = sky_projection(sub, normalize_y=True)
+    return delays, path, chord, (xp[used].cpu().numpy(), yp[used].cpu().numpy())
 
 
 def square_extent(x, y, pad: float = 1.2):

@@ -406,11 +406,20 @@ enum {
   EXC_RS_X_OBS = 12,         /* 3 columns */
   EXC_RS_X_EM = 15,          /* 3 columns */
   EXC_RS_N_ROWS = 18,        /* clean rows; components stay 0 below 2, as in compute_redshift_map */
-  EXC_RS_NCOLS = 19
+  /* time delay over the recorded rows (_postprocessing/compute_time_delay_map.py:97-126,
+   * 244-310): 0 below two clean rows, as compute_time_delays leaves them */
+  EXC_RS_PATH = 19,          /* sum of |x_{k+1} - x_k| over consecutive clean rows, m */
+  EXC_RS_CHORD = 20,         /* |x_last - x_first|, m */
+  EXC_RS_TIME_DELAY = 21,    /* path / c - chord / c, s */
+  EXC_RS_TD_KEPT = 22,       /* 1 when load_trajectories (:76-92) keeps the photon: a clean row,
+                                every clean |x| < 1e26 m and |eta| < 3e18 s; else 0 */
+  EXC_RS_NCOLS = 23
 };
 /* out: [n_photons][EXC_RS_NCOLS] float64, device. scratch: n_photons * n_rows int32,
- * device. v_obs, v_em: [n_photons][3] float64 peculiar velocities at the first and
- * last clean row (the reference's velocity_func evaluated there), or both NULL. */
+ * device, used only when n_rows > 257 (NULL allowed otherwise: up to 257 rows, the ISW
+ * Simpson sum is one numpy summation block and the kernel reads each row once). v_obs, v_em:
+ * [n_photons][3] float64 peculiar velocities at the first and last clean row (the
+ * reference's velocity_func evaluated there), or both NULL. */
 int exc_record_redshift(const double* records, int64_t n_photons, int32_t n_rows, int32_t n_cols, double c,
                         const double* v_obs, const double* v_em, int32_t* scratch, double* out, void* stream);
 /* dirs: [n_photons][3], the unit spatial velocity (columns 5..7) of each photon's first clean

@@ -67,7 +67,10 @@ def _pairwise(a, lo, n):
 
 
 def _fma(a: float, b: float, c: float) -> float:
-    """a * b + c rounded once."""
+    """a * b + c rounded once (an infinity or a NaN among the operands propagates as IEEE
+    arithmetic does)."""
+    if not (math.isfinite(a) and math.isfinite(b) and math.isfinite(c)):
+        return a * b + c
     return float(Fraction(a) * Fraction(b) + Fraction(c))
 
 
@@ -130,12 +133,40 @@ def clean_rows(states: np.ndarray) -> np.ndarray:
 
 
 def _dot3(a, b):
-    return (a[0] * b[0] + a[1] * b[1]) + a[2] * b[2]
+    """np.dot of two 3-vectors (and the square under np.linalg.norm): BLAS ddot, which on x86-64
+    (OpenBLAS with FMA) forms a0*b0 and fuses a1*b1, then a2*b2, into it."""
+    return _fma(float(a[2]), float(b[2]), _fma(float(a[1]), float(b[1]), float(a[0]) * float(b[0])))
 
 
 # output columns, as csrc/exc_maps.cu writes them (EXC_RS_* in include/excalibur_gb300.h)
 COLUMNS = ("z_H", "z_SW", "z_ISW", "z_D", "z_total", "z_total_exact", "Phi_obs", "Phi_em", "a_obs", "a_em",
-           "eta_obs", "eta_em", "x_obs0", "x_obs1", "x_obs2", "x_em0", "x_em1", "x_em2", "n_rows")
+           "eta_obs", "eta_em", "x_obs0", "x_obs1", "x_obs2", "x_em0", "x_em1", "x_em2", "n_rows",
+           "path", "chord", "time_delay", "td_kept")
+_C = {k: i for i, k in enumerate(COLUMNS)}
+
+
+def time_delay_kept(tr: np.ndarray) -> bool:
+    """compute_time_delay_map.py:76-92 (load_trajectories): a photon is kept when it has a clean
+    row and every clean |x|, |y|, |z| < 1e26 m and |eta| < 3e18 s."""
+    if len(tr) == 0:
+        return False
+    return bool(np.max(np.abs(tr[:, 1:4])) < 1e26 and np.max(np.abs(tr[:, 0])) < 3e18)
+
+
+def time_delay(tr: np.ndarray, c: float):
+    """compute_time_delays (compute_time_delay_map.py:244-310) for one clean trajectory:
+    (time_delay, path, chord); zeros below two rows. The path is summed segment by segment in
+    row order from 0.0 (compute_travel_time_deflected, :97-126); the straight path is the
+    chord |x_last - x_first| (compute_travel_time_straight returns the distance it is given)."""
+    if len(tr) < 2:
+        return 0.0, 0.0, 0.0
+    path = 0.0
+    for i in range(len(tr) - 1):
+        d = [float(tr[i + 1, 1 + k]) - float(tr[i, 1 + k]) for k in range(3)]
+        path += math.sqrt(_dot3(d, d))
+    X = [float(tr[-1, 1 + k]) - float(tr[0, 1 + k]) for k in range(3)]
+    chord = math.sqrt(_dot3(X, X))
+    return path / c - chord / c, path, chord
 
 
 def redshift_row(states: np.ndarray, c: float, v_obs=None, v_em=None) -> np.ndarray:
@@ -143,8 +174,10 @@ def redshift_row(states: np.ndarray, c: float, v_obs=None, v_em=None) -> np.ndar
     out = np.zeros(len(COLUMNS))
     tr = clean_rows(states)
     m = len(tr)
-    out[-1] = m
+    out[_C["n_rows"]] = m
     out[6:18] = np.nan
+    out[_C["td_kept"]] = 1.0 if time_delay_kept(tr) else 0.0
+    out[_C["time_delay"]], out[_C["path"]], out[_C["chord"]] = time_delay(tr, c)
     if m >= 1:
         out[10], out[11] = tr[0, 0], tr[-1, 0]
         out[12:15], out[15:18] = tr[0, 1:4], tr[-1, 1:4]

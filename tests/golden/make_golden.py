@@ -697,8 +697,91 @@ def gen_manifest():
             g.write(name + " " + " ".join(argv) + "\n")
 
 
+# ------------------------------------------------------------ time-delay map
+def _time_delay_records(rng, n_photons=36, n_rows=48):
+    """NaN-padded FLRW record blocks [n, rows, 14] in SI units: ragged lengths (0, 1, 2, 3 rows
+    first), a NaN hole, and photons the time-delay loader rejects (a position at 1e26 m, a time at
+    3e18 s, an infinite position) or keeps at the edge (just below both limits)."""
+    rec = np.full((n_photons, n_rows, 14), np.nan)
+    for i in range(n_photons):
+        m = i if i < 4 else (n_rows if i < 10 else int(rng.integers(2, n_rows + 1)))
+        start = rng.uniform(1e24, 2e24, 3)
+        steps = rng.normal(0, 2e20, (m, 3)) + np.array([-1.5e22, 0, 0])
+        rec[i, :m, 0] = 4.6e17 - np.arange(m) * 5e13
+        rec[i, :m, 1:4] = start + np.cumsum(steps, axis=0)
+        rec[i, :m, 4] = -1.0
+        rec[i, :m, 5:8] = np.array([-3e8, 0, 0]) + rng.normal(0, 1e5, 3)
+        rec[i, :m, 8] = 1.0 / (1.0 + np.linspace(0, 0.2, m))
+        rec[i, :m, 9:14] = rng.normal(0, 1e-6, (m, 5))
+        if m > 8 and i % 7 == 0:
+            rec[i, m // 2, 2] = np.nan
+    rec[5, 3, 1] = 1e26
+    rec[6, 2, 0] = 3e18
+    rec[7, 4, 3] = -np.inf
+    rec[8, 1, 2] = np.nextafter(1e26, 0)
+    rec[8, 1, 0] = np.nextafter(3e18, 0)
+    return rec
+
+
+def gen_time_delays():
+    """compute_time_delay_map.py's own loader and compute_time_delays on synthetic record blocks.
+    The module imports h5py and matplotlib at the top (both absent here): stand-in modules serve
+    the blocks as a trajectory file and give matplotlib's names, which these functions never call."""
+    import types
+
+    rec = _time_delay_records(np.random.default_rng(21))
+    files = {"records.h5": rec}
+
+    class _File:
+        def __init__(self, name, mode="r"):
+            self._rec = files[name]
+            self.attrs = {"n_photons": len(self._rec)}
+
+        def __enter__(self):
+            return self
+
+        def __exit__(self, *exc):
+            return False
+
+        def __contains__(self, key):
+            return key.startswith("photon_") and key.endswith("_states")
+
+        def __getitem__(self, key):
+            return self._rec[int(key.split("_")[1])]
+
+    h5 = types.ModuleType("h5py")
+    h5.File = _File
+    mpl = types.ModuleType("matplotlib")
+    plt = types.ModuleType("matplotlib.pyplot")
+    colors = types.ModuleType("matplotlib.colors")
+    colors.TwoSlopeNorm = object
+    mpl.pyplot, mpl.colors = plt, colors
+    saved = {k: sys.modules.get(k) for k in ("h5py", "matplotlib", "matplotlib.pyplot", "matplotlib.colors")}
+    sys.modules.update({"h5py": h5, "matplotlib": mpl, "matplotlib.pyplot": plt, "matplotlib.colors": colors})
+    try:
+        td = _load_file("compute_time_delay_map", "_postprocessing", "compute_time_delay_map.py")
+        import contextlib
+        import io
+
+        with contextlib.redirect_stdout(io.StringIO()):
+            trajs, meta = td.load_trajectories("records.h5")
+        delays, dd, ds, (xp, yp) = td.compute_time_delays(trajs, meta)
+    finally:
+        for k, v in saved.items():
+            if v is None:
+                sys.modules.pop(k, None)
+            else:
+                sys.modules[k] = v
+    # which photons the loader kept, by their first clean row
+    firsts = [t[0] for t in trajs]
+    kept = np.array([any(len(b := r[~np.isnan(r).any(axis=1)]) and np.array_equal(b[0], f) for f in firsts)
+                     for r in rec])
+    save("time_delays.npz", records=rec, kept=kept, time_delays=np.asarray(delays),
+         distances_deflected=np.asarray(dd), distances_straight=np.asarray(ds), x_proj=xp, y_proj=yp)
+
+
 GENERATORS = ["cosmology", "interp", "interp_slow", "rhs", "steps", "integrate", "integrate_modes", "generators",
-              "observables", "cfg2_small", "cfg1", "compare_job", "manifest"]
+              "observables", "cfg2_small", "cfg1", "compare_job", "manifest", "time_delays"]
 
 if __name__ == "__main__":
     if not os.path.isdir(REF):

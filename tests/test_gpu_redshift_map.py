@@ -57,8 +57,54 @@ def test_doppler_matches_oracle(cuda):
         if len(tr) >= 2:
             calls[(i, 0)], calls[(i, 1)] = tr[0, 0], tr[-1, 0]
     got = _table(rec, velocity_func=velocity)
-    ok = want[:, -1] >= 2
+    ok = want[:, O.COLUMNS.index("n_rows")] >= 2
     assert _same(got[ok], want[ok]) and np.any(got[ok, 3] != 0.0)
+
+
+def _golden_time_delays():
+    import os
+
+    return np.load(os.path.join(os.path.dirname(__file__), "golden", "time_delays.npz"))
+
+
+def test_time_delay_columns_match_oracle(cuda):
+    """The whole table, time-delay columns included, on the reference script's golden records:
+    photons the loader drops (1e26 m, 3e18 s, an infinite position) flagged, the one just below
+    both limits kept."""
+    rec = _golden_time_delays()["records"]
+    got, want = _table(rec), O.redshift_rows(rec, c)
+    assert _same(got, want)
+    assert got[:, O.COLUMNS.index("td_kept")].tolist() == _golden_time_delays()["kept"].astype(float).tolist()
+
+
+def test_compute_time_delays_matches_the_reference_script(cuda):
+    """maps.compute_time_delays against compute_time_delay_map.py's own outputs on the same
+    records (tests/golden/time_delays.npz): delays, deflected and straight distances bit for
+    bit; sky positions to CUDA's acos against libm's."""
+    from excalibur_tool_gb300.observables import maps
+
+    g = _golden_time_delays()
+    delays, dd, ds, (x, y) = maps.compute_time_delays(g["records"])
+    assert np.array_equal(delays, g["time_delays"])
+    assert np.array_equal(dd, g["distances_deflected"]) and np.array_equal(ds, g["distances_straight"])
+    th = np.hypot(g["x_proj"], g["y_proj"])
+    tol = 4e-15 * th + 1e-18
+    assert np.all(np.abs(x - g["x_proj"]) <= tol) and np.all(np.abs(y - g["y_proj"]) <= tol)
+
+
+def test_time_delay_depends_on_record_every(cuda):
+    """The recorded path is summed over the rows kept, so thinning the rows (record_every)
+    shortens it toward the chord, as in the reference; one pass (<= 257 rows) and the scratch
+    pass (> 257 rows) give the oracle's values."""
+    rng = np.random.default_rng(16)
+    rec = _records(rng, n_photons=8, n_rows=520, lag=False, lengths=[520] * 8)
+    for every in (1, 2, 4):
+        sub = np.ascontiguousarray(rec[:, ::every])
+        got, want = _table(sub), O.redshift_rows(sub, c)
+        assert _same(got, want), every
+    p1 = _table(rec)[:, O.COLUMNS.index("path")]
+    p4 = _table(np.ascontiguousarray(rec[:, ::4]))[:, O.COLUMNS.index("path")]
+    assert np.all(p4 < p1)
 
 
 def test_runner_trajectories_map(cuda):
@@ -74,7 +120,7 @@ def test_runner_trajectories_map(cuda):
     want = O.redshift_rows(tr, c)
     for k in ("z_H", "z_SW", "z_ISW", "z_D", "z_total"):
         assert np.array_equal(data[k], want[:, O.COLUMNS.index(k)]), k
-    assert np.all(want[:, -1] >= 2) and np.isfinite(data["z_total"]).all()
+    assert np.all(want[:, O.COLUMNS.index("n_rows")] >= 2) and np.isfinite(data["z_total"]).all()
     ox, oy, used = O.sky_positions(tr)
     assert len(x) == used.sum() == len(tr)
     th = np.hypot(ox, oy)
