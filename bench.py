@@ -52,6 +52,9 @@ L2_FLUSH_BYTES = 256 << 20
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--shard", action="store_true",
+                   help="N>1: split one batch of photons across the ranks (strong scaling) instead of a "
+                        "batch per rank (weak scaling); the per-rank results are gathered once after timing")
     p.add_argument("--steps", type=int, default=5)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
@@ -61,9 +64,12 @@ def parse():
     p.add_argument("--side", type=int, default=256, help="directions per side (smaller cases for profiling)")
     p.add_argument("--no-precision", action="store_true", help="skip the 512^3 / 4M-ray precision workload")
     p.add_argument("--precision-side", type=int, default=2048)
+    p.add_argument("--precision-rk45-side", type=int, default=1024,
+                   help="directions per side of the RK45 precision leg (2048: the full 4,194,304 rays)")
     p.add_argument("--no-surrogate", action="store_true", help="skip the learned sky-map leg")
     p.add_argument("--no-batching", action="store_true", help="skip the multi-field RK45 batching leg")
-    p.add_argument("--batching-scale", type=int, default=4, help="run 1/scale of the batching configuration")
+    p.add_argument("--batching-scale", type=int, default=1,
+                   help="run 1/scale of the batching configuration (1: the full 1,048,576 + 16 x 65,536 rays)")
     p.add_argument("--no-sweep", action="store_true", help="skip the comparison-sweep leg")
     p.add_argument("--no-redshift-map", action="store_true",
                    help="skip the redshift-map leg (262,144 recorded 64-row histories)")
@@ -76,6 +82,14 @@ def parse():
                    help="only run the 32-row comparison sweep of the sweep leg once and exit")
     p.add_argument("--profile-redshift-map", type=int, default=0, metavar="N",
                    help="only time the redshift-map kernels on N synthetic 64-row FLRW histories and exit")
+    p.add_argument("--profile-batching", type=int, default=0, metavar="SCALE",
+                   help="only run the multi-field RK45 launch of the batching leg once at 1/SCALE and exit")
+    p.add_argument("--profile-aux", type=int, default=0, metavar="N",
+                   help="only run the auxiliary kernels once on N rays (device photon generation, the lens "
+                        "potential on a 128^3 grid, the surrogate's Born features) and exit")
+    p.add_argument("--profile-rk45-mixed", type=int, default=0, metavar="SIDE",
+                   help="only run the mixed RK45 tracer once on SIDE x SIDE rays of the slow-Interpolator "
+                        "patch (128^3 float32 grid) and exit")
     p.add_argument("--map-side", type=int, default=4096)
     p.add_argument("--train-steps", type=int, default=8000)
     p.add_argument("--smooth-train-steps", type=int, default=12000,
@@ -84,10 +98,26 @@ def parse():
 
 
 # ------------------------------------------------------------------ dist
+def launch_ranks(n):
+    """`--gpus N` run without a launcher (WORLD_SIZE unset): start N ranks of this same command
+    under torch.distributed.run on this node (rendezvous on 127.0.0.1) and return its exit code."""
+    import socket
+
+    with socket.socket() as sk:
+        sk.bind(("127.0.0.1", 0))
+        port = sk.getsockname()[1]
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", f"--nproc-per-node={n}",
+           "--master-addr", "127.0.0.1", "--master-port", str(port), os.path.abspath(__file__), *sys.argv[1:]]
+    return subprocess.call(cmd)
+
+
 def dist_setup(n):
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))
     local = int(os.environ.get("LOCAL_RANK", 0))
+    if n > 1 and world != n:
+        raise SystemExit(f"--gpus {n} but WORLD_SIZE={world}: run under torch.distributed.run with "
+                         f"--nproc-per-node {n}, or without a launcher to have bench.py start the ranks")
     if world > 1:
         import torch.distributed as dist
 
@@ -225,6 +255,14 @@ def run_ours(args, rank, world, local):
     dev = torch.device("cuda", local)
     wl = workloads.flrw_patch(128, args.side, precision=args.precision, device=dev)
     metric, states, cfg = wl.metric, wl.states, wl.cfg
+    n_total = states.shape[0]
+    sharded = args.shard and world > 1
+    if sharded:
+        # strong scaling: this rank traces its contiguous slice of the one batch
+        from excalibur_tool_gb300.distributed import shard_range
+
+        lo, hi = shard_range(n_total, rank, world)
+        states = states[lo:hi].contiguous()
     stream = torch.cuda.current_stream(dev)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
     peaks = measured_peaks(dev)
@@ -259,6 +297,14 @@ def run_ours(args, rank, world, local):
     value = total_steps / dev_s_max
     rays_s = sum_over_ranks(float(rays * args.steps), world, dev) / dev_s_max
     gpu_launches = args.steps                     # one exc_trace kernel per step
+    gathered = None
+    if sharded:
+        # the one collective: the per-photon results, gathered once after the timed region
+        from excalibur_tool_gb300.distributed import gather_rows
+
+        full = gather_rows(res.state, n_total)
+        gathered = {"rows": int(full.shape[0]), "of": n_total,
+                    "all_finite": bool(torch.isfinite(full).all().item())}
 
     # ---- end to end through the public API: host states in, host results out ----
     integ = Integrator(metric, dt=cfg.dt, integrator="rk4", dt_min=cfg.dt_min, dt_max=cfg.dt_max,
@@ -302,18 +348,21 @@ def run_ours(args, rank, world, local):
 
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": dev_s_max * 1e3 / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None,
+            "scaling": "strong" if sharded else "weak", "vs_baseline": None,
             "dtype": {"fp64": "f64", "fp64_fast": "f64", "mixed": "f32+f64"}[args.precision],
             "data": "synthetic (seeded Plummer + Gaussian random field; patch of directions)",
             "config": {"workload": WORKLOAD, "precision": args.precision, "photons": rays,
                        "photon_steps_per_batch": steps_per_batch, "grid": "128^3 float64 (16.8 MB)",
                        "l2": "flushed between timed steps (256 MiB write); grid itself fits in L2",
-                       "parallelism": f"replicas x{world} (independent photon batches)",
+                       "parallelism": (f"sharded x{world} (one batch split by photon index)" if sharded
+                                       else f"replicas x{world} (independent photon batches)"),
                        "status_counts": status_counts},
             "rays_per_s": rays_s, "wall_s_timed": wall,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "api": "Integrator.integrate_batch(pinned host states) -> pinned host results"},
             "gpu_launches": gpu_launches, "roofline": roof, "clocks": clk}
+    if gathered is not None:
+        line["gathered"] = gathered
 
     if not args.no_variants and world == 1:
         line["variants"] = run_variants(args, wl, peaks, dev, stream, value)
@@ -516,7 +565,85 @@ def run_precision(args, dev, stream, flush, fp64_value):
             "fp64_subset_photon_steps_per_s": fp64_ps, "speedup_vs_fp64": mixed_ps / fp64_ps,
             "speedup_vs_fp64_patch_value": mixed_ps / fp64_value,
             "errors_vs_fp64_on_subset": {**err, "subset": "65,536 rays, numpy default_rng(40)"},
-            "host_field_build_s": build_s}
+            "host_field_build_s": build_s,
+            "rk45": run_precision_rk45(args, dev, stream, flush)}
+
+
+def run_precision_rk45(args, dev, stream, flush):
+    """The precision workload with the adaptive stepper its configuration names ("FP64 RK45 error
+    control"): RK45 (Fehlberg, rtol 1e-8, atol 1e-12) through the slow Interpolator's continuous
+    gradient on the 512^3 float32 grid, the box stop on the face; the mixed tracer (FP32 stages,
+    double-float state, FP64 error norm and step control) against the FP64 RK45 parity tracer on
+    a default_rng(40) subset. Rates are RK45 trial steps per second (six RHS evaluations each)."""
+    import dataclasses
+    import torch
+
+    from excalibur_tool_gb300 import _native as N
+    from excalibur_tool_gb300 import workloads
+    from excalibur_tool_gb300.trace import trace_batch
+
+    side = args.precision_rk45_side
+    wl = workloads.flrw_patch_rk45(512, side, 20.0, seed=4, device=dev)
+    n = wl.states.shape[0]
+    cfg = dataclasses.replace(wl.cfg, precision="mixed")
+    r = trace_batch(wl.metric, wl.states, cfg)
+    torch.cuda.synchronize(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    flush.fill_(1.0)
+    e0.record(stream)
+    r = trace_batch(wl.metric, wl.states, cfg)
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    sec = e0.elapsed_time(e1) / 1e3
+    raw = trace_batch(wl.metric, wl.states, dataclasses.replace(cfg, precision="mixed_raw"))
+    torch.cuda.synchronize(dev)
+    back = float((raw.status == N.PH_RETRACE).float().mean())
+    del raw
+    idx = np.sort(np.random.default_rng(40).choice(n, min(65536, n), replace=False))
+    ti = torch.as_tensor(idx, device=dev)
+    sub = wl.states[ti].contiguous()
+    c64 = dataclasses.replace(wl.cfg, precision="fp64")
+    r64 = trace_batch(wl.metric, sub, c64)
+    torch.cuda.synchronize(dev)
+    e0.record(stream)
+    r64 = trace_batch(wl.metric, sub, c64)
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    s64 = e0.elapsed_time(e1) / 1e3
+
+    class _Sub:
+        pass
+
+    rs = _Sub()
+    rs.obs, rs.state, rs.status = r.obs[ti], r.state[ti], r.status[ti]
+    both = (rs.status == N.PH_LEFT_BOX) & (r64.status == N.PH_LEFT_BOX)
+    err = errors_vs(r64, rs, both)
+    # the FP64 tracer's own sensitivity: the same rays with their initial speed changed by 1e-9
+    sub2 = sub.clone()
+    sub2[:, 5:8] *= 1.0 + 1e-9
+    r64b = trace_batch(wl.metric, sub2, c64)
+    torch.cuda.synchronize(dev)
+    both2 = both & (r64b.status == N.PH_LEFT_BOX)
+    sens = errors_vs(r64, r64b, both2)
+    err["rays_compared"] = int(both.sum())
+    err["status_counts_mixed"] = np.bincount(rs.status.cpu().numpy(), minlength=12).tolist()
+    err["status_counts_fp64"] = np.bincount(r64.status.cpu().numpy(), minlength=12).tolist()
+    trials, trials64 = int(r.n_iter.sum()), int(r64.n_iter.sum())
+    mixed_ps, fp64_ps = trials / sec, trials64 / s64
+    return {"workload": f"flrw_patch_rk45_512: {n:,} photons ({side}x{side} directions, 20x20 deg patch), Phi on "
+                        "the 512^3 float32 grid read through the slow Interpolator, RK45 Fehlberg rtol 1e-8 atol "
+                        "1e-12, dt in [1e10 s, 10 Mpc/c], box stop on the face 1.5 cells inside the last node",
+            "precision": "mixed RK45 (FP32 stages, double-float state, FP64 error norm, step control and "
+                         "re-trace of guarded rays)",
+            "rk45_trials_per_s": mixed_ps, "accepted_steps_per_s": int(r.n_steps.sum()) / sec,
+            "rays_per_s": n / sec, "s_per_batch": sec, "retrace_fraction": back,
+            "fp64_subset_rk45_trials_per_s": fp64_ps, "speedup_vs_fp64": mixed_ps / fp64_ps,
+            "trials_per_ray": trials / n, "rejected_fraction": 1 - int(r.n_steps.sum()) / max(1, trials),
+            "errors_vs_fp64_on_subset": {**err, "subset": f"{len(idx):,} rays, numpy default_rng(40); rays that "
+                                                          "left the box in both"},
+            "fp64_own_sensitivity": {**sens, "perturbation": "the FP64 parity tracer on the same rays with the "
+                                     "initial speed scaled by 1 + 1e-9 (RK45 end points are determined to the "
+                                     "method's truncation error: step sequences that part move them by this much)"}}
 
 
 def run_batching(args, dev, stream):
@@ -535,25 +662,24 @@ def run_batching(args, dev, stream):
     tuned = autotune(wl.metric, wl.states, wl.cfg, field_index=wl.field_index, use_cache=False)
     tune_s = time.perf_counter() - t1
     plan = next(iter(tune_report().values()))
-    # one eager launch with the default schedule for comparison
-    r = trace_batch(wl.metric, wl.states, wl.cfg, field_index=wl.field_index)
-    torch.cuda.synchronize(dev)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    r = trace_batch(wl.metric, wl.states, wl.cfg, field_index=wl.field_index)
-    e1.record(stream)
-    torch.cuda.synchronize(dev)
-    default_s = e0.elapsed_time(e1) / 1e3
+    # the tuned plan captured once (its constructor runs the batch eagerly, loading the kernels)
     cap = CapturedTrace(wl.metric, wl.states, tuned, field_index=wl.field_index)
-    cap.run()
     torch.cuda.synchronize(dev)
-    k = 3
+    k = 1 if scale == 1 else 3
     e0.record(stream)
     for _ in range(k):
         out = cap.run()
     e1.record(stream)
     torch.cuda.synchronize(dev)
     graph_s = e0.elapsed_time(e1) / 1e3 / k
+    # one eager launch with the library's default schedule, for comparison
+    e0.record(stream)
+    r = trace_batch(wl.metric, wl.states, wl.cfg, field_index=wl.field_index)
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    default_s = e0.elapsed_time(e1) / 1e3
+    del r
     n = wl.states.shape[0]
     steps = out.n_steps.cpu().numpy()
     iters = out.n_iter.cpu().numpy()
@@ -561,7 +687,16 @@ def run_batching(args, dev, stream):
     fidx = wl.field_index.cpu().numpy()
     sky = fidx == 0
     long = steps[sky][steps[sky] > 1]
-    return {"workload": f"lens alone on a 256^3 float64 grid with {(1 << 20) // scale:,} full-sky rays "
+
+    def dist(v):
+        v = np.asarray(v)
+        if not len(v):
+            return None
+        return {"p05": float(np.percentile(v, 5)), "median": float(np.median(v)), "p95": float(np.percentile(v, 95)),
+                "max": int(v.max()), "rays": int(len(v))}
+
+    return {"configuration": "full configuration" if scale == 1 else f"1/{scale} of the configuration",
+            "workload": f"lens alone on a 256^3 float64 grid with {(1 << 20) // scale:,} full-sky rays "
                         f"(default_rng(3)) + 16 random fields (seeds 1-16; 64^3/128^3/256^3) x "
                         f"{wl.info['patch_photons']:,} patch rays, adaptive RK45 (Fehlberg weights, rtol 1e-8, "
                         "atol 1e-12, dt in [1e10, 1e17] s) to box exit; one launch"
@@ -574,10 +709,9 @@ def run_batching(args, dev, stream):
             "default_schedule_s": default_s, "graph_replay_s": graph_s,
             "rays_per_s": n / graph_s, "accepted_steps_per_s": float(steps.sum()) / graph_s,
             "rk45_trials_per_s": float(iters.sum()) / graph_s,
-            "steps_sky_rays_leaving_forward": {"p05": float(np.percentile(long, 5)), "median": float(np.median(long)),
-                                               "p95": float(np.percentile(long, 95)), "max": int(long.max())}
-            if len(long) else None,
-            "steps_patch_rays_median": float(np.median(steps[~sky])),
+            "accepted_steps": {"sky_rays": dist(steps[sky]), "sky_rays_past_the_first_step": dist(long),
+                               "random_field_rays": dist(steps[~sky])},
+            "tried_steps": {"sky_rays": dist(iters[sky]), "random_field_rays": dist(iters[~sky])},
             "rejected_fraction": float(1 - steps.sum() / max(1, iters.sum())),
             "status_counts": np.bincount(status, minlength=12).tolist(),
             "gpu_launches_per_replay": 1}
@@ -1083,8 +1217,72 @@ def profile_redshift_map(n: int, n_rows: int = 64, reps: int = 5, host_sample: i
             "host_time_delay_photons_per_s": 1.0 / t_host_td, "host_sample": len(sample)}
 
 
+def profile_batching(scale: int) -> dict:
+    """One multi-field RK45 launch of the batching workload at 1/scale (for profiling)."""
+    import torch
+
+    from excalibur_tool_gb300 import workloads
+    from excalibur_tool_gb300.trace import trace_batch
+
+    dev = torch.device("cuda", 0)
+    wl = workloads.multi_field(n_sky=(1 << 20) // scale, n_side=max(8, 256 // int(round(scale ** 0.5))), device=dev)
+    t0 = time.perf_counter()
+    r = trace_batch(wl.metric, wl.states, wl.cfg, field_index=wl.field_index)
+    torch.cuda.synchronize(dev)
+    return {"photons": int(wl.states.shape[0]), "seconds": time.perf_counter() - t0,
+            "rk45_trials": int(r.n_iter.sum()), "accepted": int(r.n_steps.sum())}
+
+
+def profile_rk45_mixed(side: int) -> dict:
+    """The mixed RK45 tracer once on side x side rays of the slow-Interpolator patch over a 128^3
+    float32 grid (for profiling)."""
+    import dataclasses
+    import torch
+
+    from excalibur_tool_gb300 import workloads
+    from excalibur_tool_gb300.trace import trace_batch
+
+    dev = torch.device("cuda", 0)
+    wl = workloads.flrw_patch_rk45(128, side, 20.0, seed=4, device=dev)
+    t0 = time.perf_counter()
+    r = trace_batch(wl.metric, wl.states, dataclasses.replace(wl.cfg, precision="mixed_raw"))
+    torch.cuda.synchronize(dev)
+    return {"photons": int(wl.states.shape[0]), "seconds": time.perf_counter() - t0,
+            "rk45_trials": int(r.n_iter.sum()), "accepted": int(r.n_steps.sum())}
+
+
+def profile_aux(n: int) -> dict:
+    """The auxiliary kernels once each: the device patch generator on n rays, the lens potential
+    written on a 128^3 grid, and the surrogate's Born features on n directions of a 20-degree
+    patch (for profiling)."""
+    import torch
+
+    from excalibur_tool_gb300 import workloads
+    from excalibur_tool_gb300.core.constants import one_Mpc
+    from excalibur_tool_gb300.objects import spherical_mass as SM
+    from excalibur_tool_gb300.photon.photons import Photons
+    from excalibur_tool_gb300.surrogate import sky
+
+    dev = torch.device("cuda", 0)
+    wl = workloads.flrw_patch(128, 8, device=dev)
+    cz = workloads.lcdm()
+    side = int(round(n ** 0.5))
+    ph = Photons(wl.metric)
+    st = ph.device_patch_grid(side, [cz._eta_at_a1, *workloads.OBSERVER], workloads.LENS - workloads.OBSERVER, 10.0)
+    lens = SM.spherical_mass(workloads.LENS_MASS, 5 * one_Mpc, workloads.LENS)
+    pot = lens.potential_grid((128, 128, 128), (workloads.BOX / 128,) * 3, device=dev)
+    patch = sky.Patch(origin=(cz._eta_at_a1, *workloads.OBSERVER),
+                      axis=tuple(workloads.LENS - workloads.OBSERVER), patch_deg=20.0)
+    uv = torch.rand((n, 2), dtype=torch.float64, device=dev) * 2 - 1
+    f = sky.born_features(wl.metric, patch, uv, wl.cfg.stop_box)
+    torch.cuda.synchronize(dev)
+    return {"generated": int(st.shape[0]), "potential_nodes": int(pot.numel()), "born_rows": int(f.shape[0])}
+
+
 def main():
     args = parse()
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        sys.exit(launch_ranks(args.gpus))
     if args.profile_gemm:
         import torch
 
@@ -1110,6 +1308,15 @@ def main():
         return
     if args.profile_redshift_map:
         print(json.dumps(profile_redshift_map(args.profile_redshift_map)), flush=True)
+        return
+    if args.profile_batching:
+        print(json.dumps(profile_batching(args.profile_batching)), flush=True)
+        return
+    if args.profile_aux:
+        print(json.dumps(profile_aux(args.profile_aux)), flush=True)
+        return
+    if args.profile_rk45_mixed:
+        print(json.dumps(profile_rk45_mixed(args.profile_rk45_mixed)), flush=True)
         return
     rank, world, local = dist_setup(args.gpus)
     if args.impl == "reference":

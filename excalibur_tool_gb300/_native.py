@@ -41,7 +41,8 @@ DTYPE_F64, DTYPE_F32, DTYPE_F32X2 = 0, 1, 2
 STEPPER = {"rk4": 0, "rk45": 1, "leapfrog4": 2}
 TABLEAU = {"reference": 0, "fehlberg": 1}
 PRECISION = {"fp64": 0, "fp64_fast": 1, "mixed": 2, "mixed_raw": 3, "retrace": 4}
-STOP_BOX, STOP_A = 1, 2
+STOP_BOX, STOP_A, STOP_FACE = 1, 2, 4
+OPT_RETRACE_COOP, OPT_RAYS_PER_WARP_SHIFT = 1, 8
 OBS_ENDPOINTS, OBS_PATH, OBS_ISW = 1, 2, 4
 OBS_COLS = ["a_obs", "a_em", "phi_obs", "phi_em", "isw_int", "path", "chord", "excess",
             "v0x", "v0y", "v0z", "v1x", "v1y", "v1z", "min_r", "eta_obs", "eta_em"]
@@ -73,7 +74,7 @@ class ExcTraceArgs(C.Structure):
                 ("record_cols", C.c_int32), ("stepper", C.c_int32), ("tableau", C.c_int32),
                 ("precision", C.c_int32), ("renormalize_every", C.c_int32), ("stop_flags", C.c_int32),
                 ("obs_flags", C.c_int32), ("block_size", C.c_int32), ("blocks_per_sm", C.c_int32),
-                ("reserved0", C.c_int32), ("dt", C.c_double), ("dt_min", C.c_double),
+                ("options", C.c_int32), ("dt", C.c_double), ("dt_min", C.c_double),
                 ("dt_max", C.c_double), ("rtol", C.c_double), ("atol", C.c_double),
                 ("max_iter", C.c_int64), ("max_steps", C.c_int64), ("box_lo", C.c_double * 3),
                 ("box_hi", C.c_double * 3), ("a_stop", C.c_double), ("lens_center", C.c_double * 3),

@@ -271,6 +271,23 @@ __device__ __forceinline__ double np_clip(double x, double lo, double hi) {
   return fmin(fmax(x, lo), hi);
 }
 
+// EXC_STOP_FACE (FLRW): the parameter lambda >= 0 at which x + lambda * sign(dt) * u first
+// reaches a face of the stop box; a step that would come within EXC_FACE_MARGIN of it is
+// shortened to end there (`clipped`).
+__device__ __forceinline__ double face_clip(const double s[8], double dt, const double lo[3], const double hi[3],
+                                            bool& clipped) {
+  const double sg = dt < 0.0 ? -1.0 : 1.0;
+  double tmin = INFINITY;
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    const double v = sg * s[5 + d];
+    if (v > 0.0) tmin = fmin(tmin, (hi[d] - s[1 + d]) / v);
+    else if (v < 0.0) tmin = fmin(tmin, (lo[d] - s[1 + d]) / v);
+  }
+  clipped = tmin < EXC_FACE_MARGIN * fabs(dt);
+  return clipped ? sg * fmax(tmin, 0.0) : dt;
+}
+
 // ------------------------------------------------------------- queue
 __device__ __forceinline__ int64_t next_photon(const ExcTraceArgs& A, int64_t& static_next, int64_t stride) {
   if (A.queue == nullptr) {
@@ -422,6 +439,8 @@ __device__ __forceinline__ bool photon_iterate(Tracer<MK, FT>& T, const ExcTrace
   double dt = P.dt;
   if (dt < 0.0) dt = -np_clip(-dt, A.dt_min, A.dt_max);   // integrator.py:358-364
   else dt = np_clip(dt, A.dt_min, A.dt_max);
+  bool face = false;
+  if (is_flrw(MK) && (A.stop_flags & EXC_STOP_FACE)) dt = face_clip(P.s, dt, A.box_lo, A.box_hi, face);
   double ns[8];
   double dt_new = dt;
   bool accepted = true;
@@ -447,7 +466,12 @@ __device__ __forceinline__ bool photon_iterate(Tracer<MK, FT>& T, const ExcTrace
     }
     if (A.obs_flags) photon_accumulate<MK, FT>(T, A, P, s_old0);
     P.steps++;
-    if (A.stop_flags & EXC_STOP_BOX) {
+    if (is_flrw(MK) && (A.stop_flags & EXC_STOP_FACE)) {
+      if (face) {
+        P.status = EXC_PH_LEFT_BOX;
+        stop = true;
+      }
+    } else if (A.stop_flags & EXC_STOP_BOX) {
       double pc[3];
       cart_pos<MK>(T.D.m, P.s, pc);
       if (MK == EXC_METRIC_SCHWARZSCHILD) for (int i = 0; i < 3; ++i) pc[i] += T.D.m.center[i];
@@ -481,10 +505,19 @@ __device__ __forceinline__ int64_t next_work(const DevMetric& D, const ExcTraceA
 
 template <int MK, class FT, int STEPPER, bool REC>
 __global__ void __launch_bounds__(128) trace_kernel(const DevMetric D, const ExcTraceArgs A) {
+  // D.rays_per_warp > 0 (the mixed tracer's re-trace pass): a few rays per warp. GB300's FP64
+  // pipe spends its cycles on each active lane, so 32 rays in one warp share one sub-partition's
+  // pipe and each advances at 1/32 of it; spread over many warps, each ray runs at the latency
+  // of its own chain of FP64 operations.
+  const int rpw = D.rays_per_warp;
+  const int lane = threadIdx.x & 31;
+  if (rpw > 0 && lane >= rpw) return;
+  const int64_t slots = rpw > 0 ? (int64_t)(blockDim.x >> 5) * rpw : (int64_t)blockDim.x;
   Tracer<MK, FT> T(D, A);
   Photon P;
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  int64_t static_next = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t stride = (int64_t)gridDim.x * slots;
+  int64_t static_next = (int64_t)blockIdx.x * slots + (rpw > 0 ? (int64_t)(threadIdx.x >> 5) * rpw + lane
+                                                                 : (int64_t)threadIdx.x);
   const long long t0 = clock64();
   int64_t p = next_work(D, A, static_next, stride);
   bool active = p < A.n_photons;
@@ -523,7 +556,8 @@ cudaError_t launch_trace_t(const DevMetric& D, const ExcTraceArgs& A, LaunchCfg 
     if (per_sm < 1) per_sm = 1;
   }
   int64_t grid = (int64_t)lc.sm_count * per_sm;
-  const int64_t need = (A.n_photons + lc.block - 1) / lc.block;
+  const int64_t per_block = D.rays_per_warp > 0 ? (int64_t)(lc.block / 32) * D.rays_per_warp : lc.block;
+  const int64_t need = (A.n_photons + per_block - 1) / per_block;
   if (grid > need) grid = need;
   if (grid < 1) grid = 1;
   kern<<<(int)grid, lc.block, 0, s>>>(D, A);
@@ -547,8 +581,8 @@ cudaError_t launch_trace_slow(const DevMetric& D, const ExcTraceArgs& A, LaunchC
   if (D.m.fields[0].dtype == EXC_DTYPE_F32) return launch_trace_r<kFlrwSlowInterp, float, STEPPER>(D, A, lc, s);
   if (D.m.fields[0].dtype == EXC_DTYPE_F64) return launch_trace_r<kFlrwSlowInterp, double, STEPPER>(D, A, lc, s);
   if (D.m.fields[0].dtype == EXC_DTYPE_F32X2) {
-    // split grids reach the FP64 tracer only as the mixed tracer's RK4 re-trace pass (fast build)
-    if constexpr (STEPPER == EXC_STEPPER_RK4 && EXC_FAST) {
+    // split grids reach the FP64 tracer only as the mixed tracer's re-trace pass (fast build)
+    if constexpr ((STEPPER == EXC_STEPPER_RK4 || STEPPER == EXC_STEPPER_RK45) && EXC_FAST) {
       if (!A.records) return launch_trace_t<kFlrwSlowInterp, float2, STEPPER, false>(D, A, lc, s);
     }
   }
@@ -570,8 +604,8 @@ cudaError_t launch_trace_stepper(const DevMetric& D, const ExcTraceArgs& A, Laun
   }
   if (D.m.fields[0].dtype == EXC_DTYPE_F32) return launch_trace_r<EXC_METRIC_FLRW, float, STEPPER>(D, A, lc, s);
   if (D.m.fields[0].dtype == EXC_DTYPE_F32X2) {
-    // split grids reach the FP64 tracer only as the mixed tracer's RK4 re-trace pass (fast build)
-    if constexpr (STEPPER == EXC_STEPPER_RK4 && EXC_FAST) {
+    // split grids reach the FP64 tracer only as the mixed tracer's re-trace pass (fast build)
+    if constexpr ((STEPPER == EXC_STEPPER_RK4 || STEPPER == EXC_STEPPER_RK45) && EXC_FAST) {
       if (!A.records) return launch_trace_t<EXC_METRIC_FLRW, float2, STEPPER, false>(D, A, lc, s);
     }
     return cudaErrorInvalidValue;

@@ -33,9 +33,16 @@ constexpr int kThreads = 128;
 // the most rows a history can have for its pair terms (at most (n - 1) / 2) to fit one numpy block
 constexpr int kOnePassRows = 257;
 
+// |v| as an integer: for non-NaN doubles its order is that of the magnitudes. The tests below
+// run on the integer pipe; this kernel is bound by the FP64 pipe (its divisions and square
+// roots), and a floating-point NaN test or maximum per value would take a quarter of it.
+__device__ __forceinline__ unsigned long long abs_bits(double v) {
+  return (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffull;
+}
+
 __device__ __forceinline__ bool row_clean(const double* row, int n_cols) {
   for (int c = 0; c < n_cols; ++c)
-    if (isnan(row[c])) return false;
+    if (abs_bits(row[c]) > 0x7ff0000000000000ull) return false;   // NaN
   return true;
 }
 
@@ -177,14 +184,17 @@ __device__ double simpson(const Clean& cl, int m) {
 // numpy's pairwise sum of a stream of at most 128 terms, fed in order: the first eight seed the
 // eight partial sums, each later complete group of eight adds into them, and the last incomplete
 // group is added in order after the partial sums are combined (fewer than eight terms in all:
-// added in order to -0.0).
+// added in order to -0.0). The pending group shifts through eight registers, so that every
+// index is static (no local-memory array).
 struct PairwiseStream {
   double r[8], g[8];
   int ng, groups;
   __device__ __forceinline__ void init() { ng = 0; groups = 0; }
   __device__ __forceinline__ void push(double t) {
-    g[ng++] = t;
-    if (ng == 8) {
+#pragma unroll
+    for (int j = 0; j < 7; ++j) g[j] = g[j + 1];
+    g[7] = t;
+    if (++ng == 8) {
 #pragma unroll
       for (int j = 0; j < 8; ++j) r[j] = groups ? r[j] + g[j] : g[j];
       ++groups;
@@ -193,7 +203,10 @@ struct PairwiseStream {
   }
   __device__ __forceinline__ double sum() const {
     double res = groups ? ((r[0] + r[1]) + (r[2] + r[3])) + ((r[4] + r[5]) + (r[6] + r[7])) : -0.0;
-    for (int i = 0; i < ng; ++i) res += g[i];
+    // the pending terms are g[8 - ng .. 7], oldest first
+#pragma unroll
+    for (int j = 0; j < 8; ++j)
+      if (j >= 8 - ng) res += g[j];
     return res;
   }
 };
@@ -226,7 +239,12 @@ __global__ void __launch_bounds__(kThreads) record_redshift_kernel(const double*
     // and |eta|, and (one pass) the Simpson pair terms
     int m = 0, first = -1, last = -1;
     double x3[3] = {0.0, 0.0, 0.0}, y3[3] = {0.0, 0.0, 0.0}, prev[3] = {0.0, 0.0, 0.0};
-    double path = 0.0, max_pos = 0.0, max_eta = 0.0;
+    double path = 0.0;
+    // compute_time_delay_map's loader keeps a photon whose clean rows stay below 1e26 m and
+    // 3e18 s (np.max(np.abs(.)) < limit: every value below it; an infinity is not)
+    const unsigned long long pos_lim = (unsigned long long)__double_as_longlong(1e26);
+    const unsigned long long eta_lim = (unsigned long long)__double_as_longlong(3e18);
+    bool below_lim = true;
     PairwiseStream ps;
     ps.init();
     for (int r = 0; r < n_rows; ++r) {
@@ -246,9 +264,9 @@ __global__ void __launch_bounds__(kThreads) record_redshift_kernel(const double*
       }
       for (int k = 0; k < 3; ++k) {
         prev[k] = row[1 + k];
-        max_pos = fmax(max_pos, fabs(row[1 + k]));
+        below_lim = below_lim && abs_bits(row[1 + k]) < pos_lim;
       }
-      max_eta = fmax(max_eta, fabs(row[0]));
+      below_lim = below_lim && abs_bits(row[0]) < eta_lim;
       ++m;
     }
     double* o = out + i * EXC_RS_NCOLS;
@@ -267,8 +285,7 @@ __global__ void __launch_bounds__(kThreads) record_redshift_kernel(const double*
       o[EXC_RS_X_OBS + k] = f[1 + k];
       o[EXC_RS_X_EM + k] = l[1 + k];
     }
-    // compute_time_delay_map's loader keeps a photon whose clean rows stay below 1e26 m and 3e18 s
-    o[EXC_RS_TD_KEPT] = (max_pos < 1e26 && max_eta < 3e18) ? 1.0 : 0.0;
+    o[EXC_RS_TD_KEPT] = below_lim ? 1.0 : 0.0;
     if (m < 2) continue;  // compute_redshift_map and compute_time_delays leave such photons at zero
     {
       double X[3];

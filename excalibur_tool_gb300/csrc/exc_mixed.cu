@@ -102,6 +102,25 @@ struct MixField {
   df inv_s[3];       // 1 / spacing as double-float
   float inv_2s[3];   // 1 / (2 spacing)
   int slow;          // grad_mode EXC_GRAD_TRILINEAR (the slow Interpolator)
+  df box[6];         // stop-box faces in cells of this field (lo xyz, hi xyz), for EXC_STOP_FACE
+};
+
+// Fehlberg 4(5) for the mixed tracer (integrator.py:93-152). With k_j the velocity stage
+// derivatives (K for u^mu) and S_j = sum_l B_jl k_l, stage j's velocity is u + dt S_j and, as
+// x' = u, its point is x + dt c_j u + dt^2 sum_m BB_jm k_m (BB = B.B, c_j = sum_l B_jl). The
+// 5th-order update is x + dt W5 u + dt^2 sum_m CB5_m k_m, u + dt sum_j C5_j k_j (CB5 = C5.B,
+// W5 = sum C5), and y5 - y4 the same with the weight differences dC = C5 - C4 (dW = W5 - 1,
+// the 4th-order weights summing to 1). So the large dt u term is one double-float product and
+// the FP32 stage values enter only the small corrections.
+// Sums of stage values weighted by FP32-rounded coefficients would carry the coefficients'
+// rounding as the same relative bias on every step (the Hubble drag, ~1e-3 of u per step, is
+// nearly the same at every stage), so they are formed about stage 0: sum_j w_j v_j =
+// W v_0 + sum_j w_j (v_j - v_0), W = sum_j w_j kept as hi + lo (W5, and WCB5 = sum CB5).
+struct RKF {
+  float b[6][6], bb[6][6], c[6];
+  float c5[6], dc[6], cb5[6], cbe[6];
+  df w5, wcb5;
+  float dw;
 };
 
 // Constants that multiply every step's background (Hubble) terms are kept as
@@ -116,6 +135,7 @@ struct MixParams {
   df eta_min, inv_eta_step;
   int table_n, table_in_smem;
   float a_stop_f;     // a_stop rounded once on the host (no FP64 conversion in the step loop)
+  RKF rk;
 };
 
 // c * x with c = c.hi + c.lo, rounded once: the FMA adds the small c.lo * x to
@@ -412,7 +432,9 @@ struct MPhoton {
   float lc[3];   // lens centre, cell units
   float box[6];  // stop box, cell units (lo xyz, hi xyz)
   float box_tol; // largest FP32 rounding of the box faces (cells)
-  float wrate[4];  // error-window growth per step: cells of x, y, z; table cells of eta
+  float wrate[4];  // error-window growth: cells of x, y, z and table cells of eta per step
+                   // (RK4), or per unit lambda travelled (RK45)
+  float lam;       // RK45: |lambda| travelled over accepted steps
   df excess;     // sum |dx x e|^2 / (|dx| + dx.e), in x-spacing units
   df path;       // sum |dx|, in x-spacing units
   float min_r2;  // min |x - lens|^2, in x-spacing units squared
@@ -494,10 +516,13 @@ __device__ __forceinline__ void photon_begin(const MixParams& Pm, const ExcTrace
   // axis of the time-delay excess: the unit initial direction, kept as hi + lo
   const double vn = sqrt(s[5] * s[5] + s[6] * s[6] + s[7] * s[7]);
   for (int d = 0; d < 3; ++d) P.e[d] = df_of(vn > 0.0 ? s[5 + d] / vn : 0.0);
-  // error windows grow with the distance travelled: |dt u| per step, in cells of each axis
+  // error windows grow with the distance travelled: |dt u| per step (RK4), |u| per unit
+  // lambda (RK45, whose steps vary), in cells of each axis
+  const double per = A.stepper == EXC_STEPPER_RK45 ? 1.0 : fabs(dt);
   for (int d = 0; d < 3; ++d)
-    P.wrate[d] = (float)(kWinRate * fabs(dt) * vn / f.spacing[d] * (fabs(vn > 0.0 ? s[5 + d] / vn : 0.0) + kWinTrans));
-  P.wrate[3] = m.cosmology != EXC_COSMO_STATIC ? (float)(kWinRate * fabs(dt * s[4]) * Pm.D.i_eta_step) : 0.0f;
+    P.wrate[d] = (float)(kWinRate * per * vn / f.spacing[d] * (fabs(vn > 0.0 ? s[5 + d] / vn : 0.0) + kWinTrans));
+  P.wrate[3] = m.cosmology != EXC_COSMO_STATIC ? (float)(kWinRate * per * fabs(s[4]) * Pm.D.i_eta_step) : 0.0f;
+  P.lam = 0.0f;
   P.excess = {0.0f, 0.0f};
   P.path = {0.0f, 0.0f};
   float r2 = 0.0f;
@@ -519,7 +544,8 @@ __device__ __forceinline__ int df_floor2(df a, float& f, float& l) {
   return (int)fl;
 }
 
-__device__ __forceinline__ void base_stage(const MixParams& Pm, const MPhoton& P, Stage& B) {
+// `n`: the window's growth variable -- accepted steps (RK4) or lambda travelled (RK45).
+__device__ __forceinline__ void base_stage(const MixParams& Pm, const MPhoton& P, Stage& B, float n) {
   B.cx = df_floor2(P.P[0], B.fx, B.lx);
   B.cy = df_floor2(P.P[1], B.fy, B.ly);
   B.cz = df_floor2(P.P[2], B.fz, B.lz);
@@ -532,7 +558,6 @@ __device__ __forceinline__ void base_stage(const MixParams& Pm, const MPhoton& P
     B.le = 0.0f;
   }
   // the base point of step 0 is the initial position itself (no drift yet)
-  const float n = (float)P.steps;
   const float w0 = P.steps > 0 ? kWin0 : 0.0f;
   B.wx = fmaf(n, P.wrate[0], w0);
   B.wy = fmaf(n, P.wrate[1], w0);
@@ -564,13 +589,20 @@ __device__ __forceinline__ void perp_df(const df U[3], const df e[3], float out[
   }
 }
 
+// Step sizes of one step: dt, and for RK4 dt/6 and dt^2/6, as hi + lo pairs.
+struct StepDt {
+  float f;
+  df dt, d6, c6;
+};
+
 // One RK4 step (integrator.py:10-22) in mixed precision. Returns 0 or EXC_PH_*.
 template <bool SLOW>
-__device__ __forceinline__ int step_rk4_mixed(const MixParams& Pm, const float* tab_s, MPhoton& P, const bool obs) {
+__device__ __forceinline__ int step_rk4_mixed(const MixParams& Pm, const float* tab_s, MPhoton& P, const bool obs,
+                                              const StepDt& sd) {
   const MixField& F = field_of(Pm, P.fi);
   Stage B;
-  base_stage(Pm, P, B);
-  const float dt = P.dtf, h = 0.5f * dt;
+  base_stage(Pm, P, B, (float)P.steps);
+  const float dt = sd.f, h = 0.5f * dt;
   const float isx = F.inv_s[0].hi, isy = F.inv_s[1].hi, isz = F.inv_s[2].hi;
   const float ie = Pm.inv_eta_step.hi;
   const float u[4] = {P.U[0].hi, P.U[1].hi, P.U[2].hi, P.U[3].hi};
@@ -593,18 +625,18 @@ __device__ __forceinline__ int step_rk4_mixed(const MixParams& Pm, const float* 
   if (obs) perp_df(&P.U[1], P.e, up);    // perpendicular velocity at the start of the step
   // x' = u: RK4 gives dx = dt u + dt^2/6 (k1 + k2 + k3); u' = k: du = dt/6 (k1 + 2 k2 + 2 k3 + k4)
   // dt/6 and dt^2/6 as hi + lo pairs: they scale every increment (see MixParams)
-  const df d6 = P.d6, c6 = P.c6;
+  const df d6 = sd.d6, c6 = sd.c6;
   // lengths below in units of the x spacing, scaled by the hi + lo reciprocal
   // (cmul): per-photon constants rounded to FP32 would bias every step alike
   const df lunit = F.inv_s[0];
   float dxf[3];
   for (int d = 0; d < 3; ++d) {
     const float corr = cmul(c6, k1[1 + d] + k2[1 + d] + k3[1 + d]);
-    const df inc = df_add_f(df_mul(P.U[1 + d], P.dt), corr);     // metres
+    const df inc = df_add_f(df_mul(P.U[1 + d], sd.dt), corr);     // metres
     dxf[d] = cmul(lunit, inc.hi);
     P.P[d] = df_add(P.P[d], df_mul(inc, F.inv_s[d]));
   }
-  P.eta = df_add(P.eta, df_add_f(df_mul(P.U[0], P.dt), cmul(c6, k1[0] + k2[0] + k3[0])));
+  P.eta = df_add(P.eta, df_add_f(df_mul(P.U[0], sd.dt), cmul(c6, k1[0] + k2[0] + k3[0])));
   P.U[0] = df_add_f(P.U[0], cmul(d6, (k1[0] + k4[0]) + 2.0f * (k2[0] + k3[0])));
   // Spatial velocity: k_s = -(hub_s us_s + L_s) is linear in the stage velocity
   // us_s = u + c_s dt k_(s-1), so the RK4 sum (k1 + 2k2 + 2k3 + k4) equals
@@ -636,7 +668,7 @@ __device__ __forceinline__ int step_rk4_mixed(const MixParams& Pm, const float* 
     for (int d = 0; d < 3; ++d) { w[d] = fmaf(h, q2[d], up[d]); q3[d] = -fmaf(hb3, w[d], Lp[d]); }
     float dperp2 = 0.0f;
     for (int d = 0; d < 3; ++d) {
-      const float dp = cmul(lunit, cmul(P.dt, up[d]) + cmul(c6, q1[d] + q2[d] + q3[d]));
+      const float dp = cmul(lunit, cmul(sd.dt, up[d]) + cmul(c6, q1[d] + q2[d] + q3[d]));
       dperp2 = fmaf(dp, dp, dperp2);
     }
     const float len = sqrtf(fmaf(dxf[0], dxf[0], fmaf(dxf[1], dxf[1], dxf[2] * dxf[2])));
@@ -650,6 +682,222 @@ __device__ __forceinline__ int step_rk4_mixed(const MixParams& Pm, const float* 
     }
     P.min_r2 = fminf(P.min_r2, r2);
   }
+  return 0;
+}
+
+// One RK45Adaptive trial step (integrator.py:93-152) in mixed precision: six FP32 RHS
+// evaluations at the stage points, the 5th-order update on the double-float state, and the
+// error control in FP64 -- the weighted RMS norm of y5 - y4 (tol = atol + rtol max(|y|, |y5|)
+// per component, np.mean over the eight) and the step-size factor 0.9 err^-1/5 (accepted,
+// at most 5) or 0.9 err^-1/4 (rejected, at least 0.1). The components of y5 - y4 are formed
+// from the stage values (the common dt u term cancels exactly), each ratio to its tolerance in
+// FP32. On acceptance the state (and the observables) move; `dt_new` is the next trial step.
+// Returns 0 or EXC_PH_*.
+template <bool SLOW>
+__device__ __forceinline__ int step_rk45_mixed(const MixParams& Pm, const float* tab_s, MPhoton& P, const bool obs,
+                                               const StepDt& sd, const ExcTraceArgs& A, bool& accepted,
+                                               double& dt_new) {
+  const MixField& F = field_of(Pm, P.fi);
+  const RKF& R = Pm.rk;
+  Stage B;
+  base_stage(Pm, P, B, P.lam);
+  const float dt = sd.f, dt2 = dt * dt;
+  const float isx = F.inv_s[0].hi, isy = F.inv_s[1].hi, isz = F.inv_s[2].hi;
+  const float ie = Pm.inv_eta_step.hi;
+  const float u[4] = {P.U[0].hi, P.U[1].hi, P.U[2].hi, P.U[3].hi};
+  float K[6][4];
+  float kE[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+  // C5-weighted sums about stage 0 (RKF): the deviations here, the stage-0 terms added below
+  float k5_0 = 0.0f, Hs = 0.0f, rest[3] = {0.0f, 0.0f, 0.0f};
+  float hb0 = 0.0f, dr0[3] = {0.0f, 0.0f, 0.0f};
+  float up[3] = {0.0f, 0.0f, 0.0f}, Q[6][3], q5[3] = {0.0f, 0.0f, 0.0f}, Lp[3];
+  if (obs) perp_df(&P.U[1], P.e, up);
+#pragma unroll
+  for (int j = 0; j < 6; ++j) {
+    float S[4] = {0.0f, 0.0f, 0.0f, 0.0f}, O[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+#pragma unroll
+    for (int l = 0; l < j; ++l)
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        S[i] = fmaf(R.b[j][l], K[l][i], S[i]);
+        O[i] = fmaf(R.bb[j][l], K[l][i], O[i]);
+      }
+    float us[4], off[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      us[i] = fmaf(dt, S[i], u[i]);
+      off[i] = fmaf(dt * R.c[j], u[i], dt2 * O[i]);
+    }
+    float L[3], hb;
+    const int st = rhs_f32<SLOW>(Pm, F, tab_s, B, off[1] * isx, off[2] * isy, off[3] * isz, off[0] * ie,
+                                 j ? kWin0 : 0.0f, us, K[j], L, hb);
+    if (st) return st;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) kE[i] = fmaf(R.dc[j], K[j][i], kE[i]);
+    // spatial k_j = -(hb_j us_j + L_j) with us_j = u + dt S_j: sum_j C5_j k_j =
+    // -[(sum C5_j hb_j) u + sum_j C5_j (dt hb_j S_j + L_j)], the drag on u a scalar multiple
+    float dr[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) dr[d] = fmaf(dt * hb, S[1 + d], L[d]);
+    if (j == 0) {
+      hb0 = hb;
+#pragma unroll
+      for (int d = 0; d < 3; ++d) dr0[d] = dr[d];
+    } else {
+      k5_0 = fmaf(R.c5[j], K[j][0] - K[0][0], k5_0);
+      Hs = fmaf(R.c5[j], hb - hb0, Hs);
+#pragma unroll
+      for (int d = 0; d < 3; ++d) rest[d] = fmaf(R.c5[j], dr[d] - dr0[d], rest[d]);
+    }
+    if (obs) {
+      // the perpendicular velocity's stage derivatives q_j = -(hb_j w_j + L_perp_j),
+      // w_j = u_perp + dt sum_l B_jl q_l (see step_rk4_mixed)
+      perp(L, P.e, Lp);
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        float w = up[d];
+#pragma unroll
+        for (int l = 0; l < j; ++l) w = fmaf(dt * R.b[j][l], Q[l][d], w);
+        Q[j][d] = -fmaf(hb, w, Lp[d]);
+        q5[d] = fmaf(R.cb5[j], Q[j][d] - Q[0][d], q5[d]);
+      }
+    }
+  }
+  k5_0 += cmul(R.w5, K[0][0]);
+  Hs += cmul(R.w5, hb0);
+#pragma unroll
+  for (int d = 0; d < 3; ++d) rest[d] += cmul(R.w5, dr0[d]);
+  // y5 - y4 per component (SI), and the position / eta corrections of y5
+  float c5x[4], e[8];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    float cb5 = 0.0f, cbe = 0.0f;
+#pragma unroll
+    for (int m = 0; m < 6; ++m) {
+      cb5 = fmaf(R.cb5[m], K[m][i] - K[0][i], cb5);
+      cbe = fmaf(R.cbe[m], K[m][i], cbe);
+    }
+    c5x[i] = cb5 + cmul(R.wcb5, K[0][i]);
+    e[i] = dt * fmaf(R.dw, u[i], dt * cbe);    // x^mu: dt dW u + dt^2 CBE.k
+    e[4 + i] = dt * kE[i];                     // u^mu: dt dC.k
+  }
+  // tolerances atol + rtol max(|s|, |y5|): the state's coordinates in SI (FP32 is ample for a
+  // tolerance), y5 = s + increment
+  const ExcField& f = Pm.D.m.fields[P.fi];
+  double q[8];
+  {
+    const float rt = (float)A.rtol, at = (float)A.atol;
+    float sv[8], yv[8];
+    sv[0] = P.eta.hi;
+    yv[0] = fmaf(dt * R.w5.hi, u[0], dt2 * c5x[0]) + sv[0];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      sv[1 + d] = fmaf(P.P[d].hi, F.s[d], (float)(f.origin[d] - f.shift[d]));
+      yv[1 + d] = fmaf(dt * R.w5.hi, u[1 + d], dt2 * c5x[1 + d]) + sv[1 + d];
+    }
+    sv[4] = u[0];
+    yv[4] = fmaf(dt, k5_0, u[0]);
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      sv[5 + d] = u[1 + d];
+      yv[5 + d] = u[1 + d] - dt * fmaf(Hs, u[1 + d], rest[d]);
+    }
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const float tol = fmaf(rt, fmaxf(fabsf(sv[i]), fabsf(yv[i])), at);
+      const double r = (double)(e[i] / tol);
+      q[i] = r * r;
+    }
+  }
+  // FP64: np.mean of the eight squared ratios (pairwise order), its square root, the factor
+  const double err = sqrt((((q[0] + q[1]) + (q[2] + q[3])) + ((q[4] + q[5]) + (q[6] + q[7]))) * 0.125);
+  const double dtd = dbl(sd.dt);
+  if (!(err <= 1.0)) {
+    accepted = false;
+    // err^-1/4 = 1 / sqrt(sqrt(err)); NaN (a non-finite stage) keeps the step at the 0.1 floor
+    const double g = 0.9 / sqrt(sqrt(err));
+    dt_new = dtd * ((g > 0.1) ? g : 0.1);
+    return 0;
+  }
+  accepted = true;
+  if (err > 0.0) {
+    // err^-1/5: an FP32 estimate finished by one Newton step for g^-5 = err in FP64
+    double g = (double)exp2f(-0.2f * log2f((float)err));
+    const double g2 = g * g;
+    g = g * (1.2 - 0.2 * err * (g2 * g2 * g));
+    g *= 0.9;
+    dt_new = dtd * ((g < 5.0) ? g : 5.0);
+  } else {
+    dt_new = dtd * 5.0;
+  }
+  // the 5th-order update
+  const df dtw5 = df_mul(sd.dt, R.w5), dt2d = df_mul(sd.dt, sd.dt);
+  const df lunit = F.inv_s[0];
+  float dxf[3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    const df inc = df_add_f(df_mul(P.U[1 + d], dtw5), cmul(dt2d, c5x[1 + d]));   // metres
+    dxf[d] = cmul(lunit, inc.hi);
+    P.P[d] = df_add(P.P[d], df_mul(inc, F.inv_s[d]));
+  }
+  P.eta = df_add(P.eta, df_add_f(df_mul(P.U[0], dtw5), cmul(dt2d, c5x[0])));
+  P.U[0] = df_add_f(P.U[0], cmul(sd.dt, k5_0));
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    const df tot = df_add_f(df_mul_f(P.U[1 + d], Hs), rest[d]);
+    const df inc = df_mul(tot, sd.dt);
+    P.U[1 + d] = df_add(P.U[1 + d], {-inc.hi, -inc.lo});
+  }
+  P.lam += fabsf(dt);
+  if (obs) {
+    // perpendicular displacement dt W5 u_perp + dt^2 sum_m CB5_m q_m; then as in step_rk4_mixed
+#pragma unroll
+    for (int d = 0; d < 3; ++d) q5[d] += cmul(R.wcb5, Q[0][d]);
+    float dperp2 = 0.0f;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      const float dp = cmul(lunit, cmul(dtw5, up[d]) + cmul(dt2d, q5[d]));
+      dperp2 = fmaf(dp, dp, dperp2);
+    }
+    const float len = sqrtf(fmaf(dxf[0], dxf[0], fmaf(dxf[1], dxf[1], dxf[2] * dxf[2])));
+    const float par = fmaf(dxf[0], P.e[0].hi, fmaf(dxf[1], P.e[1].hi, dxf[2] * P.e[2].hi));
+    P.excess = df_add_f(P.excess, par > 0.0f ? dperp2 / (len + par) : len - par);
+    P.path = df_add_f(P.path, len);
+    float r2 = 0.0f;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      const float r = ((P.P[d].hi - P.lc[d]) + P.P[d].lo) * (F.s[d] * lunit.hi);
+      r2 = fmaf(r, r, r2);
+    }
+    P.min_r2 = fminf(P.min_r2, r2);
+  }
+  return 0;
+}
+
+// Integrator._renormalize_state_to_null (integrator.py:298-335) in FP64 at the double-float
+// state: u^0 from g00 u0^2 + g_ij u^i u^j = 0 (the metric is diagonal), the root nearer the
+// current u^0; left alone when |g00| < 1e-300 or the discriminant is negative.
+template <bool SLOW>
+__device__ __forceinline__ int renormalize_f64(const MixParams& Pm, MPhoton& P) {
+  const ExcField& f = Pm.D.m.fields[P.fi];
+  double x[4], g[4];
+  x[0] = dbl(P.eta);
+  for (int d = 0; d < 3; ++d) x[1 + d] = (f.origin[d] + dbl(P.P[d]) * f.spacing[d]) - f.shift[d];
+  int st;
+  if (f.dtype == EXC_DTYPE_F32) st = exc_mixed_f64::metric_diag<float, SLOW>(Pm.D, P.fi, x, g);
+  else if (f.dtype == EXC_DTYPE_F32X2) st = exc_mixed_f64::metric_diag<float2, SLOW>(Pm.D, P.fi, x, g);
+  else st = exc_mixed_f64::metric_diag<double, SLOW>(Pm.D, P.fi, x, g);
+  if (st) return st;
+  const double u1 = dbl(P.U[1]), u2 = dbl(P.U[2]), u3 = dbl(P.U[3]);
+  const double Acoef = g[0];
+  const double Ccoef = u1 * (g[1] * u1) + u2 * (g[2] * u2) + u3 * (g[3] * u3);
+  if (fabs(Acoef) < 1e-300) return 0;
+  const double disc = -4.0 * Acoef * Ccoef;
+  if (disc < 0.0) return 0;
+  const double sq = sqrt(disc);
+  const double ua = sq / (2.0 * Acoef), ub = -sq / (2.0 * Acoef);
+  const double cur = dbl(P.U[0]);
+  P.U[0] = df_of((fabs(ua - cur) <= fabs(ub - cur)) ? ua : ub);
   return 0;
 }
 
@@ -713,22 +961,70 @@ __device__ __forceinline__ void photon_finish(const MixParams& Pm, const ExcTrac
 __device__ __forceinline__ bool df_ge(df a, float b) { return a.hi > b || (a.hi == b && a.lo >= 0.0f); }
 __device__ __forceinline__ bool df_lt(df a, float b) { return a.hi < b || (a.hi == b && a.lo < 0.0f); }
 
+// EXC_STOP_FACE: the parameter at which the position reaches a face of the stop box along the
+// current velocity (cells of the field, faces as hi + lo pairs); a step that would come within
+// EXC_FACE_MARGIN of it is shortened to end there. Returns whether it was.
+__device__ __forceinline__ bool face_step(const MixParams& Pm, const MPhoton& P, StepDt& sd) {
+  const MixField& F = field_of(Pm, P.fi);
+  const float sg = sd.f < 0.0f ? -1.0f : 1.0f;
+  float tmin = INFINITY;
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    const float v = sg * P.U[1 + d].hi * F.inv_s[d].hi;   // cells per unit lambda
+    if (v > 0.0f) tmin = fminf(tmin, ((F.box[3 + d].hi - P.P[d].hi) + (F.box[3 + d].lo - P.P[d].lo)) / v);
+    else if (v < 0.0f) tmin = fminf(tmin, ((F.box[d].hi - P.P[d].hi) + (F.box[d].lo - P.P[d].lo)) / v);
+  }
+  if (!(tmin < (float)EXC_FACE_MARGIN * fabsf(sd.f))) return false;
+  const double t = (double)(sg * fmaxf(tmin, 0.0f));
+  sd.f = (float)t;
+  sd.dt = df_of(t);
+  sd.d6 = df_of(t / 6.0);
+  sd.c6 = df_of(t * t / 6.0);
+  return true;
+}
+
 // One iteration of the integrate_single loop (integrator.py:347-400) + stops.
-template <bool SLOW>
+template <bool SLOW, bool RK45>
 __device__ __forceinline__ bool photon_iterate(const MixParams& Pm, const float* tab_s, const ExcTraceArgs& A,
                                                MPhoton& P) {
   if (P.status >= 0) return true;    // set at begin (bad field index)
   if (P.it >= A.max_iter) { P.status = EXC_PH_MAX_ITER; return true; }
   if (P.steps >= A.max_steps) { P.status = EXC_PH_STEPS; return true; }
-  const int st = step_rk4_mixed<SLOW>(Pm, tab_s, P, A.obs_flags != 0);
+  if (RK45) {
+    // the reference clips |dt| into [dt_min, dt_max] every iteration (integrator.py:358-364)
+    double dt = dbl(P.dt);
+    const double adt = fmin(fmax(fabs(dt), A.dt_min), A.dt_max);
+    dt = dt < 0.0 ? -adt : adt;
+    P.dt = df_of(dt);
+    P.dtf = (float)dt;
+  }
+  StepDt sd{P.dtf, P.dt, P.d6, P.c6};
+  const bool face_mode = (A.stop_flags & EXC_STOP_FACE) != 0;
+  const bool face = face_mode && face_step(Pm, P, sd);
+  bool accepted = true;
+  double dt_new = 0.0;
+  const int st = RK45 ? step_rk45_mixed<SLOW>(Pm, tab_s, P, A.obs_flags != 0, sd, A, accepted, dt_new)
+                      : step_rk4_mixed<SLOW>(Pm, tab_s, P, A.obs_flags != 0, sd);
   if (st) { P.status = st; return true; }
+  if (RK45) {
+    P.dt = df_of(dt_new);
+    P.dtf = (float)dt_new;
+  }
+  if (!accepted) { P.it++; return false; }
+  if (A.renormalize_every && (P.steps % A.renormalize_every) == 0) {
+    const int rs = renormalize_f64<SLOW>(Pm, P);
+    if (rs) { P.status = rs; return true; }
+  }
   if (!isfinite(P.U[0].hi) || !isfinite(P.P[0].hi) || !isfinite(P.P[1].hi) || !isfinite(P.P[2].hi)) {
     P.status = EXC_PH_NONFINITE;
     return true;
   }
   P.steps++;
   P.it++;
-  if (A.stop_flags & EXC_STOP_BOX) {
+  if (face_mode) {
+    // the box stop lands on the face: no other box test, so no window about the faces
+    if (face) { P.status = EXC_PH_LEFT_BOX; return true; }
+  } else if (A.stop_flags & EXC_STOP_BOX) {
     bool in = true, near = false;
     const float n = (float)P.steps;
     for (int d = 0; d < 3; ++d) {
@@ -742,7 +1038,7 @@ __device__ __forceinline__ bool photon_iterate(const MixParams& Pm, const float*
   }
   if (A.stop_flags & EXC_STOP_A) {
     Stage B;
-    base_stage(Pm, P, B);
+    base_stage(Pm, P, B, RK45 ? P.lam : (float)P.steps);
     float a, aa, r2;
     cosmo_f32(Pm, tab_s, B.ce, B.fe, a, aa, r2);
     // FP32 a(eta) carries ~3e-7 relative error; within a guard band of a_stop the
@@ -767,7 +1063,7 @@ __device__ __forceinline__ bool photon_iterate(const MixParams& Pm, const float*
 // MINB = 4: capped at 128 registers (a few spills to L1) for four blocks per SM.
 // SLOW: the launch has a slow-Interpolator field (a separate instantiation, so
 // the base-node kernels keep their register allocation).
-template <int MINB, bool SLOW>
+template <int MINB, bool SLOW, bool RK45>
 __global__ void __launch_bounds__(128, MINB) trace_mixed_kernel(const MixParams Pm, const ExcTraceArgs A) {
   extern __shared__ float tab_s[];
   if (Pm.table_in_smem) {
@@ -782,7 +1078,7 @@ __global__ void __launch_bounds__(128, MINB) trace_mixed_kernel(const MixParams 
   bool active = p < A.n_photons;
   if (active) photon_begin(Pm, A, P, p);
   while (active) {
-    bool done = photon_iterate<SLOW>(Pm, tab_s, A, P);
+    bool done = photon_iterate<SLOW, RK45>(Pm, tab_s, A, P);
     if (!done && (P.it & 63) == 0) {
       if (A.abort_flag && *(volatile const int32_t*)A.abort_flag) { P.status = EXC_PH_ABORTED; done = true; }
       else if (A.deadline_cycles > 0 && clock64() - t0 > A.deadline_cycles) { P.status = EXC_PH_TIMED_OUT; done = true; }
@@ -800,9 +1096,8 @@ __global__ void __launch_bounds__(128, MINB) trace_mixed_kernel(const MixParams 
 // ------------------------------------------------------------- host side
 int check(const DevMetric& D, const ExcTraceArgs& A) {
   if (D.m.kind != EXC_METRIC_FLRW) return 1;
-  if (A.stepper != EXC_STEPPER_RK4) return 2;
+  if (A.stepper != EXC_STEPPER_RK4 && A.stepper != EXC_STEPPER_RK45) return 2;
   if (A.records) return 3;
-  if (A.renormalize_every) return 4;
   for (int i = 0; i < D.m.n_fields; ++i) {
     if (D.m.fields[i].ndim != 3) return 5;
     if (D.m.fields[i].grad_mode != EXC_GRAD_BASE_NODE && D.m.fields[i].grad_mode != EXC_GRAD_TRILINEAR) return 8;
@@ -816,9 +1111,8 @@ int check(const DevMetric& D, const ExcTraceArgs& A) {
 const char* why(int code) {
   switch (code) {
     case 1: return "mixed precision supports the FLRW metric only";
-    case 2: return "mixed precision supports the RK4 stepper only";
+    case 2: return "mixed precision supports the RK4 and RK45 steppers only";
     case 3: return "mixed precision does not record trajectories";
-    case 4: return "mixed precision does not renormalise the null condition";
     case 5: return "mixed precision supports 3-D (static) potential grids only";
     case 6: return "mixed precision needs grids below 2^31 nodes";
     case 7: return "mixed precision has no ISW accumulator (static grids only)";
@@ -873,13 +1167,65 @@ cudaError_t trace(const DevMetric& D, const ExcTraceArgs& A, int block, int bloc
     smem = (size_t)m.a_table_n * sizeof(float);
   }
   P->a_stop_f = (float)A.a_stop;
+  // stop-box faces in each field's cells, as the photons' positions are kept
+  for (int i = 0; i < m.n_fields; ++i) {
+    const ExcField& f = m.fields[i];
+    for (int d = 0; d < 3; ++d) {
+      P->mf[i].box[d] = df_host(((A.box_lo[d] + f.shift[d]) - f.origin[d]) / f.spacing[d]);
+      P->mf[i].box[3 + d] = df_host(((A.box_hi[d] + f.shift[d]) - f.origin[d]) / f.spacing[d]);
+    }
+  }
+  if (A.stepper == EXC_STEPPER_RK45) {
+    // Fehlberg's nodes and 4th-order weights; the 5th-order weights of the reference (665/1287
+    // for the third) or Fehlberg's (6656/12825), integrator.py:106-115
+    const double b[6][6] = {{0, 0, 0, 0, 0, 0},
+                            {1.0 / 4.0, 0, 0, 0, 0, 0},
+                            {3.0 / 32.0, 9.0 / 32.0, 0, 0, 0, 0},
+                            {1932.0 / 2197.0, -7200.0 / 2197.0, 7296.0 / 2197.0, 0, 0, 0},
+                            {439.0 / 216.0, -8.0, 3680.0 / 513.0, -845.0 / 4104.0, 0, 0},
+                            {-8.0 / 27.0, 2.0, -3544.0 / 2565.0, 1859.0 / 4104.0, -11.0 / 40.0, 0}};
+    const double c5[6] = {16.0 / 135.0, 0.0,
+                          A.tableau == EXC_TABLEAU_FEHLBERG ? 6656.0 / 12825.0 : 665.0 / 1287.0,
+                          28561.0 / 56430.0, -9.0 / 50.0, 2.0 / 55.0};
+    const double c4[6] = {25.0 / 216.0, 0.0, 1408.0 / 2565.0, 2197.0 / 4104.0, -1.0 / 5.0, 0.0};
+    RKF& R = P->rk;
+    double w5 = 0.0;
+    for (int j = 0; j < 6; ++j) {
+      double cj = 0.0, cb5 = 0.0, cbe = 0.0;
+      for (int l = 0; l < 6; ++l) {
+        R.b[j][l] = (float)b[j][l];
+        double bb = 0.0;
+        for (int q = 0; q < 6; ++q) bb += b[j][q] * b[q][l];
+        R.bb[j][l] = (float)bb;
+        cj += b[j][l];
+        cb5 += c5[l] * b[l][j];
+        cbe += (c5[l] - c4[l]) * b[l][j];
+      }
+      R.c[j] = (float)cj;
+      R.c5[j] = (float)c5[j];
+      R.dc[j] = (float)(c5[j] - c4[j]);
+      R.cb5[j] = (float)cb5;
+      R.cbe[j] = (float)cbe;
+      w5 += c5[j];
+    }
+    R.w5 = df_host(w5);
+    double wcb5 = 0.0;
+    for (int m = 0; m < 6; ++m)
+      for (int l = 0; l < 6; ++l) wcb5 += c5[l] * b[l][m];
+    R.wcb5 = df_host(wcb5);
+    // the 4th-order weights sum to 1: dW is the 5th-order sum's departure from it
+    R.dw = (float)(A.tableau == EXC_TABLEAU_FEHLBERG ? 0.0 : 665.0 / 1287.0 - 6656.0 / 12825.0);
+  }
   int per_sm = blocks_per_sm;
   // a plan with four or more resident blocks per SM takes the 128-register build
   bool slow = false;
   for (int i = 0; i < m.n_fields; ++i) slow = slow || P->mf[i].slow;
+  const bool rk45 = A.stepper == EXC_STEPPER_RK45;
   void (*kern)(const MixParams, const ExcTraceArgs) =
-      slow ? (per_sm >= 4 ? trace_mixed_kernel<4, true> : trace_mixed_kernel<1, true>)
-           : (per_sm >= 4 ? trace_mixed_kernel<4, false> : trace_mixed_kernel<1, false>);
+      rk45 ? (slow ? (per_sm >= 4 ? trace_mixed_kernel<4, true, true> : trace_mixed_kernel<1, true, true>)
+                   : (per_sm >= 4 ? trace_mixed_kernel<4, false, true> : trace_mixed_kernel<1, false, true>))
+           : (slow ? (per_sm >= 4 ? trace_mixed_kernel<4, true, false> : trace_mixed_kernel<1, true, false>)
+                   : (per_sm >= 4 ? trace_mixed_kernel<4, false, false> : trace_mixed_kernel<1, false, false>));
   cudaError_t e = cudaSuccess;
   if (per_sm <= 0) {
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, block, smem);

@@ -38,6 +38,7 @@ class TraceConfig:
     max_iter: int = 10_000
     max_steps: int = 100             # the "steps" stop value
     stop_box: Optional[tuple] = None  # ((lo_x, lo_y, lo_z), (hi_x, hi_y, hi_z)): stop on exit
+    stop_face: bool = False           # with stop_box (FLRW): the last step is shortened to end on the face
     a_stop: Optional[float] = None   # stop once a(eta) <= a_stop (FLRW)
     renormalize_every: int = 0
     record_every: Optional[int] = None   # None = no records; else reference semantics
@@ -49,6 +50,8 @@ class TraceConfig:
     blocks_per_sm: int = 0
     use_queue: bool = True
     deadline_cycles: int = 0
+    retrace_coop: bool = False        # mixed: the FP64 re-trace with eight lanes per ray
+    retrace_rays_per_warp: int = 0    # mixed: rays per warp of the one-thread FP64 re-trace (0 = library default)
 
     def validate(self):
         if self.stepper not in N.STEPPER:
@@ -65,6 +68,8 @@ class TraceConfig:
             raise ValueError("max_iter and max_steps must be >= 0")
         if not math.isfinite(self.dt):
             raise ValueError("dt must be finite")
+        if self.stop_face and self.stop_box is None:
+            raise ValueError("stop_face needs stop_box")
         return self
 
 
@@ -234,6 +239,8 @@ def _make_args(desc, res, cfg: TraceConfig, queue=None, abort_flag=None) -> N.Ex
         for i in range(3):
             a.box_lo[i] = float(lo[i])
             a.box_hi[i] = float(hi[i])
+        if cfg.stop_face:
+            flags |= N.STOP_FACE
     if cfg.a_stop is not None:
         flags |= N.STOP_A
         a.a_stop = float(cfg.a_stop)
@@ -253,6 +260,8 @@ def _make_args(desc, res, cfg: TraceConfig, queue=None, abort_flag=None) -> N.Ex
     a.queue = queue.data_ptr() if queue is not None else None
     a.abort_flag = abort_flag.data_ptr() if abort_flag is not None else None
     a.deadline_cycles = int(cfg.deadline_cycles)
+    a.options = (N.OPT_RETRACE_COOP if cfg.retrace_coop else 0) | \
+        ((int(cfg.retrace_rays_per_warp) & 0xff) << N.OPT_RAYS_PER_WARP_SHIFT)
     return a
 
 

@@ -82,6 +82,37 @@ def flrw_patch(n_grid=128, n_side=256, patch_deg=10.0, seed=2, field_dtype=np.fl
     return Workload(f"flrw_patch_{n_grid}", metric, states.to(device), cfg, info)
 
 
+def flrw_patch_rk45(n_grid=512, n_side=2048, patch_deg=20.0, seed=4, field_dtype=np.float32, precision="fp64",
+                    rtol=1e-8, atol=1e-12, dt_min=1e10, dt_max=20 * DLAMBDA, device="cuda"):
+    """The precision workload traced with the adaptive stepper: the patch of flrw_patch read
+    through the reference's slow Interpolator (grid/interpolator.py: its gradient, the trilinear
+    blend of corner differences, is continuous across cell faces; the base-node gradient of
+    InterpolatorFast jumps at every face, where an adaptive step shrinks to its floor), RK45 with
+    Fehlberg's weights at rtol / atol, the step free in [dt_min, dt_max], and the box stop landing
+    on the face (stop_face), so that the end point does not depend on the step sequence. The slow
+    class reads no further than its last node: the box ends 1.5 cells inside it."""
+    import torch
+
+    from .grid.interpolator import Interpolator
+
+    cz = lcdm()
+    phi = lens_plus_grf(n_grid, BOX, LENS_MASS, 5 * one_Mpc, LENS, seed=seed, dtype=field_dtype)
+    grid = Grid((n_grid,) * 3, (BOX / n_grid,) * 3, (0.0, 0.0, 0.0))
+    grid.add_field("Phi", phi)
+    metric = PerturbedFLRWMetricFast(cz.a_of_eta, grid, Interpolator(grid), adot_of_eta=cz.adot_of_eta)
+    ph = Photons(metric)
+    states = ph.generate_patch_grid(n_side, [cz._eta_at_a1, *OBSERVER], LENS - OBSERVER, patch_deg)
+    hi = (n_grid - 1.5) * BOX / n_grid
+    cfg = TraceConfig(stepper="rk45", tableau="fehlberg", rtol=rtol, atol=atol, precision=precision, dt=DLAMBDA,
+                      dt_min=dt_min, dt_max=dt_max, max_steps=2 ** 62, max_iter=100_000,
+                      stop_box=((0, 0, 0), (hi, hi, hi)), stop_face=True, a_stop=0.5, lens_center=tuple(LENS))
+    info = {"grid": f"{n_grid}^3 {np.dtype(field_dtype).name}", "photons": n_side * n_side, "patch_deg": patch_deg,
+            "seed": seed, "grid_bytes": int(phi.nbytes), "interpolator": "slow Interpolator (trilinear gradient)",
+            "stepper": f"RK45 Fehlberg rtol {rtol:g} atol {atol:g}, dt in [{dt_min:g}, {dt_max:g}] s",
+            "stop": f"box face at {hi / one_Mpc:.2f} Mpc"}
+    return Workload(f"flrw_patch_rk45_{n_grid}", metric, states.to(device), cfg, info)
+
+
 def lens_cone(n_theta=32, n_phi=32, cone_deg=5.0, n_steps=2000, precision="fp64", device="cuda"):
     from .core.coordinates import cartesian_to_spherical
 

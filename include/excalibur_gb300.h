@@ -103,7 +103,9 @@ enum { EXC_TABLEAU_REFERENCE = 0, EXC_TABLEAU_FEHLBERG = 1 };
  * MIXED:     FP32 RHS + interpolation, double-float (hi + lo FP32) state; rays
  *            that come within the error window of a discontinuity of the
  *            reference's RHS are re-traced by the FAST FP64 tracer in a second
- *            launch on the same stream (FLRW, RK4, no records).
+ *            launch on the same stream (FLRW, RK4 or RK45, no records). RK45:
+ *            the error norm and step-size control in FP64, the null-condition
+ *            renormalisation in FP64.
  * MIXED_RAW: the mixed launch alone; such rays end with EXC_PH_RETRACE.
  * RETRACE:   the second launch alone: the FAST FP64 tracer over the photons
  *            whose status is EXC_PH_RETRACE (the others are not touched), so a
@@ -115,6 +117,26 @@ enum { EXC_PREC_FP64_EXACT = 0, EXC_PREC_FP64_FAST = 1, EXC_PREC_MIXED = 2, EXC_
 /* stop_flags bits (the "steps" stop and max_iter always apply) */
 #define EXC_STOP_BOX   1
 #define EXC_STOP_A     2
+/* With EXC_STOP_BOX, FLRW: the box stop lands on the face. Before each trial step the
+ * distance to the box along the current velocity is taken; when the step would reach
+ * within EXC_FACE_MARGIN of a face (lambda_face < margin * |dt|, dt after the reference's
+ * [dt_min, dt_max] clip), the step is shortened to end on it and the photon ends
+ * (EXC_PH_LEFT_BOX) once that step is accepted; no other box test is made. The end point is
+ * then a smooth function of the initial direction, whatever the step sequence (the first
+ * step past the face, the default, moves in whole steps as the direction changes). Not in
+ * the reference, which has no box stop. */
+#define EXC_STOP_FACE  4
+#define EXC_FACE_MARGIN 1.05
+
+/* options: the mixed tracer's FP64 re-trace pass (fast FP64 build). By default one thread per
+ * ray, EXC_RETRACE_RAYS_PER_WARP rays per warp (GB300's FP64 pipe spends its cycles on each
+ * active lane, so few rays per warp, spread over every SM sub-partition, each run at the
+ * latency of its own FP64 chain); bits 8-15 set another count (1..32; 32 = every lane). With
+ * EXC_OPT_RETRACE_COOP, eight lanes per ray share each ray's right-hand side instead (FLRW,
+ * RK4, 3-D base-node fields; otherwise the one-thread pass). */
+#define EXC_OPT_RETRACE_COOP 1
+#define EXC_OPT_RAYS_PER_WARP_SHIFT 8
+#define EXC_RETRACE_RAYS_PER_WARP 1
 
 /* obs_flags bits */
 #define EXC_OBS_ENDPOINTS 1   /* a, Phi at both ends; deflection; min_r */
@@ -199,11 +221,11 @@ typedef struct ExcTraceArgs {
   int32_t obs_flags;             /* EXC_OBS_* bits */
   int32_t block_size;            /* 0 = library default */
   int32_t blocks_per_sm;         /* 0 = library default */
-  int32_t reserved0;
+  int32_t options;               /* EXC_OPT_* bits (0 = library defaults) */
   double dt, dt_min, dt_max, rtol, atol;
   int64_t max_iter;              /* reference: 10000 */
   int64_t max_steps;             /* "steps" stop value */
-  double box_lo[3], box_hi[3];   /* EXC_STOP_BOX: keep while lo <= x < hi */
+  double box_lo[3], box_hi[3];   /* EXC_STOP_BOX: keep while lo <= x < hi (EXC_STOP_FACE: end on a face) */
   double a_stop;                 /* EXC_STOP_A: stop once a <= a_stop */
   double lens_center[3];         /* cartesian centre for min_r (FLRW) */
   uint32_t* queue;               /* device scratch >= 2 uint32, zeroed by the call;

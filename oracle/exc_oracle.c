@@ -737,6 +737,20 @@ static double clip(double x, double lo, double hi) {
   return fmin(fmax(x, lo), hi);
 }
 
+/* EXC_STOP_FACE (FLRW): lambda >= 0 at which x + lambda * sign(dt) * u first reaches a face of
+ * the stop box; a step that would come within EXC_FACE_MARGIN of it ends there instead. */
+static double face_clip(const double* s, double dt, const double* lo, const double* hi, int* clipped) {
+  const double sg = dt < 0.0 ? -1.0 : 1.0;
+  double tmin = INFINITY;
+  for (int d = 0; d < 3; ++d) {
+    const double v = sg * s[5 + d];
+    if (v > 0.0) tmin = fmin(tmin, (hi[d] - s[1 + d]) / v);
+    else if (v < 0.0) tmin = fmin(tmin, (lo[d] - s[1 + d]) / v);
+  }
+  *clipped = tmin < EXC_FACE_MARGIN * fabs(dt);
+  return *clipped ? sg * fmax(tmin, 0.0) : dt;
+}
+
 /* Integrator.integrate_single, integrator.py:218-409, plus the box / a stops
  * and the in-place observables the GPU kernel accumulates. */
 static void trace_one(const ExcMetric* m, const ExcTraceArgs* A, int64_t p) {
@@ -767,6 +781,9 @@ static void trace_one(const ExcMetric* m, const ExcTraceArgs* A, int64_t p) {
     if (it >= A->max_iter) { status = EXC_PH_MAX_ITER; break; }
     if (steps >= A->max_steps) { status = EXC_PH_STEPS; break; }
     dt = dt < 0 ? -clip(-dt, A->dt_min, A->dt_max) : clip(dt, A->dt_min, A->dt_max);
+    int face = 0;
+    const int face_mode = m->kind == EXC_METRIC_FLRW && (A->stop_flags & EXC_STOP_FACE);
+    if (face_mode) dt = face_clip(s, dt, A->box_lo, A->box_hi, &face);
     double dt_new = dt;
     int accepted = 1, st;
     if (A->stepper == EXC_STEPPER_RK4) st = step_rk4(m, fi, s, dt, ns);
@@ -803,7 +820,12 @@ static void trace_one(const ExcMetric* m, const ExcTraceArgs* A, int64_t p) {
         memcpy(pprev, pc, sizeof(pc));
       }
       steps++;
-      if (A->stop_flags & EXC_STOP_BOX) {
+      if (face_mode) {
+        if (face) {
+          status = EXC_PH_LEFT_BOX;
+          stop = 1;
+        }
+      } else if (A->stop_flags & EXC_STOP_BOX) {
         double pc[3];
         cart_pos(m, s, pc);
         if (m->kind == EXC_METRIC_SCHWARZSCHILD)

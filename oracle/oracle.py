@@ -257,6 +257,8 @@ def trace(st: Spacetime, states, cfg, field_index=None, threads=1):
         flags |= N.STOP_BOX
         for i in range(3):
             a.box_lo[i], a.box_hi[i] = float(cfg.stop_box[0][i]), float(cfg.stop_box[1][i])
+        if getattr(cfg, "stop_face", False):
+            flags |= N.STOP_FACE
     if cfg.a_stop is not None:
         flags |= N.STOP_A
         a.a_stop = float(cfg.a_stop)

@@ -96,9 +96,8 @@ def test_split_grids_only_for_the_mixed_tracer(lib):
 
 
 @pytest.mark.parametrize("kw,msg", [
-    (dict(stepper=N.STEPPER["rk45"]), b"RK4 stepper only"),
+    (dict(stepper=N.STEPPER["leapfrog4"]), b"RK4 and RK45 steppers only"),
     (dict(records=4096, n_records=4096, max_records=2, record_cols=14), b"record"),
-    (dict(renormalize_every=3), b"renormalise"),
     (dict(obs=4096, obs_flags=N.OBS_ISW), b"ISW"),
 ])
 def test_mixed_rejects_what_it_does_not_implement(lib, kw, msg):

@@ -145,6 +145,37 @@ def test_mixed_raw_hands_back_untouched_rays(patch):
     assert rel_err(mixed["state"][back], o.state[back]).max() <= 1e-12
 
 
+def test_retrace_schedules_agree(patch):
+    """The FP64 re-trace pass three ways: one thread per ray with one ray per warp (the default),
+    with every lane of a warp busy, and with eight lanes sharing each ray (EXC_OPT_RETRACE_COOP).
+    The one-thread schedules give the same bits; the eight-lane pass sums in another order and
+    agrees to the last digits; all are within 1e-12 of the oracle on the handed-back rays."""
+    import torch
+    from excalibur_tool_gb300.trace import trace_batch
+
+    wl, states, o = patch
+    res = {}
+    for name, kw in (("sparse", {}), ("full", {"retrace_rays_per_warp": 32}), ("coop", {"retrace_coop": True})):
+        r = trace_batch(wl.metric, wl.states, dataclasses.replace(wl.cfg, precision="mixed", **kw))
+        torch.cuda.synchronize()
+        res[name] = {k: getattr(r, k).cpu().numpy() for k in ("state", "status", "n_steps", "obs")}
+    raw = _run(wl, "mixed_raw")
+    back = raw["status"] == N.PH_RETRACE
+    a, b, c = res["sparse"], res["full"], res["coop"]
+    for k in ("state", "status", "n_steps", "obs"):
+        assert np.array_equal(a[k], b[k], equal_nan=True), k
+    assert np.array_equal(a["status"], c["status"]) and np.array_equal(a["n_steps"], c["n_steps"])
+    for k in ("state", "obs"):
+        assert np.array_equal(a[k][~back], c[k][~back], equal_nan=True), k
+    assert rel_err(c["state"][back], a["state"][back]).max() <= 1e-13
+    assert rel_err(c["state"][back], o.state[back]).max() <= 1e-12
+    for col in ("a_em", "path", "chord", "min_r", "v1x"):
+        i = N.OBS_COLS.index(col)
+        assert rel_err(c["obs"][back, i], a["obs"][back, i]).max() <= 1e-12, col
+    i = N.OBS_COLS.index("phi_em")     # Phi near its zero crossings: an absolute floor
+    assert (np.abs(c["obs"][back, i] - a["obs"][back, i]) <= 1e-12 * np.abs(a["obs"][:, i]).max()).all()
+
+
 def test_pipelined_batches_match_single_launches(patch):
     """Re-traces overlapped on a side stream give the same photons as precision "mixed"."""
     import torch
@@ -179,3 +210,96 @@ def test_mixed_slow_interpolator_matches_fp64_oracle(cuda, n_grid, side):
     o = O.trace(spec, st, dataclasses.replace(cfg, precision="fp64"), threads=8)
     assert (o.status == N.PH_LEFT_BOX).all()
     _check_observables(r, o)
+
+
+def _rk45_face_case(n_grid, side, renormalize_every=0):
+    """The patch through the slow Interpolator (continuous gradient) with adaptive RK45
+    (Fehlberg, rtol 1e-8, atol 1e-12, dt in [1e10 s, 10 Mpc / c]) and the box stop on the face,
+    1.5 cells inside the last node (the slow class's bounds)."""
+    from excalibur_tool_gb300.core.constants import one_Mpc
+
+    spec, st, cfg = _cfg2_like(n_grid, side)
+    spec.fields[0].gradient = "trilinear"
+    hi = (n_grid - 1.5) * 1000 * one_Mpc / n_grid
+    cfg = dataclasses.replace(cfg, stepper="rk45", tableau="fehlberg", rtol=1e-8, atol=1e-12, dt_min=1e10,
+                              dt_max=20 * cfg.dt, max_iter=20000, stop_box=((0, 0, 0), (hi, hi, hi)),
+                              stop_face=True, renormalize_every=renormalize_every)
+    return spec, st, cfg
+
+
+def _deviations(r_obs, o_obs, ok):
+    z = np.abs(L.redshift_total(r_obs)[ok] - L.redshift_total(o_obs)[ok])
+    t0 = L.time_delay_excess(o_obs)[ok]
+    t = np.abs(L.time_delay_excess(r_obs)[ok] - t0) / np.abs(t0)
+    a = np.abs(L.deflection_angle(r_obs)[ok] - L.deflection_angle(o_obs)[ok])
+    return {"dz": z, "tau": t, "alpha": a}
+
+
+def _check_within_conditioning(r, spec, st, cfg):
+    """Adaptive RK45 end points are determined only to the method's truncation error: two step
+    sequences that part in their last digits (an error estimate a little above or below 1) end
+    with redshifts ~1e-6 apart at rtol 1e-8 on these fields, and the FP64 parity tracer's own
+    result moves by as much when its initial speed changes by one part in 1e9 (the FP64 fast
+    build, another sum order, moves by as much too). So the mixed tracer is held to that band:
+    against the oracle's FP64 RK45 (the parity tracer's arithmetic), its deviation in z, time
+    delay and deflection is at most 3x the oracle's own deviation under the 1e-9 speed change
+    at the largest ray and 5x at the median (with floors at the RK4 bounds). Both end every ray
+    on the box face."""
+    o = O.trace(spec, st, cfg, threads=8)
+    st2 = st.copy()
+    st2[:, 5:8] *= 1.0 + 1e-9
+    o2 = O.trace(spec, st2, cfg, threads=8)
+    assert (o.status == N.PH_LEFT_BOX).all() and (o2.status == N.PH_LEFT_BOX).all()
+    assert np.array_equal(r["status"], o.status)
+    ok = np.ones(len(st), bool)
+    mix, ref = _deviations(r["obs"], o.obs, ok), _deviations(o2.obs, o.obs, ok)
+    floor = {"dz": DZ_MAX, "tau": TAU_REL_MAX, "alpha": DEFL_ABS}
+    for k in mix:
+        assert mix[k].max() <= 3.0 * ref[k].max() + floor[k], (k, mix[k].max(), ref[k].max())
+        assert np.median(mix[k]) <= 5.0 * np.median(ref[k]) + floor[k], (k, np.median(mix[k]), np.median(ref[k]))
+    return o
+
+
+@pytest.mark.parametrize("n_grid,side", [(32, 12), (128, 12)])
+def test_mixed_rk45_within_the_fp64_tracers_conditioning(cuda, n_grid, side):
+    """Mixed-precision RK45 (FP32 stages, double-float state, FP64 error norm and step control)
+    against the oracle's FP64 RK45 on the same face-stopped patch, within the band that the FP64
+    tracer's own sensitivity sets (_check_within_conditioning)."""
+    spec, st, cfg = _rk45_face_case(n_grid, side)
+    r = gpu_trace(spec, st, dataclasses.replace(cfg, precision="mixed"))
+    o = _check_within_conditioning(r, spec, st, cfg)
+    # the adaptive steps: as many as the FP64 tracer takes, within a few per cent
+    assert abs(int(r["n_steps"].sum()) - int(o.n_steps.sum())) <= 0.05 * int(o.n_steps.sum())
+
+
+def test_mixed_renormalisation_matches_fp64_oracle(cuda):
+    """The null-condition renormalisation (integrator.py:298-335), in FP64 inside the mixed
+    tracer: every 10 accepted steps with RK4 (base-node field) within the RK4 bounds of the
+    oracle's FP64 renormalised trace; every step with RK45 (slow Interpolator) within the FP64
+    tracer's conditioning band.
+
+    The reference's FLRW equations do not keep the null condition (u^0 drifts from -1.00 to
+    about -1.24 across the patch while |u|/c grows to 1.49), so each renormalisation moves u^0
+    by a finite amount, and with RK45 "every N accepted steps" falls where each tracer's step
+    sequence puts it."""
+    spec, st, cfg = _cfg2_like(32, 8)
+    cfg = dataclasses.replace(cfg, renormalize_every=10)
+    r = gpu_trace(spec, st, dataclasses.replace(cfg, precision="mixed"))
+    o = O.trace(spec, st, cfg, threads=8)
+    _check_observables(r, o)
+    spec, st, cfg = _rk45_face_case(32, 8, renormalize_every=1)
+    r = gpu_trace(spec, st, dataclasses.replace(cfg, precision="mixed"))
+    _check_within_conditioning(r, spec, st, cfg)
+
+
+def test_mixed_rk45_retraces_only_near_the_outer_cells(cuda):
+    """With the slow Interpolator the mixed RK45 tracer hands back only rays whose stage points
+    come within the error window of the grid's outer cells (none on this patch), and those it
+    keeps equal what precision "mixed" returns."""
+    spec, st, cfg = _rk45_face_case(32, 12)
+    raw = gpu_trace(spec, st, dataclasses.replace(cfg, precision="mixed_raw"))
+    mixed = gpu_trace(spec, st, dataclasses.replace(cfg, precision="mixed"))
+    back = raw["status"] == N.PH_RETRACE
+    assert back.mean() < 0.05
+    for k in ("state", "status", "n_steps", "obs"):
+        assert np.array_equal(raw[k][~back], mixed[k][~back], equal_nan=True), k

@@ -309,6 +309,36 @@ def test_cfg2_patch_subset_matches_oracle(cuda):
     _assert_matches_oracle(r, spec, st, cfg, 1e-12)
 
 
+@pytest.mark.parametrize("stepper,gradient", [("rk4", "base_node"), ("rk45", "trilinear")])
+def test_box_face_stop_matches_oracle(cuda, stepper, gradient):
+    """stop_face: the last step shortened to end on the box face. The FP64 tracer equals the
+    oracle's face stop bit for bit (states, statuses, step counts, observables), and every ray
+    ends within a small fraction of a step of a face (the shortened step is aimed along the
+    velocity; the trajectory's curvature over that step is what remains)."""
+    import dataclasses
+
+    from excalibur_tool_gb300.core.constants import one_Mpc
+
+    spec, st, cfg = _cfg2_like(32, 8)
+    spec.fields[0].gradient = gradient
+    hi = 1000 * one_Mpc if gradient == "base_node" else 29.5 * 1000 * one_Mpc / 32   # slow class: inside its nodes
+    kw = dict(stop_face=True, stop_box=((0.0, 0.0, 0.0), (hi, hi, hi)))
+    if stepper == "rk45":
+        kw.update(stepper="rk45", tableau="fehlberg", rtol=1e-8, atol=1e-12, dt_min=1e10, dt_max=20 * cfg.dt,
+                  max_iter=20000)
+    cfg = dataclasses.replace(cfg, **kw)
+    r = gpu_trace(spec, st, cfg)
+    with O.power_mode("dd"):
+        od = O.trace(spec, st, cfg, threads=8)
+    for k in ("status", "n_steps", "n_iter", "state"):
+        assert np.array_equal(r[k], getattr(od, k)), k
+    assert np.array_equal(r["obs"], od.obs, equal_nan=True)
+    assert (r["status"] == N.PH_LEFT_BOX).all()
+    x = r["state"][:, 1:4]
+    to_face = np.minimum(x, hi - x).min(axis=1)
+    assert np.abs(to_face).max() <= (1e-3 if stepper == "rk4" else 0.05) * one_Mpc
+
+
 def test_cfg2_grid128_fast_build_matches_oracle(cuda):
     import dataclasses
 

@@ -54,6 +54,61 @@ def test_gradients_match_autograd(cuda):
         assert abs(float(buf["loss"][e]) / (B * 4) - float(loss)) <= 1e-3 * float(loss)
 
 
+def test_gradients_match_fp64_cpu_reference(cuda):
+    """One forward/backward of the project's kernels against the FP64 CPU reference
+    (oracle/surrogate_ref.py) of the same network, on the kernels' own bf16 features.
+
+    Tolerances, from what bf16 storage and fp32 sums leave: the reference rounds to bf16 at
+    the kernels' storage points (Z, H, dZ) and is otherwise exact, so the kernels differ from it
+    by their fp32 accumulation (~1e-6 relative per sum) and by the bf16 roundings that this moves
+    across a midpoint (about 2e-6 / 2^-8 = 3e-4 of the stored values, each by one bf16 ulp,
+    2^-8). Over a weight gradient (a sum of 512 products) that is well under 2e-3 of its norm;
+    a wrong bias, SiLU-derivative or head term is off by O(1). Against the exact-arithmetic
+    gradient (no bf16 rounding), storage alone puts the kernels ~2^-8 away, so the bf16
+    reference must be the much closer of the two."""
+    import torch
+    from excalibur_tool_gb300.surrogate.model import SkySurrogate
+    from oracle import surrogate_ref as R
+
+    torch.manual_seed(0)
+    m = SkySurrogate(n_members=2, seed=3)
+    for b in m.b:
+        b.copy_(torch.randn_like(b) * 0.1)
+    m.b_head.copy_(torch.randn_like(m.b_head) * 0.1)
+    B = 512
+    rng = np.random.default_rng(0)
+    uv = torch.as_tensor(rng.uniform(-1, 1, (B, 2)), device="cuda")
+    t = torch.randn(B, 4, device="cuda")
+    buf = m._buffers(B, 4)
+    m.forward_backward(uv, t, buf)
+    x0 = m._features(uv, B).double().cpu().numpy()
+    torch.cuda.synchronize()
+    # the features: bf16 of the float64 formula, but where the fp32 phase (k u rounded to fp32,
+    # ~1.2e-5 absolute in sin for k = 64) moves a value across a bf16 rounding midpoint
+    f64 = R.features(uv.cpu().numpy(), m.nf)
+    mism = x0 != R.bf16_round(f64)
+    assert mism.mean() < 1e-2 and np.all(np.abs(x0 - f64) <= 2.0 ** -8 * np.abs(f64) + 3e-5)
+    tt = t.double().cpu().numpy()
+    for e in range(m.E):
+        W = [m.wb[l][e].double().cpu().numpy() for l in range(m.depth)]
+        bb = [m.b[l][e].double().cpu().numpy() for l in range(m.depth)]
+        Wh, bh = m.w_head[e].double().cpu().numpy(), m.b_head[e].double().cpu().numpy()
+        ref = R.forward_backward(x0, W, bb, Wh, bh, tt, bf16=True)
+        exact = R.forward_backward(x0, W, bb, Wh, bh, tt, bf16=False)
+        got = {"gw": [buf["gw"][l][e].double().cpu().numpy() for l in range(m.depth)],
+               "gb": [buf["gb"][l][e].double().cpu().numpy() for l in range(m.depth)],
+               "gwh": buf["gwh"][e].double().cpu().numpy(), "gbh": buf["gbh"][e].double().cpu().numpy()}
+        pairs = [(got["gw"][l], ref["gw"][l], exact["gw"][l], f"gw{l}") for l in range(m.depth)] + \
+                [(got["gb"][l], ref["gb"][l], exact["gb"][l], f"gb{l}") for l in range(m.depth)] + \
+                [(got["gwh"], ref["gwh"], exact["gwh"], "gwh"), (got["gbh"], ref["gbh"], exact["gbh"], "gbh")]
+        for g, r, x, name in pairs:
+            rel = np.linalg.norm(g - r) / np.linalg.norm(r)
+            rel_exact = np.linalg.norm(g - x) / np.linalg.norm(x)
+            assert rel <= 2e-3, (e, name, rel)
+            assert rel <= 0.5 * rel_exact or rel <= 1e-5, (e, name, rel, rel_exact)
+        assert abs(float(buf["loss"][e]) - ref["loss"]) <= 1e-5 * ref["loss"]
+
+
 def test_graphed_training_equals_eager(cuda):
     """Training steps replayed from a captured CUDA graph (one multi-tensor Adam launch reading
     the step's schedule on the device) follow the eager loop (same batches, per-tensor Adam
