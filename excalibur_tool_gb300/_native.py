@@ -42,7 +42,6 @@ STEPPER = {"rk4": 0, "rk45": 1, "leapfrog4": 2}
 TABLEAU = {"reference": 0, "fehlberg": 1}
 PRECISION = {"fp64": 0, "fp64_fast": 1, "mixed": 2, "mixed_raw": 3, "retrace": 4}
 STOP_BOX, STOP_A, STOP_FACE = 1, 2, 4
-OPT_RETRACE_COOP, OPT_RAYS_PER_WARP_SHIFT = 1, 8
 OBS_ENDPOINTS, OBS_PATH, OBS_ISW = 1, 2, 4
 OBS_COLS = ["a_obs", "a_em", "phi_obs", "phi_em", "isw_int", "path", "chord", "excess",
             "v0x", "v0y", "v0z", "v1x", "v1y", "v1z", "min_r", "eta_obs", "eta_em"]
@@ -74,7 +73,7 @@ class ExcTraceArgs(C.Structure):
                 ("record_cols", C.c_int32), ("stepper", C.c_int32), ("tableau", C.c_int32),
                 ("precision", C.c_int32), ("renormalize_every", C.c_int32), ("stop_flags", C.c_int32),
                 ("obs_flags", C.c_int32), ("block_size", C.c_int32), ("blocks_per_sm", C.c_int32),
-                ("options", C.c_int32), ("dt", C.c_double), ("dt_min", C.c_double),
+                ("reserved0", C.c_int32), ("dt", C.c_double), ("dt_min", C.c_double),
                 ("dt_max", C.c_double), ("rtol", C.c_double), ("atol", C.c_double),
                 ("max_iter", C.c_int64), ("max_steps", C.c_int64), ("box_lo", C.c_double * 3),
                 ("box_hi", C.c_double * 3), ("a_stop", C.c_double), ("lens_center", C.c_double * 3),
@@ -112,6 +111,12 @@ class ExcGemm(C.Structure):
 
 
 EPI_F32, EPI_BIAS_SILU, EPI_DSILU, EPI_SPLITK = 0, 1, 2, 3
+
+
+class ExcMlpInfer(C.Structure):
+    _fields_ = [("x", C.c_void_p), ("w", C.c_void_p), ("b", C.c_void_p), ("w_head", C.c_void_p),
+                ("b_head", C.c_void_p), ("y", C.c_void_p), ("m", C.c_int64), ("width", C.c_int32),
+                ("n_members", C.c_int32), ("n_out", C.c_int32), ("depth", C.c_int32)]
 
 
 class ExcBornArgs(C.Structure):
@@ -164,6 +169,7 @@ EXPORTS = {
                               _V]),
     # surrogate kernels (include/excalibur_mlp.h)
     "exc_gemm_bf16": (C.c_int, [C.POINTER(ExcGemm), _V]),
+    "exc_mlp_infer": (C.c_int, [C.POINTER(ExcMlpInfer), _V]),
     "exc_mlp_features": (C.c_int, [_V, C.c_int64, C.c_int64, C.c_int32, C.POINTER(C.c_double),
                                    C.POINTER(C.c_double), _V, _V]),
     "exc_mlp_head": (C.c_int, [_V, C.c_int64, C.c_int32, C.c_int32, C.c_int32, _V, _V, _V, _V, _V, _V, _V,

@@ -27,7 +27,6 @@ UNITS = {
     **{f"exc_exact_{s}_slow.cu": ["--fmad=false"] for s in ("rk4", "rk45", "lf4")},
     **{f"exc_fast_{s}_slow.cu": ["--fmad=true"] for s in ("rk4", "rk45", "lf4")},
     "exc_mixed.cu": ["--fmad=true"],
-    "exc_coop.cu": ["--fmad=true"],
     "exc_capi.cu": [],
     "exc_noalloc.cu": [],
     "exc_mlp.cu": [],

@@ -12,7 +12,6 @@
 #include <mutex>
 
 #include "exc_dispatch.h"
-#include "exc_coop.h"
 #include "exc_mixed.h"
 
 namespace {
@@ -214,19 +213,7 @@ int exc_trace(const ExcMetric* metric, const ExcTraceArgs* a, void* stream) {
         if (ce != cudaSuccess) return cuda_fail(ce, "queue reset");
       }
       D.retrace_only = 1;
-      if ((a->options & EXC_OPT_RETRACE_COOP) && exc_coop::supports(D, *a)) {
-        ce = exc_coop::retrace(D, *a, sms, s);
-      } else {
-        int rpw = (a->options >> EXC_OPT_RAYS_PER_WARP_SHIFT) & 0xff;
-        if (rpw <= 0) rpw = EXC_RETRACE_RAYS_PER_WARP;
-        if (rpw >= 32) {
-          ce = exc_fast::trace(D, *a, block, a->blocks_per_sm, sms, s);
-        } else {
-          // one-warp blocks, eight per SM: two warps per sub-partition
-          D.rays_per_warp = rpw;
-          ce = exc_fast::trace(D, *a, 32, 8, sms, s);
-        }
-      }
+      ce = exc_fast::trace(D, *a, block, a->blocks_per_sm, sms, s);
       if (ce != cudaSuccess) return cuda_fail(ce, "re-trace launch");
     }
     return EXC_SUCCESS;

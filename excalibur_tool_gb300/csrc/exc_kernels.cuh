@@ -505,19 +505,10 @@ __device__ __forceinline__ int64_t next_work(const DevMetric& D, const ExcTraceA
 
 template <int MK, class FT, int STEPPER, bool REC>
 __global__ void __launch_bounds__(128) trace_kernel(const DevMetric D, const ExcTraceArgs A) {
-  // D.rays_per_warp > 0 (the mixed tracer's re-trace pass): a few rays per warp. GB300's FP64
-  // pipe spends its cycles on each active lane, so 32 rays in one warp share one sub-partition's
-  // pipe and each advances at 1/32 of it; spread over many warps, each ray runs at the latency
-  // of its own chain of FP64 operations.
-  const int rpw = D.rays_per_warp;
-  const int lane = threadIdx.x & 31;
-  if (rpw > 0 && lane >= rpw) return;
-  const int64_t slots = rpw > 0 ? (int64_t)(blockDim.x >> 5) * rpw : (int64_t)blockDim.x;
   Tracer<MK, FT> T(D, A);
   Photon P;
-  const int64_t stride = (int64_t)gridDim.x * slots;
-  int64_t static_next = (int64_t)blockIdx.x * slots + (rpw > 0 ? (int64_t)(threadIdx.x >> 5) * rpw + lane
-                                                                 : (int64_t)threadIdx.x);
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  int64_t static_next = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const long long t0 = clock64();
   int64_t p = next_work(D, A, static_next, stride);
   bool active = p < A.n_photons;
@@ -556,8 +547,7 @@ cudaError_t launch_trace_t(const DevMetric& D, const ExcTraceArgs& A, LaunchCfg 
     if (per_sm < 1) per_sm = 1;
   }
   int64_t grid = (int64_t)lc.sm_count * per_sm;
-  const int64_t per_block = D.rays_per_warp > 0 ? (int64_t)(lc.block / 32) * D.rays_per_warp : lc.block;
-  const int64_t need = (A.n_photons + per_block - 1) / per_block;
+  const int64_t need = (A.n_photons + lc.block - 1) / lc.block;
   if (grid > need) grid = need;
   if (grid < 1) grid = 1;
   kern<<<(int)grid, lc.block, 0, s>>>(D, A);

@@ -388,6 +388,247 @@ __global__ void features_kernel(const double* dirs, int64_t n, int64_t n_pad, in
   }
 }
 
+// ------------------------------------------------------------ fused inference
+// The ensemble's forward pass for prediction (exc_mlp_infer): one persistent CTA per SM. A
+// 128-row tile of Fourier features is loaded once with TMA and stays in shared memory; for
+// every member the hidden layers run on it back to back -- tcgen05.mma of the 128 x 256
+// activations against the layer's 256 x 256 weights (64-wide K chunks streamed through a
+// two-stage TMA ring) into a 256-column TMEM accumulator, then an epilogue that adds the bias,
+// applies SiLU and rounds to BF16 exactly as the layer-by-layer kernel stores its outputs, and
+// writes the result back into shared memory in the 128-byte-swizzled K-major layout that TMA
+// would have produced (16-byte unit u of row r of a chunk at unit u ^ (r % 8)), where the next
+// layer's MMAs read it. The last layer's epilogue forms the linear head in FP32 registers.
+// Activations never leave the SM: per row, HBM sees the 512 B of features and the outputs.
+//
+// Warps 0-7 are the epilogue (warp w reads TMEM lanes 32 (w % 4) .. and columns 128 (w / 4) ..);
+// warp 8 lane 0 streams the weight chunks; warp 9 lane 0 issues the MMAs and loads each tile's
+// features once the last member's first-layer MMAs of the previous tile have completed. Three
+// mbarriers order them besides the weight ring: `fbar` (features landed), `mdone` (a layer's
+// MMAs completed: epilogue may read TMEM) and `hready` (the epilogue has read TMEM and written
+// the activations: the next layer may start). Every wait is bounded, as in the GEMM.
+constexpr int kInferEpiWarps = 8;
+constexpr int kInferThreads = (kInferEpiWarps + 2) * 32;
+constexpr int kActBytes = 4 * kStageA;                           // 128 x 256 BF16 in 4 K chunks
+constexpr int kInferSmem = 2 * kActBytes + 2 * kStageB + 1024;   // features, hidden, 2 weight stages
+constexpr int kInferMaxOut = 8;
+
+struct InferParams {
+  const float* b;        // [depth][E][256]
+  const float* w_head;   // [E][n_out][256]
+  const float* b_head;   // [E][n_out]
+  float* y;              // [E][m][n_out]
+  int64_t m;
+  int n_members, n_out, depth;
+};
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+// a bounded wait on an mbarrier phase, uniform across the warp (every lane leaves together, so
+// the warp-aligned tcgen05.ld that follows runs on all 32 lanes); false when it gave up
+__device__ __forceinline__ bool warp_wait(uint64_t* bar, uint32_t parity, volatile int* lost) {
+  for (long long w = 0; w < kSpinLimit; ++w) {
+    if (__all_sync(0xffffffffu, mbar_try_wait(bar, parity))) return true;
+    if (__any_sync(0xffffffffu, *lost != 0)) return false;
+  }
+  return false;
+}
+
+__global__ void __launch_bounds__(kInferThreads, 1) mlp_infer_kernel(const __grid_constant__ CUtensorMap tmX,
+                                                                     const __grid_constant__ CUtensorMap tmW,
+                                                                     const InferParams P) {
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
+  uint8_t* sF = smem;                    // features of the tile
+  uint8_t* sH = smem + kActBytes;        // hidden activations (overwritten layer after layer)
+  uint8_t* sW = smem + 2 * kActBytes;    // weight stages
+  __shared__ uint64_t full[2], empty[2], fbar, mdone, hready, ybar;
+  __shared__ uint32_t tmem_base;
+  __shared__ int lost;
+  __shared__ float ypart[kTileM][kInferMaxOut];   // the head's partial sums of the upper 128 columns
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t n_tiles = (P.m + kTileM - 1) / kTileM;
+  const int E = P.n_members, depth = P.depth;
+  const int my_tiles = (int64_t)blockIdx.x < n_tiles ? (int)((n_tiles - 1 - blockIdx.x) / gridDim.x + 1) : 0;
+  if (warp == 0) {
+    tmem_alloc(&tmem_base, kTmemCols);
+    tmem_relinquish();
+  }
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < 2; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    mbar_init(&fbar, 1);
+    mbar_init(&mdone, 1);
+    mbar_init(&hready, kInferEpiWarps * 32);
+    mbar_init(&ybar, kInferEpiWarps * 16);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    lost = 0;
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = tmem_base;
+  volatile int* vlost = &lost;
+
+  if (warp == kInferEpiWarps) {
+    // weight producer: chunks in the order the issuer consumes them
+    if (lane == 0) {
+      int64_t i = 0;   // chunks issued
+      for (int t = 0; t < my_tiles && !*vlost; ++t)
+        for (int e = 0; e < E && !*vlost; ++e)
+          for (int l = 0; l < depth && !*vlost; ++l)
+            for (int kc = 0; kc < 4; ++kc) {
+              const int s = (int)(i & 1);
+              if (i >= 2 && !mbar_wait(&empty[s], (uint32_t)(((i >> 1) - 1) & 1))) {
+                atomicOr(&lost, 1);
+                break;
+              }
+              mbar_expect_tx(&full[s], (uint32_t)kStageB);
+              tma_load_3d(sW + s * kStageB, &tmW, kc * kChunkK, 0, l * E + e, &full[s]);
+              ++i;
+            }
+      // before the CTA can end, the copies it issued have landed (bounded; immediate when the
+      // issuer consumed them)
+      for (int64_t j = i - 2 > 0 ? i - 2 : 0; j < i; ++j) mbar_wait(&full[j & 1], (uint32_t)((j >> 1) & 1));
+    }
+  } else if (warp == kInferEpiWarps + 1) {
+    // MMA issuer (and the features of each tile)
+    if (lane == 0 && my_tiles > 0) {
+      const uint32_t idesc = idesc_bf16_f32(kTileM, 256);
+      int f_issued = 0;
+      auto load_features = [&](int t) {
+        ++f_issued;
+        const int64_t tile = (int64_t)blockIdx.x + (int64_t)t * gridDim.x;
+        mbar_expect_tx(&fbar, (uint32_t)kActBytes);
+        for (int kc = 0; kc < 4; ++kc) tma_load_3d(sF + kc * kStageA, &tmX, kc * kChunkK, (int)(tile * kTileM), 0, &fbar);
+      };
+      load_features(0);
+      int64_t i = 0, layer = 0;
+      bool f_pending = false, ok = true;
+      for (int t = 0; t < my_tiles && ok; ++t) {
+        if (f_pending) {
+          // the features buffer is free once the previous tile's last first layer has been read
+          if (!mbar_wait(&hready, (uint32_t)((layer - 1) & 1))) { ok = false; break; }
+          load_features(t);
+          f_pending = false;
+        }
+        if (!mbar_wait(&fbar, (uint32_t)(t & 1))) { ok = false; break; }
+        for (int e = 0; e < E && ok; ++e)
+          for (int l = 0; l < depth && ok; ++l, ++layer) {
+            // the accumulator (and sH) are free once the previous layer's epilogue is done
+            if (layer > 0 && !mbar_wait(&hready, (uint32_t)((layer - 1) & 1))) { ok = false; break; }
+            if (f_pending) {
+              load_features(t + 1);
+              f_pending = false;
+            }
+            tc_fence_after();
+            const uint8_t* A = l == 0 ? sF : sH;
+            for (int kc = 0; kc < 4; ++kc, ++i) {
+              const int s = (int)(i & 1);
+              if (!mbar_wait(&full[s], (uint32_t)((i >> 1) & 1))) { ok = false; break; }
+              tc_fence_after();
+              const uint32_t a0 = smem_u32(A + kc * kStageA), b0 = smem_u32(sW + s * kStageB);
+#pragma unroll
+              for (int j = 0; j < kChunkK / 16; ++j)
+                umma_bf16(tmem, smem_desc_sw128(a0 + j * 32), smem_desc_sw128(b0 + j * 32), idesc,
+                          (kc > 0 || j > 0) ? 1u : 0u);
+              umma_commit(&empty[s]);
+            }
+            if (!ok) break;
+            umma_commit(&mdone);
+            if (e == E - 1 && l == 0 && t + 1 < my_tiles) f_pending = true;
+          }
+      }
+      if (!ok) {
+        atomicOr(&lost, 1);
+        // a features load still in flight lands before the CTA ends (bounded)
+        mbar_wait(&fbar, (uint32_t)(f_issued - 1) & 1u);
+      }
+    }
+  } else {
+    // epilogue: lane r of TMEM quarter q is tile row r; this warp's half of the 256 columns
+    const int q = warp & 3, half = warp >> 2;
+    const int r = q * 32 + lane;
+    const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(half * 128);
+    const int n_out = P.n_out;
+    int64_t layer = 0, heads = 0;
+    bool ok = true;
+    for (int t = 0; t < my_tiles && ok; ++t) {
+      const int64_t row = ((int64_t)blockIdx.x + (int64_t)t * gridDim.x) * kTileM + r;
+      for (int e = 0; e < E && ok; ++e)
+        for (int l = 0; l < depth; ++l, ++layer) {
+          if (!warp_wait(&mdone, (uint32_t)(layer & 1), vlost)) { ok = false; break; }
+          tc_fence_after();
+          const float* bias = P.b + ((int64_t)l * E + e) * 256 + half * 128;
+          const bool last = l == depth - 1;
+          float yacc[kInferMaxOut];
+#pragma unroll
+          for (int j = 0; j < kInferMaxOut; ++j) yacc[j] = 0.0f;
+          for (int c16 = 0; c16 < 8; ++c16) {
+            float v[16];
+            tmem_ld16(taddr + (uint32_t)(c16 * 16), v);
+            __align__(16) __nv_bfloat16 hb[16];
+#pragma unroll
+            for (int k = 0; k < 16; ++k) {
+              const __nv_bfloat16 zb = __float2bfloat16_rn(v[k] + __ldg(bias + c16 * 16 + k));
+              const float zr = __bfloat162float(zb);
+              hb[k] = __float2bfloat16_rn(zr * sigmoid(zr));
+            }
+            const int col0 = half * 128 + c16 * 16;
+            if (!last) {
+              const int kc = col0 >> 6, u = (col0 & 63) >> 3;
+              uint8_t* rowp = sH + kc * kStageA + r * 128;
+              *reinterpret_cast<uint4*>(rowp + ((u ^ (r & 7)) << 4)) = *reinterpret_cast<const uint4*>(&hb[0]);
+              *reinterpret_cast<uint4*>(rowp + (((u + 1) ^ (r & 7)) << 4)) = *reinterpret_cast<const uint4*>(&hb[8]);
+            } else {
+              const float* wh = P.w_head + (int64_t)e * n_out * 256 + col0;
+#pragma unroll
+              for (int k = 0; k < 16; ++k) {
+                const float h = __bfloat162float(hb[k]);
+#pragma unroll
+                for (int j = 0; j < kInferMaxOut; ++j)
+                  if (j < n_out) yacc[j] = fmaf(h, __ldg(wh + j * 256 + k), yacc[j]);
+              }
+            }
+          }
+          if (!last) {
+            fence_proxy_async_smem();   // the generic stores, visible to the tensor core's reads
+          } else {
+            // the upper half hands its partial sums to the lower half through shared memory
+            // (ybar); its next write there comes after this head's hready, so no second barrier
+            if (half == 1) {
+#pragma unroll
+              for (int j = 0; j < kInferMaxOut; ++j) ypart[r][j] = yacc[j];
+              mbar_arrive(&ybar);
+            } else {
+              if (!warp_wait(&ybar, (uint32_t)(heads & 1), vlost)) { ok = false; break; }
+              if (row < P.m) {
+#pragma unroll
+                for (int j = 0; j < kInferMaxOut; ++j)
+                  if (j < n_out)
+                    P.y[((int64_t)e * P.m + row) * n_out + j] =
+                        (yacc[j] + ypart[r][j]) + __ldg(P.b_head + e * n_out + j);
+              }
+            }
+            ++heads;
+          }
+          tc_fence_before();
+          mbar_arrive(&hready);
+        }
+    }
+    if (!ok) atomicOr(&lost, 1);
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (lost && threadIdx.x == 0) atomicAdd(&g_timeouts, 1u);
+  if (warp == 0) {
+    tc_fence_after();
+    tmem_dealloc(tmem, kTmemCols);
+  }
+}
+
 // ---------------------------------------------------------------------- head
 // A block walks tiles of kHeadRows consecutive rows; in a tile each warp takes kHeadRows / 8
 // rows, one at a time, lane l holding columns 8l .. 8l+7 of the 256-wide hidden row. The
@@ -818,6 +1059,40 @@ int exc_mlp_adam_multi(const ExcAdamTensor* tensors, int32_t n_tensors, const fl
   if (bx > cap) bx = cap;
   dim3 grid((unsigned)(bx < 1 ? 1 : bx), (unsigned)n_tensors);
   adam_multi_kernel<<<grid, 256, 0, (cudaStream_t)stream>>>(P, sched, beta1, beta2, eps);
+  return mlp_cuda(cudaGetLastError());
+}
+
+int exc_mlp_infer(const ExcMlpInfer* a, void* stream) {
+  if (!a) return mlp_fail(EXC_ERR_INVALID, "infer: args NULL");
+  if (a->m < 1 || a->m % kTileM) return mlp_fail(EXC_ERR_INVALID, "infer: m must be a positive multiple of 128");
+  if (a->width != 256) return mlp_fail(EXC_ERR_INVALID, "infer: width must be 256");
+  if (a->n_members < 1 || a->depth < 1 || (int64_t)a->depth * a->n_members > 65535)
+    return mlp_fail(EXC_ERR_INVALID, "infer: n_members and depth must be >= 1");
+  if (a->n_out < 1 || a->n_out > kInferMaxOut) return mlp_fail(EXC_ERR_INVALID, "infer: n_out must be in [1, 8]");
+  if (!a->x || !a->w || !a->b || !a->w_head || !a->b_head || !a->y || !aligned16(a->x) || !aligned16(a->w))
+    return mlp_fail(EXC_ERR_INVALID, "infer: x, w (16-byte aligned), b, w_head, b_head and y are required");
+  if (a->m > (int64_t)INT32_MAX - kTileM) return mlp_fail(EXC_ERR_INVALID, "infer: m too large for one launch");
+  CUtensorMap tx, tw;
+  if (!make_map(&tx, a->x, a->m, 256, 0, 1, kTileM) ||
+      !make_map(&tw, a->w, 256, 256, (int64_t)256 * 256, a->depth * a->n_members, 256))
+    return mlp_fail(EXC_ERR_CUDA, "infer: tensor map encoding failed");
+  cudaError_t e = cudaFuncSetAttribute(mlp_infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kInferSmem);
+  if (e != cudaSuccess) return mlp_cuda(e);
+  int dev = 0, sms = 0;
+  if ((e = cudaGetDevice(&dev)) != cudaSuccess) return mlp_cuda(e);
+  if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return mlp_cuda(e);
+  const int64_t n_tiles = a->m / kTileM;
+  const int grid = (int)(n_tiles < sms ? n_tiles : sms);
+  InferParams P;
+  P.b = a->b;
+  P.w_head = a->w_head;
+  P.b_head = a->b_head;
+  P.y = a->y;
+  P.m = a->m;
+  P.n_members = a->n_members;
+  P.n_out = a->n_out;
+  P.depth = a->depth;
+  mlp_infer_kernel<<<grid, kInferThreads, kInferSmem, (cudaStream_t)stream>>>(tx, tw, P);
   return mlp_cuda(cudaGetLastError());
 }
 

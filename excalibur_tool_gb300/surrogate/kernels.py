@@ -75,6 +75,25 @@ def features(dirs, n_pad, n_freq, center, scale, out):
             "exc_mlp_features")
 
 
+def infer(x, w, b, w_head, b_head, y):
+    """The ensemble's forward pass in one launch (exc_mlp_infer): x [m, 256] bf16 features (m a
+    multiple of 128), w [depth, E, 256, 256] bf16, b [depth, E, 256] f32, w_head [E, n_out, 256]
+    f32, b_head [E, n_out] f32 -> y [E, m, n_out] f32 (preallocated)."""
+    import torch
+
+    for t in (x, w, b, w_head, b_head, y):
+        if not t.is_contiguous():
+            raise ValueError("infer: operands and output must be contiguous")
+    if x.dtype != torch.bfloat16 or w.dtype != torch.bfloat16:
+        raise TypeError("infer: x and w must be bfloat16")
+    depth, E = w.shape[0], w.shape[1]
+    a = N.ExcMlpInfer()
+    a.x, a.w, a.b = x.data_ptr(), w.data_ptr(), b.data_ptr()
+    a.w_head, a.b_head, a.y = w_head.data_ptr(), b_head.data_ptr(), y.data_ptr()
+    a.m, a.width, a.n_members, a.n_out, a.depth = x.shape[0], x.shape[1], E, w_head.shape[1], depth
+    N.check(N.load().exc_mlp_infer(C.byref(a), _stream(x)), "exc_mlp_infer")
+
+
 def head(h, w, b, *, y=None, targets=None, z=None, dh=None, dht=None, dw=None, db=None, loss=None):
     """Linear head over h [E, M, 256] bf16 with w [E, n_out, 256] f32, b [E, n_out] f32."""
     E, M, width = h.shape

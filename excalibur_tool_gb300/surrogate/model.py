@@ -313,24 +313,32 @@ class SkySurrogate:
         return TrainReport(steps, B, curve[-1][1] if curve else [], secs, curve)
 
     # ------------------------------------------------------------ inference
-    def predict_members(self, uv, extra=None):
+    def predict_members(self, uv, extra=None, fused: bool = True):
         """Every member's outputs [E, m, n_out] (physical units, float64, on the device) for
         directions uv ([m, 2] float64 device tensor) and their baseline features `extra`
-        ([m, k] device tensor, as given to fit)."""
+        ([m, k] device tensor, as given to fit). `fused`: the whole forward pass in one kernel
+        (exc_mlp_infer, activations kept on chip); otherwise layer by layer through HBM (the
+        training kernels' forward path; the same roundings, the head summed in another order)."""
         import torch
 
         m = uv.shape[0]
         mp = ((m + 127) // 128) * 128
         E, W, dev, bf = self.E, self.W, self.device, torch.bfloat16
-        ha = torch.empty((E, mp, W), dtype=bf, device=dev)
-        hb = torch.empty((E, mp, W), dtype=bf, device=dev)
         y = torch.empty((E, mp, self.n_out), device=dev)
         inp = self._features(uv, mp)
-        for l in range(self.depth):
-            o = ha if l % 2 == 0 else hb
-            K.gemm(inp, self.wb[l], epilogue="bias_silu", bias=self.b[l], c2=o)
-            inp = o
-        K.head(inp, self.w_head, self.b_head, y=y)
+        if fused:
+            # the layers' bf16 weights and biases stacked [depth, E, ...] for the one launch (2 MB,
+            # copied each call: training updates the per-layer tensors in place)
+            K.infer(inp, torch.stack(self.wb).contiguous(), torch.stack(self.b).contiguous(), self.w_head,
+                    self.b_head, y)
+        else:
+            ha = torch.empty((E, mp, W), dtype=bf, device=dev)
+            hb = torch.empty((E, mp, W), dtype=bf, device=dev)
+            for l in range(self.depth):
+                o = ha if l % 2 == 0 else hb
+                K.gemm(inp, self.wb[l], epilogue="bias_silu", bias=self.b[l], c2=o)
+                inp = o
+            K.head(inp, self.w_head, self.b_head, y=y)
         # undo the target normalisation (six-term quadratic baseline + per-output scale)
         u, v = uv[:, 0], uv[:, 1]
         cols = [torch.ones_like(u), u, v, u * u, u * v, v * v]

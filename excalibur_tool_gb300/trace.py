@@ -50,8 +50,6 @@ class TraceConfig:
     blocks_per_sm: int = 0
     use_queue: bool = True
     deadline_cycles: int = 0
-    retrace_coop: bool = False        # mixed: the FP64 re-trace with eight lanes per ray
-    retrace_rays_per_warp: int = 0    # mixed: rays per warp of the one-thread FP64 re-trace (0 = library default)
 
     def validate(self):
         if self.stepper not in N.STEPPER:
@@ -260,8 +258,6 @@ def _make_args(desc, res, cfg: TraceConfig, queue=None, abort_flag=None) -> N.Ex
     a.queue = queue.data_ptr() if queue is not None else None
     a.abort_flag = abort_flag.data_ptr() if abort_flag is not None else None
     a.deadline_cycles = int(cfg.deadline_cycles)
-    a.options = (N.OPT_RETRACE_COOP if cfg.retrace_coop else 0) | \
-        ((int(cfg.retrace_rays_per_warp) & 0xff) << N.OPT_RAYS_PER_WARP_SHIFT)
     return a
 
 

@@ -128,15 +128,7 @@ enum { EXC_PREC_FP64_EXACT = 0, EXC_PREC_FP64_FAST = 1, EXC_PREC_MIXED = 2, EXC_
 #define EXC_STOP_FACE  4
 #define EXC_FACE_MARGIN 1.05
 
-/* options: the mixed tracer's FP64 re-trace pass (fast FP64 build). By default one thread per
- * ray, EXC_RETRACE_RAYS_PER_WARP rays per warp (GB300's FP64 pipe spends its cycles on each
- * active lane, so few rays per warp, spread over every SM sub-partition, each run at the
- * latency of its own FP64 chain); bits 8-15 set another count (1..32; 32 = every lane). With
- * EXC_OPT_RETRACE_COOP, eight lanes per ray share each ray's right-hand side instead (FLRW,
- * RK4, 3-D base-node fields; otherwise the one-thread pass). */
-#define EXC_OPT_RETRACE_COOP 1
-#define EXC_OPT_RAYS_PER_WARP_SHIFT 8
-#define EXC_RETRACE_RAYS_PER_WARP 1
+
 
 /* obs_flags bits */
 #define EXC_OBS_ENDPOINTS 1   /* a, Phi at both ends; deflection; min_r */
@@ -221,7 +213,7 @@ typedef struct ExcTraceArgs {
   int32_t obs_flags;             /* EXC_OBS_* bits */
   int32_t block_size;            /* 0 = library default */
   int32_t blocks_per_sm;         /* 0 = library default */
-  int32_t options;               /* EXC_OPT_* bits (0 = library defaults) */
+  int32_t reserved0;
   double dt, dt_min, dt_max, rtol, atol;
   int64_t max_iter;              /* reference: 10000 */
   int64_t max_steps;             /* "steps" stop value */

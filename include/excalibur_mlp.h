@@ -78,6 +78,28 @@ int exc_mlp_head(const void* h, int64_t m, int32_t width, int32_t n_out, int32_t
                  const float* b, float* y, const float* targets, const void* z, void* dh, void* dht, int64_t ldt,
                  float* dw, float* db, float* loss, void* stream);
 
+/* The ensemble's forward pass for prediction in one launch, activations kept on chip: per
+ * 128-row tile of features x and member e, depth hidden layers h <- bf16(silu(bf16(h W^T + b)))
+ * (tcgen05, BF16 x BF16 -> FP32 in tensor memory; the same roundings as exc_gemm_bf16 with
+ * EXC_EPI_BIAS_SILU) and the linear head y = h . w_head^T + b_head in FP32. The inference half
+ * of exc_gemm_bf16 + exc_mlp_head, without the hidden activations' HBM round trips.
+ * x: [m][width] bf16 (m a multiple of 128); w: [depth][n_members][width][width] bf16 (layer l of
+ * member e maps its input through w[l][e] (out x in)); b: [depth][n_members][width] f32;
+ * w_head: [n_members][n_out][width] f32; b_head: [n_members][n_out] f32; y: [n_members][m][n_out]
+ * f32. Limits: width 256, n_out <= 8. No reference counterpart (the surrogate is new). */
+typedef struct ExcMlpInfer {
+  const void* x;
+  const void* w;
+  const float* b;
+  const float* w_head;
+  const float* b_head;
+  float* y;
+  int64_t m;
+  int32_t width, n_members, n_out, depth;
+} ExcMlpInfer;
+
+int exc_mlp_infer(const ExcMlpInfer* a, void* stream);
+
 /* Sum of a [batch][splits][rows][cols] f32 partial-sum array over splits -> out [batch][rows][cols] f32. */
 int exc_mlp_reduce_splits(const float* part, int32_t n_batch, int32_t splits, int64_t rows_x_cols, float* out,
                           void* stream);

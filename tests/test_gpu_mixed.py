@@ -145,37 +145,6 @@ def test_mixed_raw_hands_back_untouched_rays(patch):
     assert rel_err(mixed["state"][back], o.state[back]).max() <= 1e-12
 
 
-def test_retrace_schedules_agree(patch):
-    """The FP64 re-trace pass three ways: one thread per ray with one ray per warp (the default),
-    with every lane of a warp busy, and with eight lanes sharing each ray (EXC_OPT_RETRACE_COOP).
-    The one-thread schedules give the same bits; the eight-lane pass sums in another order and
-    agrees to the last digits; all are within 1e-12 of the oracle on the handed-back rays."""
-    import torch
-    from excalibur_tool_gb300.trace import trace_batch
-
-    wl, states, o = patch
-    res = {}
-    for name, kw in (("sparse", {}), ("full", {"retrace_rays_per_warp": 32}), ("coop", {"retrace_coop": True})):
-        r = trace_batch(wl.metric, wl.states, dataclasses.replace(wl.cfg, precision="mixed", **kw))
-        torch.cuda.synchronize()
-        res[name] = {k: getattr(r, k).cpu().numpy() for k in ("state", "status", "n_steps", "obs")}
-    raw = _run(wl, "mixed_raw")
-    back = raw["status"] == N.PH_RETRACE
-    a, b, c = res["sparse"], res["full"], res["coop"]
-    for k in ("state", "status", "n_steps", "obs"):
-        assert np.array_equal(a[k], b[k], equal_nan=True), k
-    assert np.array_equal(a["status"], c["status"]) and np.array_equal(a["n_steps"], c["n_steps"])
-    for k in ("state", "obs"):
-        assert np.array_equal(a[k][~back], c[k][~back], equal_nan=True), k
-    assert rel_err(c["state"][back], a["state"][back]).max() <= 1e-13
-    assert rel_err(c["state"][back], o.state[back]).max() <= 1e-12
-    for col in ("a_em", "path", "chord", "min_r", "v1x"):
-        i = N.OBS_COLS.index(col)
-        assert rel_err(c["obs"][back, i], a["obs"][back, i]).max() <= 1e-12, col
-    i = N.OBS_COLS.index("phi_em")     # Phi near its zero crossings: an absolute floor
-    assert (np.abs(c["obs"][back, i] - a["obs"][back, i]) <= 1e-12 * np.abs(a["obs"][:, i]).max()).all()
-
-
 def test_pipelined_batches_match_single_launches(patch):
     """Re-traces overlapped on a side stream give the same photons as precision "mixed"."""
     import torch

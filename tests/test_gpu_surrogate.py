@@ -109,6 +109,36 @@ def test_gradients_match_fp64_cpu_reference(cuda):
         assert abs(float(buf["loss"][e]) - ref["loss"]) <= 1e-5 * ref["loss"]
 
 
+def test_fused_inference_matches_layer_by_layer(cuda):
+    """exc_mlp_infer (the whole forward pass of every member in one kernel, activations kept in
+    shared memory) against the layer-by-layer kernels: the hidden activations take the same
+    bf16 roundings, so only the head's fp32 sum differs in order -- agreement to ~1e-6 of the
+    outputs' scale; several tiles per CTA and a row count that is not a multiple of 128."""
+    import torch
+    from excalibur_tool_gb300.surrogate.model import SkySurrogate
+
+    torch.manual_seed(1)
+    m = SkySurrogate(n_members=3, seed=7, n_out=6)
+    for b in m.b:
+        b.copy_(torch.randn_like(b) * 0.1)
+    m.b_head.copy_(torch.randn_like(m.b_head) * 0.1)
+    rng = np.random.default_rng(3)
+    for n in (1000, 152 * 128 * 3 + 77):
+        uv = torch.as_tensor(rng.uniform(-1, 1, (n, 2)), device="cuda")
+        a = m.predict_members(uv, fused=True)
+        b = m.predict_members(uv, fused=False)
+        torch.cuda.synchronize()
+        scale = float(b.abs().max())
+        assert a.shape == b.shape and bool(torch.isfinite(a).all())
+        assert float((a - b).abs().max()) <= 1e-5 * scale, (n, float((a - b).abs().max()), scale)
+    from excalibur_tool_gb300 import _native as N
+    import ctypes as C
+
+    cnt = C.c_uint32(0)
+    N.check(N.load().exc_mlp_error_count(C.byref(cnt)), "exc_mlp_error_count")
+    assert cnt.value == 0
+
+
 def test_graphed_training_equals_eager(cuda):
     """Training steps replayed from a captured CUDA graph (one multi-tensor Adam launch reading
     the step's schedule on the device) follow the eager loop (same batches, per-tensor Adam
