@@ -49,6 +49,13 @@ __device__ __forceinline__ double py_fmod(double a, double b) {
   return m;
 }
 
+// py_fmod(d, L) for the periodic wrap, L > 0: a d already in (0, L) is its own remainder (fmod is
+// exact), so the division-free test returns it unchanged and only the rare wrap pays for fmod.
+// The same bits as py_fmod for every d (0 and -0 take the fmod path, which gives +0).
+__device__ __forceinline__ double py_wrap(double d, double L) {
+  return (d > 0.0 && d < L) ? d : py_fmod(d, L);
+}
+
 // Python integer modulo (non-negative for n > 0).
 __device__ __forceinline__ int64_t py_imod(int64_t i, int64_t n) {
   int64_t r = i % n;
@@ -138,9 +145,9 @@ __device__ __forceinline__ int interp_snapshot(const ExcField& f, const double* 
   if (f.boundary == EXC_BOUNDARY_PERIODIC) {
     // fused_interpolation_gradient_3d_periodic, interpolator_4d_fast.py:195-255
     const double Lx = (double)nx * sx, Ly = (double)ny * sy, Lz = (double)nz * sz;
-    x = ox + py_fmod(x - ox, Lx);
-    y = oy + py_fmod(y - oy, Ly);
-    z = oz + py_fmod(z - oz, Lz);
+    x = ox + py_wrap(x - ox, Lx);
+    y = oy + py_wrap(y - oy, Ly);
+    z = oz + py_wrap(z - oz, Lz);
     const double rx = div_rn(x - ox, sx, fi[0]), ry = div_rn(y - oy, sy, fi[1]), rz = div_rn(z - oz, sz, fi[2]);
     if (!isfinite(rx) || !isfinite(ry) || !isfinite(rz)) return EXC_PH_NONFINITE;
     int64_t i0 = (int64_t)floor(rx), j0 = (int64_t)floor(ry), k0 = (int64_t)floor(rz);
