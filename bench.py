@@ -705,9 +705,12 @@ def run_batching(args, dev, stream):
                         + (f"; 1/{scale} of the 1,048,576 + 16 x 65,536 configuration" if scale > 1 else ""),
             "photons": n, "fields": wl.info["fields"], "host_build_s": build_s,
             "autotune": {"block_size": plan["block_size"], "blocks_per_sm": plan["blocks_per_sm"],
+                         "staging": plan["staging"], "knobs": "threads per block x blocks per SM, then the "
+                                                              "3 fastest with the a(eta) table in shared memory",
                          "best_steps_tried_per_s": plan["best_rate"], "trials": len(plan["trials"]),
                          "seconds": tune_s, "sample": plan["sample"], "time_box": "1e8 SM cycles per trial",
-                         "all_trials": [{"block": t[0], "per_sm": t[1], "rate": t[3]} for t in plan["trials"]]},
+                         "all_trials": [{"block": t[0], "per_sm": t[1], "staging": t[2], "rate": t[4]}
+                                        for t in plan["trials"]]},
             "default_schedule_s": default_s, "graph_replay_s": graph_s,
             "rays_per_s": n / graph_s, "accepted_steps_per_s": float(steps.sum()) / graph_s,
             "rk45_trials_per_s": float(iters.sum()) / graph_s,

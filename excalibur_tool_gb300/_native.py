@@ -73,7 +73,7 @@ class ExcTraceArgs(C.Structure):
                 ("record_cols", C.c_int32), ("stepper", C.c_int32), ("tableau", C.c_int32),
                 ("precision", C.c_int32), ("renormalize_every", C.c_int32), ("stop_flags", C.c_int32),
                 ("obs_flags", C.c_int32), ("block_size", C.c_int32), ("blocks_per_sm", C.c_int32),
-                ("reserved0", C.c_int32), ("dt", C.c_double), ("dt_min", C.c_double),
+                ("staging", C.c_int32), ("dt", C.c_double), ("dt_min", C.c_double),
                 ("dt_max", C.c_double), ("rtol", C.c_double), ("atol", C.c_double),
                 ("max_iter", C.c_int64), ("max_steps", C.c_int64), ("box_lo", C.c_double * 3),
                 ("box_hi", C.c_double * 3), ("a_stop", C.c_double), ("lens_center", C.c_double * 3),
@@ -93,13 +93,17 @@ class ExcPhotonGen(C.Structure):
 
 
 EXC_TUNE_MAX_TRIALS = 32
+# where the FP64 tracers read the a(eta) table (ExcTraceArgs.staging)
+STAGING = {"cache": 0, "shared": 1}
+STAGING_MAX_TABLE = 12288
 
 
 class ExcLaunchPlan(C.Structure):
     _fields_ = [("block_size", C.c_int32), ("blocks_per_sm", C.c_int32), ("best_ms", C.c_float),
                 ("best_rate", C.c_float), ("n_trials", C.c_int32), ("trial_block", C.c_int32 * EXC_TUNE_MAX_TRIALS),
                 ("trial_blocks_per_sm", C.c_int32 * EXC_TUNE_MAX_TRIALS),
-                ("trial_ms", C.c_float * EXC_TUNE_MAX_TRIALS), ("trial_rate", C.c_float * EXC_TUNE_MAX_TRIALS)]
+                ("trial_ms", C.c_float * EXC_TUNE_MAX_TRIALS), ("trial_rate", C.c_float * EXC_TUNE_MAX_TRIALS),
+                ("staging", C.c_int32), ("trial_staging", C.c_int32 * EXC_TUNE_MAX_TRIALS)]
 
 
 class ExcGemm(C.Structure):

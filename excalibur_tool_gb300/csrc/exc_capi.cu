@@ -180,6 +180,14 @@ int exc_trace(const ExcMetric* metric, const ExcTraceArgs* a, void* stream) {
       return fail(EXC_ERR_INVALID, "records need n_records, max_records >= 1 and record_cols == %d", want);
   }
   if (a->obs_flags && !a->obs) return fail(EXC_ERR_INVALID, "obs_flags set but obs is NULL");
+  if (a->staging != EXC_STAGING_CACHE && a->staging != EXC_STAGING_SHARED)
+    return fail(EXC_ERR_INVALID, "unknown staging %d", a->staging);
+  // the FP64 launches read the a(eta) table from shared memory only when the metric has one
+  const bool uses_table = metric->kind == EXC_METRIC_FLRW && metric->cosmology != EXC_COSMO_STATIC;
+  if (a->staging == EXC_STAGING_SHARED && uses_table && metric->a_table_n > EXC_STAGING_MAX_TABLE)
+    return fail(EXC_ERR_INVALID, "staging: the a(eta) table has %lld entries (shared memory holds %d)",
+                (long long)metric->a_table_n, EXC_STAGING_MAX_TABLE);
+  const int stage_table = a->staging == EXC_STAGING_SHARED && uses_table ? 1 : 0;
   const int block = a->block_size > 0 ? a->block_size : 128;
   if (block % 32 != 0 || block > 128)
     return fail(EXC_ERR_INVALID, "block_size must be a multiple of 32 and <= 128");
@@ -196,11 +204,11 @@ int exc_trace(const ExcMetric* metric, const ExcTraceArgs* a, void* stream) {
     ce = cudaMemsetAsync(a->queue, 0, 2 * sizeof(uint32_t), s);
     if (ce != cudaSuccess) return cuda_fail(ce, "queue reset");
   }
-  if (a->precision == EXC_PREC_FP64_EXACT)
-    ce = exc_exact::trace(D, *a, block, a->blocks_per_sm, sms, s);
-  else if (a->precision == EXC_PREC_FP64_FAST)
-    ce = exc_fast::trace(D, *a, block, a->blocks_per_sm, sms, s);
-  else {
+  if (a->precision == EXC_PREC_FP64_EXACT || a->precision == EXC_PREC_FP64_FAST) {
+    D.stage_table = stage_table;
+    ce = a->precision == EXC_PREC_FP64_EXACT ? exc_exact::trace(D, *a, block, a->blocks_per_sm, sms, s)
+                                              : exc_fast::trace(D, *a, block, a->blocks_per_sm, sms, s);
+  } else {
     if (a->precision != EXC_PREC_RETRACE) {
       ce = exc_mixed::trace(D, *a, block, a->blocks_per_sm, sms, s);
       if (ce != cudaSuccess) return cuda_fail(ce, "mixed trace launch");
@@ -213,6 +221,7 @@ int exc_trace(const ExcMetric* metric, const ExcTraceArgs* a, void* stream) {
         if (ce != cudaSuccess) return cuda_fail(ce, "queue reset");
       }
       D.retrace_only = 1;
+      D.stage_table = stage_table;
       ce = exc_fast::trace(D, *a, block, a->blocks_per_sm, sms, s);
       if (ce != cudaSuccess) return cuda_fail(ce, "re-trace launch");
     }

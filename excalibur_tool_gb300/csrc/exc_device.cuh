@@ -444,21 +444,28 @@ __device__ __forceinline__ int interp_field(const ExcField& f, const double* fi,
 }
 
 // ------------------------------------------------------------ cosmology
+// The block's copy of the a(eta) table under EXC_STAGING_SHARED (dynamic shared memory, filled by
+// the trace kernel's prologue).
+extern __shared__ double stage_tab_s[];
+
+__device__ __forceinline__ double a_table_at(const DevMetric& D, int64_t i) {
+  return D.stage_table ? stage_tab_s[i] : __ldg(D.m.a_table + i);
+}
+
 // a_interp_numba, core/cosmology.py:8-25 (clamped linear interpolation).
 __device__ __forceinline__ double a_interp(const DevMetric& D, double eta, int& st) {
   const ExcMetric& m = D.m;
-  const double* __restrict__ tab = m.a_table;
   const int64_t n = m.a_table_n;
-  if (eta <= m.eta_min) return __ldg(tab);
+  if (eta <= m.eta_min) return a_table_at(D, 0);
   const double max_eta = m.eta_min + m.eta_step * (double)(n - 1);
-  if (eta >= max_eta) return __ldg(tab + n - 1);
+  if (eta >= max_eta) return a_table_at(D, n - 1);
   if (isnan(eta)) { st = EXC_PH_NONFINITE; return NAN; }
   int64_t i = (int64_t)div_c(eta - m.eta_min, m.eta_step, D.i_eta_step);
   // the quotient can round up to n-1 within an ulp of the table end (the
   // reference would index past its table there); stay on the last cell
   if (i > n - 2) i = n - 2;
   const double t = div_c(eta - (m.eta_min + (double)i * m.eta_step), m.eta_step, D.i_eta_step);
-  return (1.0 - t) * __ldg(tab + i) + t * __ldg(tab + i + 1);
+  return (1.0 - t) * a_table_at(D, i) + t * a_table_at(D, i + 1);
 }
 
 // LCDM_Cosmology.adot_of_eta given a = a_of_eta(eta), inv_a = 1/a (core/cosmology.py:69-93).

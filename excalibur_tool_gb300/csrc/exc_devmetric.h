@@ -11,6 +11,7 @@ struct DevMetric {
   double ic2, ic4, i_eta_step;
   double finv[EXC_MAX_FIELDS][8];   // 1/s0, 1/s1, 1/s2, 1/s3, 1/(2 s0), 1/(2 s1), 1/(2 s2), 1/(2 s3)
   int retrace_only;                 // trace only photons whose status is EXC_PH_RETRACE
+  int stage_table;                  // the a(eta) table is read from the block's shared-memory copy
 };
 
 }  // namespace exc

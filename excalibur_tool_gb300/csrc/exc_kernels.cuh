@@ -505,6 +505,10 @@ __device__ __forceinline__ int64_t next_work(const DevMetric& D, const ExcTraceA
 
 template <int MK, class FT, int STEPPER, bool REC>
 __global__ void __launch_bounds__(128) trace_kernel(const DevMetric D, const ExcTraceArgs A) {
+  if (D.stage_table) {
+    for (int64_t i = threadIdx.x; i < D.m.a_table_n; i += blockDim.x) stage_tab_s[i] = __ldg(D.m.a_table + i);
+    __syncthreads();
+  }
   Tracer<MK, FT> T(D, A);
   Photon P;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
@@ -540,9 +544,14 @@ struct LaunchCfg {
 template <int MK, class FT, int STEPPER, bool REC>
 cudaError_t launch_trace_t(const DevMetric& D, const ExcTraceArgs& A, LaunchCfg lc, cudaStream_t s) {
   auto kern = trace_kernel<MK, FT, STEPPER, REC>;
+  const size_t smem = D.stage_table ? (size_t)D.m.a_table_n * sizeof(double) : 0;
+  if (smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+  }
   int per_sm = lc.blocks_per_sm;
   if (per_sm <= 0) {
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, lc.block, 0);
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, lc.block, smem);
     if (e != cudaSuccess) return e;
     if (per_sm < 1) per_sm = 1;
   }
@@ -550,7 +559,7 @@ cudaError_t launch_trace_t(const DevMetric& D, const ExcTraceArgs& A, LaunchCfg 
   const int64_t need = (A.n_photons + lc.block - 1) / lc.block;
   if (grid > need) grid = need;
   if (grid < 1) grid = 1;
-  kern<<<(int)grid, lc.block, 0, s>>>(D, A);
+  kern<<<(int)grid, lc.block, smem, s>>>(D, A);
   return cudaGetLastError();
 }
 

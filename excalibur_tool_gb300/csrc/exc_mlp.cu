@@ -103,18 +103,17 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
   for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
-// The sigmoid of the SiLU epilogues with one special-function operation (the epilogues are bound
-// by that pipe): t = 2^(-|z| log2 e) in (0, 1] from ex2.approx, 1 / (1 + t) on the FMA pipe (a
-// quadratic start on (1, 2] refined by two Newton steps), and sigma(-|z|) = t sigma(|z|). Within
-// 3e-7 relative of the exact sigmoid for every z; the outputs are rounded to BF16.
+// The sigmoid of the SiLU epilogues: 1 / (1 + 2^(-z log2 e)) from the hardware's approximate
+// base-2 exponential and reciprocal (two special-function operations, four instructions; the
+// conversions to BF16 around it are packed in pairs so that the special-function pipe keeps
+// pace with the FMA pipe). Saturates to 0 and 1 without a branch: 2^(-z log2 e) overflows to
+// +inf for z < -88 and the reciprocal of +inf is 0. Within ~1e-6 relative of the exact sigmoid;
+// the outputs are rounded to BF16.
 __device__ __forceinline__ float sigmoid(float z) {
-  float t;
-  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(t) : "f"(-fabsf(z) * 1.4426950408889634f));
-  const float d = 1.0f + t;
-  float r = fmaf(fmaf(0.31367889f, d, -1.42502104f), d, 2.09950988f);
-  r = fmaf(r, fmaf(-d, r, 1.0f), r);
-  r = fmaf(r, fmaf(-d, r, 1.0f), r);
-  return z >= 0.0f ? r : t * r;
+  float t, r;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(t) : "f"(z * -1.4426950408889634f));
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(1.0f + t));
+  return r;
 }
 
 // TMA: one 3-D tile (x = K element, y = row, z = batch member) into shared memory,
@@ -197,22 +196,22 @@ __device__ __forceinline__ void epilogue(const ExcGemm& g, uint32_t tmem, int64_
           *reinterpret_cast<float4*>(tf + r * kPitchF + c0 + i) = make_float4(v[i], v[i + 1], v[i + 2], v[i + 3]);
       } else if (EPI == EXC_EPI_BIAS_SILU) {
         const float* bias = sbias + cb + c0;
-        __align__(16) __nv_bfloat16 zb[16], hb[16];
+        // pairs rounded to BF16 with one conversion each (the same round-to-nearest-even values)
+        __align__(16) __nv_bfloat162 zb[8], hb[8];
 #pragma unroll
-        for (int i = 0; i < 16; ++i) {
-          const float z = v[i] + bias[i];
-          zb[i] = __float2bfloat16_rn(z);
-          const float zr = __bfloat162float(zb[i]);   // the value the backward pass will see
-          hb[i] = __float2bfloat16_rn(zr * sigmoid(zr));
+        for (int i = 0; i < 8; ++i) {
+          zb[i] = __floats2bfloat162_rn(v[2 * i] + bias[2 * i], v[2 * i + 1] + bias[2 * i + 1]);
+          const float z0 = __low2float(zb[i]), z1 = __high2float(zb[i]);   // what the backward pass sees
+          hb[i] = __floats2bfloat162_rn(z0 * sigmoid(z0), z1 * sigmoid(z1));
         }
         if (g.c) {   // the pre-activation is staged only when it is an output (training)
           uint4* d1 = reinterpret_cast<uint4*>(t1 + r * kPitchH + c0);
           d1[0] = *reinterpret_cast<uint4*>(&zb[0]);
-          d1[1] = *reinterpret_cast<uint4*>(&zb[8]);
+          d1[1] = *reinterpret_cast<uint4*>(&zb[4]);
         }
         uint4* d2 = reinterpret_cast<uint4*>(t2 + r * kPitchH + c0);
         d2[0] = *reinterpret_cast<uint4*>(&hb[0]);
-        d2[1] = *reinterpret_cast<uint4*>(&hb[8]);
+        d2[1] = *reinterpret_cast<uint4*>(&hb[4]);
       } else {  // EXC_EPI_DSILU
         __align__(16) __nv_bfloat16 db[16];
         if (row < g.m) {
@@ -404,24 +403,32 @@ __global__ void features_kernel(const double* dirs, int64_t n, int64_t n_pad, in
 // 128-row tile of Fourier features is loaded once with TMA and stays in shared memory; for
 // every member the hidden layers run on it back to back -- tcgen05.mma of the 128 x 256
 // activations against the layer's 256 x 256 weights (64-wide K chunks streamed through a
-// two-stage TMA ring) into a 256-column TMEM accumulator, then an epilogue that adds the bias,
-// applies SiLU and rounds to BF16 exactly as the layer-by-layer kernel stores its outputs, and
-// writes the result back into shared memory in the 128-byte-swizzled K-major layout that TMA
-// would have produced (16-byte unit u of row r of a chunk at unit u ^ (r % 8)), where the next
-// layer's MMAs read it. The last layer's epilogue forms the linear head in FP32 registers.
-// Activations never leave the SM: per row, HBM sees the 512 B of features and the outputs.
+// three-stage TMA ring) into one of two 256-column TMEM accumulators, then an epilogue that adds
+// the bias, applies SiLU and rounds to BF16 exactly as the layer-by-layer kernel stores its
+// outputs, and writes the result back into shared memory in the 128-byte-swizzled K-major layout
+// that TMA would have produced (16-byte unit u of row r of a chunk at unit u ^ (r % 8)), where
+// the next layer's MMAs read it. The last layer's epilogue forms the linear head in FP32
+// registers. Activations never leave the SM: per row, HBM sees the 512 B of features and the
+// outputs.
 //
-// Warps 0-7 are the epilogue (warp w reads TMEM lanes 32 (w % 4) .. and columns 128 (w / 4) ..);
-// warp 8 lane 0 streams the weight chunks; warp 9 lane 0 issues the MMAs and loads each tile's
-// features once the last member's first-layer MMAs of the previous tile have completed. Three
-// mbarriers order them besides the weight ring: `fbar` (features landed), `mdone` (a layer's
-// MMAs completed: epilogue may read TMEM) and `hready` (the epilogue has read TMEM and written
-// the activations: the next layer may start). Every wait is bounded, as in the GEMM.
-constexpr int kInferEpiWarps = 8;
+// Sixteen epilogue warps walk the accumulator K chunk by K chunk (warp w reads TMEM lanes
+// 32 (w % 4) .. and, in chunk c, columns 64 c + 16 (w / 4) ..) and release each chunk of the next
+// layer's A operand as soon as it is written, so that the next layer's MMAs, into the other
+// accumulator, follow the epilogue chunk by chunk. Warp 16 lane 0 streams the weight chunks;
+// warp 17 lane 0 issues the MMAs and loads each tile's features once the last member's
+// first-layer MMAs of the previous tile have completed. Barriers besides the weight ring:
+// `fbar` (features landed), `mdone[b]` (a layer's MMAs into accumulator b completed),
+// `hready[c]` (chunk c of a layer's activations written), `tfree[b]` (the epilogue is done with
+// accumulator b) and `ybar` (the head's partial sums of column quarters 1-3 are in shared
+// memory). Every wait is bounded, as in the GEMM.
+constexpr int kInferEpiWarps = 16;
 constexpr int kInferThreads = (kInferEpiWarps + 2) * 32;
-constexpr int kActBytes = 4 * kStageA;                           // 128 x 256 BF16 in 4 K chunks
-constexpr int kInferSmem = 2 * kActBytes + 2 * kStageB + 1024;   // features, hidden, 2 weight stages
+constexpr int kInferStages = 3;
+constexpr int kActBytes = 4 * kStageA;                                      // 128 x 256 BF16 in 4 K chunks
+constexpr int kInferSmem = 2 * kActBytes + kInferStages * kStageB + 1024;   // features, hidden, weight stages
+constexpr uint32_t kInferTmemCols = 512;                                     // two 256-column accumulators
 constexpr int kInferMaxOut = 8;
+static_assert(kInferSmem + 256 <= 227 * 1024, "fused inference: shared memory per block");
 
 struct InferParams {
   const float* b;        // [depth][E][256]
@@ -435,14 +442,67 @@ struct InferParams {
 __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
+__device__ __forceinline__ int ld_shared_volatile(const int* p) {
+  int v;
+  asm volatile("ld.volatile.shared.b32 %0, [%1];" : "=r"(v) : "r"(smem_u32(p)));
+  return v;
+}
+__device__ __forceinline__ void st_shared_v4(uint32_t addr, uint32_t a, uint32_t b, uint32_t c, uint32_t d) {
+  asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(addr), "r"(a), "r"(b), "r"(c), "r"(d) : "memory");
+}
+__device__ __forceinline__ float4 ld_shared_f4(uint32_t addr) {
+  float4 v;
+  asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];" : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w) : "r"(addr)
+               : "memory");
+  return v;
+}
 // a bounded wait on an mbarrier phase, uniform across the warp (every lane leaves together, so
-// the warp-aligned tcgen05.ld that follows runs on all 32 lanes); false when it gave up
-__device__ __forceinline__ bool warp_wait(uint64_t* bar, uint32_t parity, volatile int* lost) {
+// the warp-aligned tcgen05.ld that follows runs on all 32 lanes); false when it gave up, or when
+// another role gave up (the shared `lost` word, looked at every 16 polls)
+__device__ __forceinline__ bool warp_wait(uint64_t* bar, uint32_t parity, const int* lost) {
   for (long long w = 0; w < kSpinLimit; ++w) {
     if (__all_sync(0xffffffffu, mbar_try_wait(bar, parity))) return true;
-    if (__any_sync(0xffffffffu, *lost != 0)) return false;
+    if ((w & 15) == 15 && __any_sync(0xffffffffu, ld_shared_volatile(lost) != 0)) return false;
   }
   return false;
+}
+// 16 columns of this thread's TMEM lane: the load is issued, and waited for separately (the
+// wait names the registers, so that nothing reads them before it)
+__device__ __forceinline__ void tmem_ld16_issue(uint32_t taddr, uint32_t (&r)[16]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+      "%15}, [%16];\n"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+}
+__device__ __forceinline__ void tmem_ld_wait(uint32_t (&r)[16]) {
+  asm volatile("tcgen05.wait::ld.sync.aligned;"
+               : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]), "+r"(r[6]), "+r"(r[7]),
+                 "+r"(r[8]), "+r"(r[9]), "+r"(r[10]), "+r"(r[11]), "+r"(r[12]), "+r"(r[13]), "+r"(r[14]), "+r"(r[15])
+               :
+               : "memory");
+}
+// the lanes' shared-memory writes (and, with tcgen05.fence before it, their TMEM reads) ordered
+// before one arrival for the warp
+__device__ __forceinline__ void warp_arrive(uint64_t* bar, int lane) {
+  __syncwarp();
+  if (lane == 0) mbar_arrive(bar);
+}
+__device__ __forceinline__ uint32_t bf16x2_bits(__nv_bfloat162 h) { return *reinterpret_cast<uint32_t*>(&h); }
+__device__ __forceinline__ void prefetch_l1(const void* p) {
+  asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
+}
+// 16 consecutive floats (16-byte aligned) through the read-only path
+__device__ __forceinline__ void load16(float (&d)[16], const float* p) {
+#pragma unroll
+  for (int k = 0; k < 16; k += 4) {
+    const float4 f = __ldg(reinterpret_cast<const float4*>(p + k));
+    d[k] = f.x;
+    d[k + 1] = f.y;
+    d[k + 2] = f.z;
+    d[k + 3] = f.w;
+  }
 }
 
 __global__ void __launch_bounds__(kInferThreads, 1) mlp_infer_kernel(const __grid_constant__ CUtensorMap tmX,
@@ -453,27 +513,29 @@ __global__ void __launch_bounds__(kInferThreads, 1) mlp_infer_kernel(const __gri
   uint8_t* sF = smem;                    // features of the tile
   uint8_t* sH = smem + kActBytes;        // hidden activations (overwritten layer after layer)
   uint8_t* sW = smem + 2 * kActBytes;    // weight stages
-  __shared__ uint64_t full[2], empty[2], fbar, mdone, hready, ybar;
+  __shared__ uint64_t full[kInferStages], empty[kInferStages], fbar, mdone[2], hready[4], tfree[2], ybar;
   __shared__ uint32_t tmem_base;
   __shared__ int lost;
-  __shared__ float ypart[kTileM][kInferMaxOut];   // the head's partial sums of the upper 128 columns
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int64_t n_tiles = (P.m + kTileM - 1) / kTileM;
   const int E = P.n_members, depth = P.depth;
   const int my_tiles = (int64_t)blockIdx.x < n_tiles ? (int)((n_tiles - 1 - blockIdx.x) / gridDim.x + 1) : 0;
   if (warp == 0) {
-    tmem_alloc(&tmem_base, kTmemCols);
+    tmem_alloc(&tmem_base, kInferTmemCols);
     tmem_relinquish();
   }
   if (threadIdx.x == 0) {
-    for (int s = 0; s < 2; ++s) {
+    for (int s = 0; s < kInferStages; ++s) {
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], 1);
     }
     mbar_init(&fbar, 1);
-    mbar_init(&mdone, 1);
-    mbar_init(&hready, kInferEpiWarps * 32);
-    mbar_init(&ybar, kInferEpiWarps * 16);
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&mdone[b], 1);
+      mbar_init(&tfree[b], kInferEpiWarps);
+    }
+    for (int c = 0; c < 4; ++c) mbar_init(&hready[c], kInferEpiWarps);
+    mbar_init(&ybar, kInferEpiWarps - 4);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     lost = 0;
   }
@@ -491,8 +553,8 @@ __global__ void __launch_bounds__(kInferThreads, 1) mlp_infer_kernel(const __gri
         for (int e = 0; e < E && !*vlost; ++e)
           for (int l = 0; l < depth && !*vlost; ++l)
             for (int kc = 0; kc < 4; ++kc) {
-              const int s = (int)(i & 1);
-              if (i >= 2 && !mbar_wait(&empty[s], (uint32_t)(((i >> 1) - 1) & 1))) {
+              const int s = (int)(i % kInferStages);
+              if (i >= kInferStages && !mbar_wait(&empty[s], (uint32_t)((i / kInferStages - 1) & 1))) {
                 atomicOr(&lost, 1);
                 break;
               }
@@ -502,7 +564,8 @@ __global__ void __launch_bounds__(kInferThreads, 1) mlp_infer_kernel(const __gri
             }
       // before the CTA can end, the copies it issued have landed (bounded; immediate when the
       // issuer consumed them)
-      for (int64_t j = i - 2 > 0 ? i - 2 : 0; j < i; ++j) mbar_wait(&full[j & 1], (uint32_t)((j >> 1) & 1));
+      for (int64_t j = i > kInferStages ? i - kInferStages : 0; j < i; ++j)
+        mbar_wait(&full[j % kInferStages], (uint32_t)((j / kInferStages) & 1));
     }
   } else if (warp == kInferEpiWarps + 1) {
     // MMA issuer (and the features of each tile)
@@ -516,40 +579,42 @@ __global__ void __launch_bounds__(kInferThreads, 1) mlp_infer_kernel(const __gri
         for (int kc = 0; kc < 4; ++kc) tma_load_3d(sF + kc * kStageA, &tmX, kc * kChunkK, (int)(tile * kTileM), 0, &fbar);
       };
       load_features(0);
-      int64_t i = 0, layer = 0;
-      bool f_pending = false, ok = true;
+      // i: weight chunks consumed; L: layers issued; nh: issued layers whose epilogue writes activations
+      int64_t i = 0, L = 0, nh = 0;
+      bool ok = true;
       for (int t = 0; t < my_tiles && ok; ++t) {
-        if (f_pending) {
-          // the features buffer is free once the previous tile's last first layer has been read
-          if (!mbar_wait(&hready, (uint32_t)((layer - 1) & 1))) { ok = false; break; }
-          load_features(t);
-          f_pending = false;
-        }
         if (!mbar_wait(&fbar, (uint32_t)(t & 1))) { ok = false; break; }
         for (int e = 0; e < E && ok; ++e)
-          for (int l = 0; l < depth && ok; ++l, ++layer) {
-            // the accumulator (and sH) are free once the previous layer's epilogue is done
-            if (layer > 0 && !mbar_wait(&hready, (uint32_t)((layer - 1) & 1))) { ok = false; break; }
-            if (f_pending) {
-              load_features(t + 1);
-              f_pending = false;
-            }
-            tc_fence_after();
+          for (int l = 0; l < depth && ok; ++l, ++L) {
+            const int b = (int)(L & 1);
+            // accumulator b is free once the epilogue of layer L - 2 is done with it; with one layer
+            // a member, the epilogue of layer L - 1 (its head) also finishes first, so that at most
+            // one head's partial sums are in shared memory
+            if (L >= 2 && !mbar_wait(&tfree[b], (uint32_t)(((L >> 1) - 1) & 1))) { ok = false; break; }
+            if (depth == 1 && L >= 1 && !mbar_wait(&tfree[b ^ 1], (uint32_t)(((L - 1) >> 1) & 1))) { ok = false; break; }
             const uint8_t* A = l == 0 ? sF : sH;
+            const uint32_t d = tmem + (uint32_t)(b * 256);
             for (int kc = 0; kc < 4; ++kc, ++i) {
-              const int s = (int)(i & 1);
-              if (!mbar_wait(&full[s], (uint32_t)((i >> 1) & 1))) { ok = false; break; }
+              // chunk kc of the previous layer's activations is in place
+              if (l > 0 && !mbar_wait(&hready[kc], (uint32_t)((nh - 1) & 1))) { ok = false; break; }
+              const int s = (int)(i % kInferStages);
+              if (!mbar_wait(&full[s], (uint32_t)((i / kInferStages) & 1))) { ok = false; break; }
               tc_fence_after();
               const uint32_t a0 = smem_u32(A + kc * kStageA), b0 = smem_u32(sW + s * kStageB);
 #pragma unroll
               for (int j = 0; j < kChunkK / 16; ++j)
-                umma_bf16(tmem, smem_desc_sw128(a0 + j * 32), smem_desc_sw128(b0 + j * 32), idesc,
+                umma_bf16(d, smem_desc_sw128(a0 + j * 32), smem_desc_sw128(b0 + j * 32), idesc,
                           (kc > 0 || j > 0) ? 1u : 0u);
               umma_commit(&empty[s]);
             }
             if (!ok) break;
-            umma_commit(&mdone);
-            if (e == E - 1 && l == 0 && t + 1 < my_tiles) f_pending = true;
+            umma_commit(&mdone[b]);
+            if (l < depth - 1) ++nh;
+            if (e == E - 1 && l == 0 && t + 1 < my_tiles) {
+              // the features buffer is free once these MMAs, its last readers, have completed
+              if (!mbar_wait(&mdone[b], (uint32_t)((L >> 1) & 1))) { ok = false; break; }
+              load_features(t + 1);
+            }
           }
       }
       if (!ok) {
@@ -559,60 +624,81 @@ __global__ void __launch_bounds__(kInferThreads, 1) mlp_infer_kernel(const __gri
       }
     }
   } else {
-    // epilogue: lane r of TMEM quarter q is tile row r; this warp's half of the 256 columns
-    const int q = warp & 3, half = warp >> 2;
+    // epilogue: lane r of TMEM quarter q is tile row r; this warp's 16 columns of every K chunk
+    const int q = warp & 3, sub = warp >> 2;
     const int r = q * 32 + lane;
-    const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(half * 128);
+    const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(sub * 16);
+    // this warp's two 16-byte units of row r in a K chunk of the activations (swizzled)
+    const int u0 = ((2 * sub) ^ (r & 7)) << 4, u1 = ((2 * sub + 1) ^ (r & 7)) << 4;
+    // the head's partial sums of column quarter p (1-3) for row r: units 0 and 1 of row r in chunk
+    // p - 1 of the activations, which only the quarter-0 thread of row r writes (and reads back)
+    const int y0 = (0 ^ (r & 7)) << 4, y1 = (1 ^ (r & 7)) << 4;
     const int n_out = P.n_out;
-    int64_t layer = 0, heads = 0;
+    const uint32_t sH_u32 = smem_u32(sH);
+    int64_t L = 0, heads = 0;
     bool ok = true;
     for (int t = 0; t < my_tiles && ok; ++t) {
       const int64_t row = ((int64_t)blockIdx.x + (int64_t)t * gridDim.x) * kTileM + r;
       for (int e = 0; e < E && ok; ++e)
-        for (int l = 0; l < depth; ++l, ++layer) {
-          if (!warp_wait(&mdone, (uint32_t)(layer & 1), vlost)) { ok = false; break; }
+        for (int l = 0; l < depth; ++l, ++L) {
+          const int b = (int)(L & 1);
+          const float* bias = P.b + ((int64_t)l * E + e) * 256 + sub * 16;
+          {
+            // the next layer's bias slices and, before a member's last layer, its head weights are
+            // brought into L1 a layer ahead (the shared-memory carve-out leaves L1 small, and these
+            // lines were last read a tile ago)
+            const int ln = l + 1 < depth ? l + 1 : 0;
+            const int en = l + 1 < depth ? e : (e + 1 < E ? e + 1 : 0);
+            if (lane < 4) prefetch_l1(P.b + ((int64_t)ln * E + en) * 256 + sub * 16 + lane * 64);
+            if (ln == depth - 1 && lane < 4 * n_out)
+              prefetch_l1(P.w_head + ((int64_t)en * n_out + (lane >> 2)) * 256 + sub * 16 + (lane & 3) * 64);
+          }
+          if (!warp_wait(&mdone[b], (uint32_t)((L >> 1) & 1), &lost)) { ok = false; break; }
           tc_fence_after();
-          const float* bias = P.b + ((int64_t)l * E + e) * 256 + half * 128;
+          const float* wh = P.w_head + (int64_t)e * n_out * 256 + sub * 16;
           const bool last = l == depth - 1;
+          const uint32_t tl = taddr + (uint32_t)(b * 256);
           float yacc[kInferMaxOut];
 #pragma unroll
           for (int j = 0; j < kInferMaxOut; ++j) yacc[j] = 0.0f;
-          for (int c16 = 0; c16 < 8; ++c16) {
-            float v[16];
-            tmem_ld16(taddr + (uint32_t)(c16 * 16), v);
+          // TMEM reads one chunk ahead: chunk kc + 1's load is in flight while chunk kc is worked on
+          uint32_t va[16], vb[16];
+          tmem_ld16_issue(tl, va);
+          tmem_ld_wait(va);
+#pragma unroll
+          for (int kc = 0; kc < 4; ++kc) {
+            uint32_t(&v)[16] = (kc & 1) ? vb : va;
+            uint32_t(&vn)[16] = (kc & 1) ? va : vb;
+            if (kc < 3) tmem_ld16_issue(tl + (uint32_t)((kc + 1) * 64), vn);
             float bv[16];
+            load16(bv, bias + kc * 64);
+            uint32_t hp[8];
 #pragma unroll
-            for (int k = 0; k < 16; k += 4) {
-              const float4 b4 = __ldg(reinterpret_cast<const float4*>(bias + c16 * 16 + k));
-              bv[k] = b4.x;
-              bv[k + 1] = b4.y;
-              bv[k + 2] = b4.z;
-              bv[k + 3] = b4.w;
+            for (int k = 0; k < 8; ++k) {
+              const __nv_bfloat162 z2 = __floats2bfloat162_rn(__uint_as_float(v[2 * k]) + bv[2 * k],
+                                                              __uint_as_float(v[2 * k + 1]) + bv[2 * k + 1]);
+              const float z0 = __low2float(z2), z1 = __high2float(z2);
+              hp[k] = bf16x2_bits(__floats2bfloat162_rn(z0 * sigmoid(z0), z1 * sigmoid(z1)));
             }
-            __align__(16) __nv_bfloat16 hb[16];
-#pragma unroll
-            for (int k = 0; k < 16; ++k) {
-              const __nv_bfloat16 zb = __float2bfloat16_rn(v[k] + bv[k]);
-              const float zr = __bfloat162float(zb);
-              hb[k] = __float2bfloat16_rn(zr * sigmoid(zr));
-            }
-            const int col0 = half * 128 + c16 * 16;
             if (!last) {
-              const int kc = col0 >> 6, u = (col0 & 63) >> 3;
-              uint8_t* rowp = sH + kc * kStageA + r * 128;
-              *reinterpret_cast<uint4*>(rowp + ((u ^ (r & 7)) << 4)) = *reinterpret_cast<const uint4*>(&hb[0]);
-              *reinterpret_cast<uint4*>(rowp + (((u + 1) ^ (r & 7)) << 4)) = *reinterpret_cast<const uint4*>(&hb[8]);
+              const uint32_t rowp = sH_u32 + (uint32_t)(kc * kStageA + r * 128);
+              st_shared_v4(rowp + u0, hp[0], hp[1], hp[2], hp[3]);
+              st_shared_v4(rowp + u1, hp[4], hp[5], hp[6], hp[7]);
+              fence_proxy_async_smem();   // the generic stores, visible to the tensor core's reads
+              warp_arrive(&hready[kc], lane);
             } else {
-              const float* wh = P.w_head + (int64_t)e * n_out * 256 + col0;
               float h[16];
 #pragma unroll
-              for (int k = 0; k < 16; ++k) h[k] = __bfloat162float(hb[k]);
+              for (int k = 0; k < 8; ++k) {
+                h[2 * k] = __uint_as_float(hp[k] << 16);
+                h[2 * k + 1] = __uint_as_float(hp[k] & 0xffff0000u);
+              }
 #pragma unroll
               for (int j = 0; j < kInferMaxOut; ++j) {
                 if (j >= n_out) break;
 #pragma unroll
                 for (int k = 0; k < 16; k += 4) {
-                  const float4 w4 = __ldg(reinterpret_cast<const float4*>(wh + j * 256 + k));
+                  const float4 w4 = __ldg(reinterpret_cast<const float4*>(wh + j * 256 + kc * 64 + k));
                   yacc[j] = fmaf(h[k], w4.x, yacc[j]);
                   yacc[j] = fmaf(h[k + 1], w4.y, yacc[j]);
                   yacc[j] = fmaf(h[k + 2], w4.z, yacc[j]);
@@ -620,30 +706,42 @@ __global__ void __launch_bounds__(kInferThreads, 1) mlp_infer_kernel(const __gri
                 }
               }
             }
+            if (kc < 3) tmem_ld_wait(vn);
           }
-          if (!last) {
-            fence_proxy_async_smem();   // the generic stores, visible to the tensor core's reads
-          } else {
-            // the upper half hands its partial sums to the lower half through shared memory
-            // (ybar); its next write there comes after this head's hready, so no second barrier
-            if (half == 1) {
-#pragma unroll
-              for (int j = 0; j < kInferMaxOut; ++j) ypart[r][j] = yacc[j];
-              mbar_arrive(&ybar);
+          if (last) {
+            // column quarters 1-3 hand their partial sums to quarter 0 through shared memory (the
+            // activations' units that only quarter 0 writes; the last layer's MMAs, their readers,
+            // have completed)
+            if (sub > 0) {
+              const uint32_t yp = sH_u32 + (uint32_t)((sub - 1) * kStageA + r * 128);
+              st_shared_v4(yp + y0, __float_as_uint(yacc[0]), __float_as_uint(yacc[1]), __float_as_uint(yacc[2]),
+                           __float_as_uint(yacc[3]));
+              st_shared_v4(yp + y1, __float_as_uint(yacc[4]), __float_as_uint(yacc[5]), __float_as_uint(yacc[6]),
+                           __float_as_uint(yacc[7]));
+              warp_arrive(&ybar, lane);
             } else {
-              if (!warp_wait(&ybar, (uint32_t)(heads & 1), vlost)) { ok = false; break; }
+              if (!warp_wait(&ybar, (uint32_t)(heads & 1), &lost)) { ok = false; break; }
+              float ys[kInferMaxOut];
+#pragma unroll
+              for (int j = 0; j < kInferMaxOut; ++j) ys[j] = yacc[j];
+#pragma unroll
+              for (int p = 0; p < 3; ++p) {
+                const uint32_t yp = sH_u32 + (uint32_t)(p * kStageA + r * 128);
+                const float4 a4 = ld_shared_f4(yp + y0);
+                const float4 c4 = ld_shared_f4(yp + y1);
+                ys[0] += a4.x; ys[1] += a4.y; ys[2] += a4.z; ys[3] += a4.w;
+                ys[4] += c4.x; ys[5] += c4.y; ys[6] += c4.z; ys[7] += c4.w;
+              }
               if (row < P.m) {
 #pragma unroll
                 for (int j = 0; j < kInferMaxOut; ++j)
-                  if (j < n_out)
-                    P.y[((int64_t)e * P.m + row) * n_out + j] =
-                        (yacc[j] + ypart[r][j]) + __ldg(P.b_head + e * n_out + j);
+                  if (j < n_out) P.y[((int64_t)e * P.m + row) * n_out + j] = ys[j] + __ldg(P.b_head + e * n_out + j);
               }
             }
             ++heads;
           }
           tc_fence_before();
-          mbar_arrive(&hready);
+          warp_arrive(&tfree[b], lane);
         }
     }
     if (!ok) atomicOr(&lost, 1);
@@ -653,7 +751,7 @@ __global__ void __launch_bounds__(kInferThreads, 1) mlp_infer_kernel(const __gri
   if (lost && threadIdx.x == 0) atomicAdd(&g_timeouts, 1u);
   if (warp == 0) {
     tc_fence_after();
-    tmem_dealloc(tmem, kTmemCols);
+    tmem_dealloc(tmem, kInferTmemCols);
   }
 }
 

@@ -2,9 +2,11 @@
 //
 // The tracer is latency-bound per photon (dependent gathers and, for FP64, a
 // narrow FP64 pipe), so the best (threads per block, resident blocks per SM)
-// pair depends on the precision build, the stepper, the grid sizes and the
-// spread of trajectory lengths. This times the real kernel on a caller-given
-// sample for each candidate and returns the fastest.
+// pair, and whether the a(eta) table is better read from shared memory than
+// through the read-only cache (which the grid gathers compete for), depend on
+// the precision build, the stepper, the grid sizes and the spread of trajectory
+// lengths. This times the real kernel on a caller-given sample for each
+// candidate and returns the fastest.
 #include <cuda_runtime.h>
 
 #include <cstring>
@@ -40,6 +42,13 @@ extern "C" int exc_autotune(const ExcMetric* metric, const ExcTraceArgs* args, c
         cand_p[n] = p;
         ++n;
       }
+  const int n_cache = n;
+  // the second pass (the staged table) exists for FP64 launches of a metric with a table
+  const bool fp64 = args->precision == EXC_PREC_FP64_EXACT || args->precision == EXC_PREC_FP64_FAST ||
+                    args->precision == EXC_PREC_MIXED || args->precision == EXC_PREC_RETRACE;
+  const bool can_stage = fp64 && metric->kind == EXC_METRIC_FLRW && metric->cosmology != EXC_COSMO_STATIC &&
+                         metric->a_table_n <= EXC_STAGING_MAX_TABLE;
+  const int n_staged = can_stage ? 3 : 0;
   cudaEvent_t e0, e1;
   if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
     exc::set_last_error("autotune: cudaEventCreate failed");
@@ -50,10 +59,25 @@ extern "C" int exc_autotune(const ExcMetric* metric, const ExcTraceArgs* args, c
   int32_t* iters = nullptr;    // host copy of n_iter for the rate
   if (args->n_iter) iters = new int32_t[(size_t)args->n_photons];
   int rc = EXC_SUCCESS;
-  for (int t = -1; t < n && rc == EXC_SUCCESS; ++t) {   // t = -1: untimed warm-up
+  int32_t cand_s[EXC_TUNE_MAX_TRIALS] = {0};
+  for (int t = -1; t < n_cache + n_staged && rc == EXC_SUCCESS; ++t) {   // t = -1: untimed warm-up
+    if (t == n_cache) {
+      // second pass: the fastest n_staged schedules of the first, with the staged table
+      bool taken[EXC_TUNE_MAX_TRIALS] = {false};
+      for (int k = 0; k < n_staged; ++k) {
+        int best = -1;
+        for (int j = 0; j < n_cache; ++j)
+          if (!taken[j] && (best < 0 || plan->trial_rate[j] > plan->trial_rate[best])) best = j;
+        taken[best] = true;
+        cand_b[n_cache + k] = cand_b[best];
+        cand_p[n_cache + k] = cand_p[best];
+        cand_s[n_cache + k] = EXC_STAGING_SHARED;
+      }
+    }
     ExcTraceArgs a = *args;
     a.block_size = t < 0 ? cand_b[0] : cand_b[t];
     a.blocks_per_sm = t < 0 ? cand_p[0] : cand_p[t];
+    a.staging = t < 0 ? EXC_STAGING_CACHE : cand_s[t];
     if (cudaMemcpyAsync(a.state, pristine_state, bytes, cudaMemcpyDeviceToDevice, s) != cudaSuccess) {
       exc::set_last_error("autotune: restoring the sample failed");
       rc = EXC_ERR_CUDA;
@@ -92,12 +116,14 @@ extern "C" int exc_autotune(const ExcMetric* metric, const ExcTraceArgs* args, c
     plan->trial_blocks_per_sm[t] = a.blocks_per_sm;
     plan->trial_ms[t] = ms;
     plan->trial_rate[t] = (float)rate;
+    plan->trial_staging[t] = a.staging;
     plan->n_trials = t + 1;
     if (rate > plan->best_rate) {
       plan->best_rate = (float)rate;
       plan->best_ms = ms;
       plan->block_size = a.block_size;
       plan->blocks_per_sm = a.blocks_per_sm;
+      plan->staging = a.staging;
     }
   }
   delete[] iters;

@@ -48,6 +48,7 @@ class TraceConfig:
     lens_center: tuple = (0.0, 0.0, 0.0)
     block_size: int = 0
     blocks_per_sm: int = 0
+    staging: str = "cache"           # FP64 tracers' a(eta) table: "cache" (read-only cache) | "shared" (shared memory)
     use_queue: bool = True
     deadline_cycles: int = 0
 
@@ -68,6 +69,8 @@ class TraceConfig:
             raise ValueError("dt must be finite")
         if self.stop_face and self.stop_box is None:
             raise ValueError("stop_face needs stop_box")
+        if self.staging not in N.STAGING:
+            raise ValueError(f"staging must be one of {list(N.STAGING)}")
         return self
 
 
@@ -246,6 +249,7 @@ def _make_args(desc, res, cfg: TraceConfig, queue=None, abort_flag=None) -> N.Ex
     a.obs_flags = (N.OBS_ENDPOINTS | N.OBS_PATH | (N.OBS_ISW if cfg.isw else 0)) if obs is not None else 0
     a.block_size = int(cfg.block_size)
     a.blocks_per_sm = int(cfg.blocks_per_sm)
+    a.staging = N.STAGING[cfg.staging]
     a.dt = float(cfg.dt)
     a.dt_min = float(cfg.dt_min)
     a.dt_max = float(cfg.dt_max)
@@ -324,7 +328,7 @@ _TUNE_CACHE: dict = {}
 
 def autotune(metric, states, cfg: TraceConfig, *, field_index=None, sample: Optional[int] = None, seed: int = 0,
              time_box_cycles: int = 1_000_000_000, use_cache: bool = True) -> TraceConfig:
-    """`cfg` with the (block_size, blocks_per_sm) that exc_autotune measured fastest.
+    """`cfg` with the (block_size, blocks_per_sm, staging) that exc_autotune measured fastest.
 
     By default every trial traces the whole batch (in a seeded shuffled order), so
     the score -- steps tried per second -- includes the wave quantisation and the
@@ -341,7 +345,7 @@ def autotune(metric, states, cfg: TraceConfig, *, field_index=None, sample: Opti
            int(desc.struct.fields[0].dtype), int(desc.struct.n_fields), int(states.shape[0]))
     if use_cache and key in _TUNE_CACHE:
         b, p = _TUNE_CACHE[key][:2]
-        return dataclasses.replace(cfg, block_size=b, blocks_per_sm=p)
+        return dataclasses.replace(cfg, block_size=b, blocks_per_sm=p, staging=_TUNE_CACHE[key][6])
     n = states.shape[0]
     g = torch.Generator(device="cpu").manual_seed(seed)
     idx = torch.randperm(n, generator=g)[:min(sample or n, n)].to(dev)
@@ -361,14 +365,16 @@ def autotune(metric, states, cfg: TraceConfig, *, field_index=None, sample: Opti
     with torch.cuda.device(dev):
         N.check(lib.exc_autotune(C.byref(desc.struct), C.byref(a), C.c_void_p(pristine.data_ptr()), C.byref(plan),
                                  N.stream_handle(dev)), "exc_autotune")
-    trials = [(plan.trial_block[i], plan.trial_blocks_per_sm[i], plan.trial_ms[i], plan.trial_rate[i])
-              for i in range(plan.n_trials)]
-    _TUNE_CACHE[key] = (plan.block_size, plan.blocks_per_sm, plan.best_ms, trials, plan.best_rate, m)
-    return dataclasses.replace(cfg, block_size=plan.block_size, blocks_per_sm=plan.blocks_per_sm)
+    names = {v: k for k, v in N.STAGING.items()}
+    trials = [(plan.trial_block[i], plan.trial_blocks_per_sm[i], names[plan.trial_staging[i]], plan.trial_ms[i],
+               plan.trial_rate[i]) for i in range(plan.n_trials)]
+    staging = names[plan.staging]
+    _TUNE_CACHE[key] = (plan.block_size, plan.blocks_per_sm, plan.best_ms, trials, plan.best_rate, m, staging)
+    return dataclasses.replace(cfg, block_size=plan.block_size, blocks_per_sm=plan.blocks_per_sm, staging=staging)
 
 
 def tune_report() -> dict:
-    return {str(k): {"block_size": v[0], "blocks_per_sm": v[1], "best_ms": v[2], "trials": v[3],
+    return {str(k): {"block_size": v[0], "blocks_per_sm": v[1], "staging": v[6], "best_ms": v[2], "trials": v[3],
                      "best_rate": v[4], "sample": v[5]} for k, v in _TUNE_CACHE.items()}
 
 

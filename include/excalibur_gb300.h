@@ -126,6 +126,14 @@ enum { EXC_PREC_FP64_EXACT = 0, EXC_PREC_FP64_FAST = 1, EXC_PREC_MIXED = 2, EXC_
  * step past the face, the default, moves in whole steps as the direction changes). Not in
  * the reference, which has no box stop. */
 #define EXC_STOP_FACE  4
+
+/* Grid staging of the FP64 tracers (ExcTraceArgs.staging; an autotuner knob): the a(eta) table
+ * read through the read-only data cache (EXC_STAGING_CACHE, the default) or copied once per
+ * block into shared memory at kernel start (EXC_STAGING_SHARED; tables of at most
+ * EXC_STAGING_MAX_TABLE entries). Same values either way. The mixed-precision tracer always
+ * keeps its FP32 copy of the table in shared memory when it fits. */
+enum { EXC_STAGING_CACHE = 0, EXC_STAGING_SHARED = 1 };
+#define EXC_STAGING_MAX_TABLE 12288
 #define EXC_FACE_MARGIN 1.05
 
 
@@ -213,7 +221,7 @@ typedef struct ExcTraceArgs {
   int32_t obs_flags;             /* EXC_OBS_* bits */
   int32_t block_size;            /* 0 = library default */
   int32_t blocks_per_sm;         /* 0 = library default */
-  int32_t reserved0;
+  int32_t staging;               /* EXC_STAGING_*: where the FP64 tracers read the a(eta) table */
   double dt, dt_min, dt_max, rtol, atol;
   int64_t max_iter;              /* reference: 10000 */
   int64_t max_steps;             /* "steps" stop value */
@@ -349,7 +357,10 @@ int exc_spherical_mass_grid(const int64_t n[3], const double origin[3], const do
 /* ---- launch-schedule autotuner (no reference counterpart: the reference has no
  * GPU schedule). Runs exc_trace on a sample batch for each candidate (block size
  * 64, 96, 128) x (blocks per SM 2, 3, 4, 5, 6, 8 within 2048 threads per SM, and
- * 0 = the occupancy limit) and returns the one with the highest rate. The sample's
+ * 0 = the occupancy limit), then the three fastest of those again with the a(eta) table
+ * staged in shared memory (EXC_STAGING_SHARED; FP64 launches of an FLRW metric with a
+ * table of at most EXC_STAGING_MAX_TABLE entries), and returns the one with the highest
+ * rate (args->staging is ignored; plan->staging is the chosen staging). The sample's
  * buffers are scratch: before every trial the library copies pristine_state
  * ([n][8] float64, device) into args->state; args->dt_state must be NULL (trials
  * start from args->dt); args->block_size / blocks_per_sm are ignored. With
@@ -369,6 +380,8 @@ typedef struct ExcLaunchPlan {
   int32_t trial_blocks_per_sm[EXC_TUNE_MAX_TRIALS];
   float trial_ms[EXC_TUNE_MAX_TRIALS];
   float trial_rate[EXC_TUNE_MAX_TRIALS];
+  int32_t staging;          /* EXC_STAGING_* of the chosen candidate */
+  int32_t trial_staging[EXC_TUNE_MAX_TRIALS];
 } ExcLaunchPlan;
 
 int exc_autotune(const ExcMetric* metric, const ExcTraceArgs* args, const double* pristine_state,

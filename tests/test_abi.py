@@ -115,12 +115,12 @@ def test_struct_layout_matches_c():
 #include "excalibur_gb300.h"
 #include "excalibur_mlp.h"
 int main(void) {
-  printf("%zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu\n", sizeof(ExcField), sizeof(ExcMetric),
+  printf("%zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu\n", sizeof(ExcField), sizeof(ExcMetric),
          sizeof(ExcTraceArgs), offsetof(ExcMetric, fields), offsetof(ExcTraceArgs, dt), offsetof(ExcTraceArgs, queue),
          offsetof(ExcTraceArgs, deadline_cycles), sizeof(ExcGemm), offsetof(ExcGemm, bias),
          offsetof(ExcGemm, stride_ct), sizeof(ExcPhotonGen), offsetof(ExcPhotonGen, uv), sizeof(ExcLaunchPlan),
          offsetof(ExcLaunchPlan, trial_rate), offsetof(ExcField, shift), sizeof(ExcAdamTensor),
-         offsetof(ExcAdamTensor, rows));
+         offsetof(ExcAdamTensor, rows), offsetof(ExcTraceArgs, staging), offsetof(ExcLaunchPlan, trial_staging));
   return 0;
 }
 '''
@@ -134,8 +134,38 @@ int main(void) {
             N.ExcTraceArgs.dt.offset, N.ExcTraceArgs.queue.offset, N.ExcTraceArgs.deadline_cycles.offset,
             C.sizeof(N.ExcGemm), N.ExcGemm.bias.offset, N.ExcGemm.stride_ct.offset, C.sizeof(N.ExcPhotonGen),
             N.ExcPhotonGen.uv.offset, C.sizeof(N.ExcLaunchPlan), N.ExcLaunchPlan.trial_rate.offset,
-            N.ExcField.shift.offset, C.sizeof(N.ExcAdamTensor), N.ExcAdamTensor.rows.offset]
+            N.ExcField.shift.offset, C.sizeof(N.ExcAdamTensor), N.ExcAdamTensor.rows.offset,
+            N.ExcTraceArgs.staging.offset, N.ExcLaunchPlan.trial_staging.offset]
     assert got == want
+
+
+def _table_flrw_metric(n_table):
+    m = N.ExcMetric()
+    m.kind = N.METRIC_FLRW
+    m.c, m.c2, m.c4 = 299792458.0, 299792458.0 ** 2, 299792458.0 ** 4
+    m.cosmology = 1                    # EXC_COSMO_TABLE
+    m.a_table, m.a_table_n = 4096, n_table
+    m.eta_min, m.eta_step = 0.0, 1.0
+    m.n_fields = 1
+    f = m.fields[0]
+    f.data = 4096                      # never dereferenced: every case fails validation first
+    f.dtype = N.DTYPE_F64
+    f.ndim = 3
+    for d in range(3):
+        f.n[d], f.spacing[d] = 8, 1.0
+    return m
+
+
+def test_staging_is_validated_on_the_host(lib):
+    """An unknown staging value, or a table too large for shared memory with EXC_STAGING_SHARED,
+    is refused before any device work."""
+    L = N.load()
+    m = _table_flrw_metric(5000)
+    assert L.exc_trace(C.byref(m), C.byref(_args(staging=7)), None) == N.EXC_ERR_INVALID
+    assert b"unknown staging" in L.exc_last_error()
+    big = _table_flrw_metric(N.STAGING_MAX_TABLE + 1)
+    assert L.exc_trace(C.byref(big), C.byref(_args(staging=N.STAGING["shared"])), None) == N.EXC_ERR_INVALID
+    assert b"staging" in L.exc_last_error()
 
 
 def test_new_entry_points_validate_before_any_launch(lib):

@@ -72,8 +72,11 @@ def test_autotune_and_graph_replay_reproduce_the_launch(cuda):
     tuned = autotune(wl.metric, wl.states, wl.cfg, field_index=wl.field_index, sample=1024, use_cache=False)
     assert tune_report()  # plan recorded
     assert tuned.block_size in (64, 96, 128) and tuned.blocks_per_sm in (0, 2, 3, 4, 5, 6, 8)
+    assert tuned.staging in N.STAGING
     rep = next(iter(tune_report().values()))
-    assert len(rep["trials"]) >= 20 and rep["best_rate"] > 0
+    assert len(rep["trials"]) >= 24 and rep["best_rate"] > 0
+    # the three fastest schedules again with the a(eta) table in shared memory
+    assert [t[2] for t in rep["trials"]].count("shared") == 3
     cap = CapturedTrace(wl.metric, wl.states, tuned, field_index=wl.field_index)
     for _ in range(2):
         out = cap.run()
@@ -102,3 +105,24 @@ def test_mixed_precision_graph_capture(cuda):
     out = cap.run()
     torch.cuda.synchronize()
     assert torch.equal(out.state, ref.state) and torch.equal(out.status, ref.status)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp64_fast"])
+def test_staged_table_gives_the_same_bits(cuda, precision):
+    """EXC_STAGING_SHARED (the a(eta) table copied into each block's shared memory) changes where
+    the table is read, not what is computed: the multi-field RK45 launch gives the same bits as
+    with the table read through the read-only cache, on every schedule tried."""
+    import torch
+    from excalibur_tool_gb300.trace import trace_batch
+
+    wl = _small(cuda)
+    cfg = dataclasses.replace(wl.cfg, precision=precision)
+    ref = trace_batch(wl.metric, wl.states, cfg, field_index=wl.field_index)
+    for block, per_sm in ((128, 0), (64, 5), (96, 8)):
+        got = trace_batch(wl.metric, wl.states, dataclasses.replace(cfg, staging="shared", block_size=block,
+                                                                    blocks_per_sm=per_sm),
+                          field_index=wl.field_index)
+        torch.cuda.synchronize()
+        for k in ("state", "status", "n_steps", "n_iter", "dt"):
+            assert torch.equal(getattr(got, k), getattr(ref, k)), (k, block, per_sm)
+        assert torch.allclose(got.obs, ref.obs, rtol=0, atol=0, equal_nan=True)
