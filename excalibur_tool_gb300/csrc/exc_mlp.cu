@@ -116,6 +116,54 @@ __device__ __forceinline__ float sigmoid(float z) {
   return r;
 }
 
+// Packed FP32 pairs (add/mul/fma .rn.f32x2: two IEEE single-precision operations in one
+// instruction, the same values as the scalar ones) for the epilogues, which are bound by the
+// number of instructions they issue.
+__device__ __forceinline__ uint64_t f2pack(float a, float b) {
+  uint64_t r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+  return r;
+}
+__device__ __forceinline__ void f2unpack(uint64_t r, float& a, float& b) {
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(r));
+}
+__device__ __forceinline__ uint64_t add2(uint64_t a, uint64_t b) {
+  uint64_t r;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+__device__ __forceinline__ uint64_t mul2(uint64_t a, uint64_t b) {
+  uint64_t r;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+__device__ __forceinline__ uint64_t fma2(uint64_t a, uint64_t b, uint64_t c) {
+  uint64_t r;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+  return r;
+}
+__device__ __forceinline__ uint32_t bf16x2_bits(__nv_bfloat162 h) { return *reinterpret_cast<uint32_t*>(&h); }
+
+// The BIAS_SILU epilogue of a pair of accumulator columns: z = acc + bias rounded to BF16
+// (*zbits, the value the backward pass sees), returns SiLU(z) = z sigmoid(z) rounded to BF16 --
+// per element exactly the operations of sigmoid() above, two columns an instruction.
+__device__ __forceinline__ uint32_t silu_pair(float v0, float v1, float b0, float b1, uint32_t* zbits) {
+  float s0, s1;
+  f2unpack(add2(f2pack(v0, v1), f2pack(b0, b1)), s0, s1);
+  const uint32_t zb = bf16x2_bits(__floats2bfloat162_rn(s0, s1));
+  if (zbits) *zbits = zb;
+  const uint64_t z = f2pack(__uint_as_float(zb << 16), __uint_as_float(zb & 0xffff0000u));
+  float a0, a1, t0, t1, d0, d1, r0, r1, h0, h1;
+  f2unpack(mul2(z, f2pack(-1.4426950408889634f, -1.4426950408889634f)), a0, a1);
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(t0) : "f"(a0));
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(t1) : "f"(a1));
+  f2unpack(add2(f2pack(t0, t1), f2pack(1.0f, 1.0f)), d0, d1);
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r0) : "f"(d0));
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r1) : "f"(d1));
+  f2unpack(mul2(z, f2pack(r0, r1)), h0, h1);
+  return bf16x2_bits(__floats2bfloat162_rn(h0, h1));
+}
+
 // TMA: one 3-D tile (x = K element, y = row, z = batch member) into shared memory,
 // completion counted in bytes on an mbarrier. The tensor map lives in the kernel's
 // parameter space (__grid_constant__); its generic address is what the
@@ -196,14 +244,10 @@ __device__ __forceinline__ void epilogue(const ExcGemm& g, uint32_t tmem, int64_
           *reinterpret_cast<float4*>(tf + r * kPitchF + c0 + i) = make_float4(v[i], v[i + 1], v[i + 2], v[i + 3]);
       } else if (EPI == EXC_EPI_BIAS_SILU) {
         const float* bias = sbias + cb + c0;
-        // pairs rounded to BF16 with one conversion each (the same round-to-nearest-even values)
-        __align__(16) __nv_bfloat162 zb[8], hb[8];
+        // column pairs: one BF16 conversion and one packed FP32 operation per step for both
+        __align__(16) uint32_t zb[8], hb[8];
 #pragma unroll
-        for (int i = 0; i < 8; ++i) {
-          zb[i] = __floats2bfloat162_rn(v[2 * i] + bias[2 * i], v[2 * i + 1] + bias[2 * i + 1]);
-          const float z0 = __low2float(zb[i]), z1 = __high2float(zb[i]);   // what the backward pass sees
-          hb[i] = __floats2bfloat162_rn(z0 * sigmoid(z0), z1 * sigmoid(z1));
-        }
+        for (int i = 0; i < 8; ++i) hb[i] = silu_pair(v[2 * i], v[2 * i + 1], bias[2 * i], bias[2 * i + 1], &zb[i]);
         if (g.c) {   // the pre-activation is staged only when it is an output (training)
           uint4* d1 = reinterpret_cast<uint4*>(t1 + r * kPitchH + c0);
           d1[0] = *reinterpret_cast<uint4*>(&zb[0]);
@@ -417,7 +461,9 @@ __global__ void features_kernel(const double* dirs, int64_t n, int64_t n_pad, in
 // accumulator, follow the epilogue chunk by chunk. Warp 16 lane 0 streams the weight chunks;
 // warp 17 lane 0 issues the MMAs and loads each tile's features once the last member's
 // first-layer MMAs of the previous tile have completed. Barriers besides the weight ring:
-// `fbar` (features landed), `mdone[b]` (a layer's MMAs into accumulator b completed),
+// `fbar` (features landed), `mdone[b]` (a layer's MMAs into accumulator b completed; the last K
+// chunk's MMAs run in two column halves, and `mdone_lo[b]` lets the epilogue start on columns
+// 0-127 while those of columns 128-255 finish),
 // `hready[c]` (chunk c of a layer's activations written), `tfree[b]` (the epilogue is done with
 // accumulator b) and `ybar` (the head's partial sums of column quarters 1-3 are in shared
 // memory). Every wait is bounded, as in the GEMM.
@@ -429,6 +475,7 @@ constexpr int kInferSmem = 2 * kActBytes + kInferStages * kStageB + 1024;   // f
 constexpr uint32_t kInferTmemCols = 512;                                     // two 256-column accumulators
 constexpr int kInferMaxOut = 8;
 static_assert(kInferSmem + 256 <= 227 * 1024, "fused inference: shared memory per block");
+static_assert(kInferMaxOut * 256 * 4 <= kStageA, "a member's head weights fit one activation chunk");
 
 struct InferParams {
   const float* b;        // [depth][E][256]
@@ -489,21 +536,6 @@ __device__ __forceinline__ void warp_arrive(uint64_t* bar, int lane) {
   __syncwarp();
   if (lane == 0) mbar_arrive(bar);
 }
-__device__ __forceinline__ uint32_t bf16x2_bits(__nv_bfloat162 h) { return *reinterpret_cast<uint32_t*>(&h); }
-__device__ __forceinline__ void prefetch_l1(const void* p) {
-  asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
-}
-// 16 consecutive floats (16-byte aligned) through the read-only path
-__device__ __forceinline__ void load16(float (&d)[16], const float* p) {
-#pragma unroll
-  for (int k = 0; k < 16; k += 4) {
-    const float4 f = __ldg(reinterpret_cast<const float4*>(p + k));
-    d[k] = f.x;
-    d[k + 1] = f.y;
-    d[k + 2] = f.z;
-    d[k + 3] = f.w;
-  }
-}
 
 __global__ void __launch_bounds__(kInferThreads, 1) mlp_infer_kernel(const __grid_constant__ CUtensorMap tmX,
                                                                      const __grid_constant__ CUtensorMap tmW,
@@ -513,7 +545,8 @@ __global__ void __launch_bounds__(kInferThreads, 1) mlp_infer_kernel(const __gri
   uint8_t* sF = smem;                    // features of the tile
   uint8_t* sH = smem + kActBytes;        // hidden activations (overwritten layer after layer)
   uint8_t* sW = smem + 2 * kActBytes;    // weight stages
-  __shared__ uint64_t full[kInferStages], empty[kInferStages], fbar, mdone[2], hready[4], tfree[2], ybar;
+  __shared__ uint64_t full[kInferStages], empty[kInferStages], fbar, mdone[2], mdone_lo[2], hready[4], tfree[2];
+  __shared__ uint64_t ybar, wbar;
   __shared__ uint32_t tmem_base;
   __shared__ int lost;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -532,10 +565,12 @@ __global__ void __launch_bounds__(kInferThreads, 1) mlp_infer_kernel(const __gri
     mbar_init(&fbar, 1);
     for (int b = 0; b < 2; ++b) {
       mbar_init(&mdone[b], 1);
+      mbar_init(&mdone_lo[b], 1);
       mbar_init(&tfree[b], kInferEpiWarps);
     }
     for (int c = 0; c < 4; ++c) mbar_init(&hready[c], kInferEpiWarps);
     mbar_init(&ybar, kInferEpiWarps - 4);
+    mbar_init(&wbar, kInferEpiWarps);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     lost = 0;
   }
@@ -570,7 +605,7 @@ __global__ void __launch_bounds__(kInferThreads, 1) mlp_infer_kernel(const __gri
   } else if (warp == kInferEpiWarps + 1) {
     // MMA issuer (and the features of each tile)
     if (lane == 0 && my_tiles > 0) {
-      const uint32_t idesc = idesc_bf16_f32(kTileM, 256);
+      const uint32_t idesc = idesc_bf16_f32(kTileM, 256), idesc_half = idesc_bf16_f32(kTileM, 128);
       int f_issued = 0;
       auto load_features = [&](int t) {
         ++f_issued;
@@ -601,10 +636,22 @@ __global__ void __launch_bounds__(kInferThreads, 1) mlp_infer_kernel(const __gri
               if (!mbar_wait(&full[s], (uint32_t)((i / kInferStages) & 1))) { ok = false; break; }
               tc_fence_after();
               const uint32_t a0 = smem_u32(A + kc * kStageA), b0 = smem_u32(sW + s * kStageB);
+              if (kc < 3) {
 #pragma unroll
-              for (int j = 0; j < kChunkK / 16; ++j)
-                umma_bf16(d, smem_desc_sw128(a0 + j * 32), smem_desc_sw128(b0 + j * 32), idesc,
-                          (kc > 0 || j > 0) ? 1u : 0u);
+                for (int j = 0; j < kChunkK / 16; ++j)
+                  umma_bf16(d, smem_desc_sw128(a0 + j * 32), smem_desc_sw128(b0 + j * 32), idesc,
+                            (kc > 0 || j > 0) ? 1u : 0u);
+              } else {
+                // the last K chunk by column halves (B rows 128-255 start 128 x 128 B into the stage)
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+#pragma unroll
+                  for (int j = 0; j < kChunkK / 16; ++j)
+                    umma_bf16(d + (uint32_t)(h * 128), smem_desc_sw128(a0 + j * 32),
+                              smem_desc_sw128(b0 + (uint32_t)(h * 128 * 128) + j * 32), idesc_half, 1u);
+                  if (h == 0) umma_commit(&mdone_lo[b]);
+                }
+              }
               umma_commit(&empty[s]);
             }
             if (!ok) break;
@@ -635,51 +682,77 @@ __global__ void __launch_bounds__(kInferThreads, 1) mlp_infer_kernel(const __gri
     const int y0 = (0 ^ (r & 7)) << 4, y1 = (1 ^ (r & 7)) << 4;
     const int n_out = P.n_out;
     const uint32_t sH_u32 = smem_u32(sH);
+    const uint32_t sWh_u32 = sH_u32 + 3 * kStageA;   // a member's head weights during its last layer
     int64_t L = 0, heads = 0;
     bool ok = true;
+    // The 64 bias values a warp needs in a layer (16 columns of each K chunk) are spread over its
+    // lanes, two a lane (lane j: chunk j / 8, columns 2 (j % 8) and 2 (j % 8) + 1 of the warp's
+    // 16), loaded a whole layer ahead -- an L2 round trip (the shared-memory carve-out leaves L1
+    // small and the line was last read a tile ago) -- and handed to every lane with a shuffle
+    // when a chunk needs them.
+    const int bofs = (lane >> 3) * 64 + sub * 16 + 2 * (lane & 7);
+    float2 bcur = __ldg(reinterpret_cast<const float2*>(P.b + bofs));
     for (int t = 0; t < my_tiles && ok; ++t) {
       const int64_t row = ((int64_t)blockIdx.x + (int64_t)t * gridDim.x) * kTileM + r;
       for (int e = 0; e < E && ok; ++e)
         for (int l = 0; l < depth; ++l, ++L) {
           const int b = (int)(L & 1);
-          const float* bias = P.b + ((int64_t)l * E + e) * 256 + sub * 16;
-          {
-            // the next layer's bias slices and, before a member's last layer, its head weights are
-            // brought into L1 a layer ahead (the shared-memory carve-out leaves L1 small, and these
-            // lines were last read a tile ago)
-            const int ln = l + 1 < depth ? l + 1 : 0;
-            const int en = l + 1 < depth ? e : (e + 1 < E ? e + 1 : 0);
-            if (lane < 4) prefetch_l1(P.b + ((int64_t)ln * E + en) * 256 + sub * 16 + lane * 64);
-            if (ln == depth - 1 && lane < 4 * n_out)
-              prefetch_l1(P.w_head + ((int64_t)en * n_out + (lane >> 2)) * 256 + sub * 16 + (lane & 3) * 64);
-          }
-          if (!warp_wait(&mdone[b], (uint32_t)((L >> 1) & 1), &lost)) { ok = false; break; }
+          const int ln = l + 1 < depth ? l + 1 : 0;
+          const int en = l + 1 < depth ? e : (e + 1 < E ? e + 1 : 0);
+          const float2 bnext = __ldg(reinterpret_cast<const float2*>(P.b + ((int64_t)ln * E + en) * 256 + bofs));
+          // columns 0-127 first; the rest (mdone) before chunk 2
+          if (!warp_wait(&mdone_lo[b], (uint32_t)((L >> 1) & 1), &lost)) { ok = false; break; }
           tc_fence_after();
-          const float* wh = P.w_head + (int64_t)e * n_out * 256 + sub * 16;
           const bool last = l == depth - 1;
+          if (last) {
+            // the copy below overwrites chunk 3 of the activations, which the second half of the
+            // last K chunk's MMAs reads: all of this layer's MMAs complete first
+            if (!warp_wait(&mdone[b], (uint32_t)((L >> 1) & 1), &lost)) { ok = false; break; }
+            tc_fence_after();
+            // the member's head weights go to chunk 3 of the activation buffer, whose last reader
+            // (this layer's MMAs) has completed; with one layer a member the previous head, which
+            // read them there, is finished first
+            if (depth == 1 && L > 0 && !warp_wait(&tfree[b ^ 1], (uint32_t)(((L - 1) >> 1) & 1), &lost)) {
+              ok = false;
+              break;
+            }
+            const float4* src = reinterpret_cast<const float4*>(P.w_head + (int64_t)e * n_out * 256);
+            for (int i = threadIdx.x; i < n_out * 64; i += kInferEpiWarps * 32) {
+              const float4 w4 = __ldg(src + i);
+              st_shared_v4(sWh_u32 + (uint32_t)(i * 16), __float_as_uint(w4.x), __float_as_uint(w4.y),
+                           __float_as_uint(w4.z), __float_as_uint(w4.w));
+            }
+            warp_arrive(&wbar, lane);
+            if (!warp_wait(&wbar, (uint32_t)(heads & 1), &lost)) { ok = false; break; }
+          } else if (l == 0 && L > 0) {
+            // chunk 3 still holds the previous member's head weights until every warp has finished
+            // that head (the previous layer released its accumulator)
+            if (!warp_wait(&tfree[b ^ 1], (uint32_t)(((L - 1) >> 1) & 1), &lost)) { ok = false; break; }
+          }
           const uint32_t tl = taddr + (uint32_t)(b * 256);
-          float yacc[kInferMaxOut];
+          uint64_t yacc2[kInferMaxOut];   // the head's sums over this warp's even and odd columns
 #pragma unroll
-          for (int j = 0; j < kInferMaxOut; ++j) yacc[j] = 0.0f;
-          // TMEM reads one chunk ahead: chunk kc + 1's load is in flight while chunk kc is worked on
-          uint32_t va[16], vb[16];
-          tmem_ld16_issue(tl, va);
-          tmem_ld_wait(va);
+          for (int j = 0; j < kInferMaxOut; ++j) yacc2[j] = 0;
 #pragma unroll
           for (int kc = 0; kc < 4; ++kc) {
-            uint32_t(&v)[16] = (kc & 1) ? vb : va;
-            uint32_t(&vn)[16] = (kc & 1) ? va : vb;
-            if (kc < 3) tmem_ld16_issue(tl + (uint32_t)((kc + 1) * 64), vn);
+            if (kc == 2 && !last) {
+              if (!warp_wait(&mdone[b], (uint32_t)((L >> 1) & 1), &lost)) { ok = false; break; }
+              tc_fence_after();
+            }
             float bv[16];
-            load16(bv, bias + kc * 64);
-            uint32_t hp[8];
 #pragma unroll
             for (int k = 0; k < 8; ++k) {
-              const __nv_bfloat162 z2 = __floats2bfloat162_rn(__uint_as_float(v[2 * k]) + bv[2 * k],
-                                                              __uint_as_float(v[2 * k + 1]) + bv[2 * k + 1]);
-              const float z0 = __low2float(z2), z1 = __high2float(z2);
-              hp[k] = bf16x2_bits(__floats2bfloat162_rn(z0 * sigmoid(z0), z1 * sigmoid(z1)));
+              bv[2 * k] = __shfl_sync(0xffffffffu, bcur.x, kc * 8 + k);
+              bv[2 * k + 1] = __shfl_sync(0xffffffffu, bcur.y, kc * 8 + k);
             }
+            uint32_t v[16];
+            tmem_ld16_issue(tl + (uint32_t)(kc * 64), v);
+            tmem_ld_wait(v);
+            uint32_t hp[8];
+#pragma unroll
+            for (int k = 0; k < 8; ++k)
+              hp[k] = silu_pair(__uint_as_float(v[2 * k]), __uint_as_float(v[2 * k + 1]), bv[2 * k], bv[2 * k + 1],
+                                nullptr);
             if (!last) {
               const uint32_t rowp = sH_u32 + (uint32_t)(kc * kStageA + r * 128);
               st_shared_v4(rowp + u0, hp[0], hp[1], hp[2], hp[3]);
@@ -687,28 +760,32 @@ __global__ void __launch_bounds__(kInferThreads, 1) mlp_infer_kernel(const __gri
               fence_proxy_async_smem();   // the generic stores, visible to the tensor core's reads
               warp_arrive(&hready[kc], lane);
             } else {
-              float h[16];
+              uint64_t h2[8];
 #pragma unroll
-              for (int k = 0; k < 8; ++k) {
-                h[2 * k] = __uint_as_float(hp[k] << 16);
-                h[2 * k + 1] = __uint_as_float(hp[k] & 0xffff0000u);
-              }
+              for (int k = 0; k < 8; ++k)
+                h2[k] = f2pack(__uint_as_float(hp[k] << 16), __uint_as_float(hp[k] & 0xffff0000u));
 #pragma unroll
               for (int j = 0; j < kInferMaxOut; ++j) {
                 if (j >= n_out) break;
 #pragma unroll
-                for (int k = 0; k < 16; k += 4) {
-                  const float4 w4 = __ldg(reinterpret_cast<const float4*>(wh + j * 256 + kc * 64 + k));
-                  yacc[j] = fmaf(h[k], w4.x, yacc[j]);
-                  yacc[j] = fmaf(h[k + 1], w4.y, yacc[j]);
-                  yacc[j] = fmaf(h[k + 2], w4.z, yacc[j]);
-                  yacc[j] = fmaf(h[k + 3], w4.w, yacc[j]);
+                for (int k = 0; k < 8; k += 2) {
+                  const float4 w4 = ld_shared_f4(sWh_u32 + (uint32_t)((j * 256 + kc * 64 + sub * 16 + 2 * k) * 4));
+                  yacc2[j] = fma2(h2[k], f2pack(w4.x, w4.y), yacc2[j]);
+                  yacc2[j] = fma2(h2[k + 1], f2pack(w4.z, w4.w), yacc2[j]);
                 }
               }
             }
-            if (kc < 3) tmem_ld_wait(vn);
           }
+          if (!ok) break;
+          bcur = bnext;
           if (last) {
+            float yacc[kInferMaxOut];
+#pragma unroll
+            for (int j = 0; j < kInferMaxOut; ++j) {
+              float lo, hi;
+              f2unpack(yacc2[j], lo, hi);
+              yacc[j] = lo + hi;
+            }
             // column quarters 1-3 hand their partial sums to quarter 0 through shared memory (the
             // activations' units that only quarter 0 writes; the last layer's MMAs, their readers,
             // have completed)
