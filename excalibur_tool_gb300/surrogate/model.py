@@ -106,6 +106,7 @@ class SkySurrogate:
         resid = targets - A @ self.baseline
         self.t_mean = resid.mean(0)
         self.t_std = resid.std(0) + 1e-300
+        self._norm_key = None   # the device copies used by prediction are made again
 
     def _normalise(self, uv: np.ndarray, targets: np.ndarray, extra: Optional[np.ndarray] = None) -> np.ndarray:
         return ((targets - _baseline_design(uv, extra) @ self.baseline - self.t_mean) / self.t_std).astype(np.float32)
@@ -347,9 +348,14 @@ class SkySurrogate:
                 raise ValueError(f"this model was fitted with {self.n_extra} baseline features")
             cols += [extra[:, k].double() for k in range(self.n_extra)]
         design = torch.stack(cols, 1)
-        base = design @ torch.as_tensor(self.baseline, device=dev)
-        scale = torch.as_tensor(self.t_std, device=dev)
-        shift = torch.as_tensor(self.t_mean, device=dev)
+        # the normalisation's device copies, made once per fit (no host copy, and so no
+        # synchronisation, on each call)
+        key = (id(self.baseline), id(self.t_std), id(self.t_mean))
+        if getattr(self, "_norm_key", None) != key:
+            self._norm_dev = tuple(torch.as_tensor(a, device=dev) for a in (self.baseline, self.t_std, self.t_mean))
+            self._norm_key = key
+        baseline, scale, shift = self._norm_dev
+        base = design @ baseline
         return y[:, :m].double() * scale + shift + base[None]
 
     def predict(self, uv: np.ndarray, chunk: int = 1 << 20, return_members: bool = False,

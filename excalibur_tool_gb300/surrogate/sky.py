@@ -52,6 +52,7 @@ from __future__ import annotations
 
 import dataclasses
 import time
+from typing import Optional
 
 import numpy as np
 
@@ -278,6 +279,17 @@ def pixel_centres(n_side: int) -> np.ndarray:
     return np.stack([A.reshape(-1), B.reshape(-1)], 1)
 
 
+def pixel_centres_t(n_side: int, device, start: int = 0, stop: Optional[int] = None):
+    """Rows start..stop of pixel_centres(n_side) built on the device (the same float64
+    operations, so the same values)."""
+    import torch
+
+    stop = n_side * n_side if stop is None else stop
+    i = torch.arange(start, stop, device=device, dtype=torch.int64)
+    t = lambda j: (j.to(torch.float64) + 0.5) / n_side * 2 - 1
+    return torch.stack([t(torch.div(i, n_side, rounding_mode="floor")), t(i % n_side)], 1)
+
+
 def fill_sky_map(model: SkySurrogate, metric, patch: Patch, cfg: TraceConfig, n_side: int = 4096,
                  std_threshold: float = 1e-7, audit_fraction: float = 0.01, audit_seed: int = 5,
                  chunk: int = 1 << 20):
@@ -292,16 +304,19 @@ def fill_sky_map(model: SkySurrogate, metric, patch: Patch, cfg: TraceConfig, n_
     obs_terms = observer_terms(metric, patch)
     uv = pixel_centres(n_side)
     n = len(uv)
-    out = np.empty((n, 4))
-    zstd = np.empty(n)
     t0 = time.perf_counter()
+    # the pixel centres are made on the device and the map stays there until one copy at the end
+    out_d = torch.empty((n, 4), dtype=torch.float64, device=model.device)
+    zstd_d = torch.empty(n, dtype=torch.float64, device=model.device)
     for s in range(0, n, chunk):
-        uvc = torch.as_tensor(uv[s:s + chunk], device=model.device)
+        uvc = pixel_centres_t(n_side, model.device, s, min(s + chunk, n))
         ex = born_features(metric, patch, uvc, cfg.stop_box) if model.n_extra else None
         y = model.predict_members(uvc, ex)                               # [E, m, 6] on the device
         members = compose_t(metric, patch, geo, uvc, y, obs_terms)       # [E, m, 4]
-        out[s:s + chunk] = compose_t(metric, patch, geo, uvc, y.mean(0), obs_terms).cpu().numpy()
-        zstd[s:s + chunk] = members[..., 0].std(0, unbiased=False).cpu().numpy()
+        out_d[s:s + chunk] = compose_t(metric, patch, geo, uvc, y.mean(0), obs_terms)
+        zstd_d[s:s + chunk] = members[..., 0].std(0, unbiased=False)
+    out, zstd = out_d.cpu().numpy(), zstd_d.cpu().numpy()
+    del out_d, zstd_d
     t_pred = time.perf_counter() - t0
     fallback = ~(zstd <= std_threshold) | ~np.isfinite(out).all(1)
     t1 = time.perf_counter()
