@@ -22,6 +22,7 @@
 #include <cstdint>
 
 #include "../../include/excalibur_gb300.h"
+#include "exc_divrn.cuh"
 
 namespace exc {
 void set_last_error(const char* msg);
@@ -78,7 +79,12 @@ __device__ __forceinline__ double simpson_term(double x0, double x1, double x2, 
   const double t0 = y0 * (2.0 - div0(1.0, h0divh1));
   const double t1 = y1 * (hsum * div0(hsum, hprod));
   const double t2 = y2 * (2.0 - h0divh1);
-  return hsum / 6.0 * ((t0 + t1) + t2);
+  // hsum / 6 as the correctly rounded quotient from RN(1/6) (div_rn: the IEEE quotient in three
+  // FP64 slots instead of about eight); operands below 2^-960, where the remainder could leave
+  // the normal range, take the division (the test is on the bits, on the integer pipe)
+  const bool big = ((unsigned long long)__double_as_longlong(hsum) & 0x7fffffffffffffffull) >= 0x03f0000000000000ull;
+  const double q6 = big ? div_rn(hsum, 6.0, 1.0 / 6.0) : hsum / 6.0;
+  return q6 * ((t0 + t1) + t2);
 }
 
 // the term of the pair starting at clean sample 2j

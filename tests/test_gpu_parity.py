@@ -447,7 +447,7 @@ def test_division_by_launch_constants_is_ieee(cuda):
     from excalibur_tool_gb300.core import constants as K
 
     cz = golden("cosmology.npz")
-    divs = [K.C2_F64, K.C4_F64, float(cz["eta_step"])]
+    divs = [K.C2_F64, K.C4_F64, float(cz["eta_step"]), 6.0]   # 6: the redshift table's Simpson terms
     for n in (32, 64, 96, 128, 256, 512):
         h = 1000 * K.one_Mpc / n
         divs += [h, 2.0 * h]
