@@ -139,6 +139,42 @@ def test_fused_inference_matches_layer_by_layer(cuda):
     assert cnt.value == 0
 
 
+@pytest.mark.parametrize("E,depth,n_out,m", [(1, 1, 1, 128), (3, 1, 8, 152 * 128 * 2 + 128), (2, 2, 3, 1280),
+                                           (5, 3, 6, 152 * 128 * 2), (4, 4, 7, 152 * 128 + 256)])
+def test_fused_inference_shapes_match_layer_by_layer(cuda, E, depth, n_out, m):
+    """exc_mlp_infer for other ensemble sizes, depths and head widths (one layer a member -- every
+    layer is a head --, fewer tiles than SMs, several tiles per CTA) against the layer-by-layer
+    kernels on random operands: the same bf16 activations, the head summed in another order."""
+    import torch
+    from excalibur_tool_gb300.surrogate import kernels as Kn
+
+    g = torch.Generator(device="cuda").manual_seed(E * 100 + depth * 10 + n_out)
+    x = (torch.rand((m, 256), generator=g, device="cuda") * 2 - 1).to(torch.bfloat16)
+    w = (torch.randn((depth, E, 256, 256), generator=g, device="cuda") * 0.08).to(torch.bfloat16)
+    b = torch.randn((depth, E, 256), generator=g, device="cuda") * 0.1
+    wh = torch.randn((E, n_out, 256), generator=g, device="cuda") * 0.1
+    bh = torch.randn((E, n_out), generator=g, device="cuda") * 0.1
+    y = torch.full((E, m, n_out), float("nan"), device="cuda")
+    Kn.infer(x, w, b, wh, bh, y)
+    inp = x
+    for l in range(depth):
+        o = torch.empty((E, m, 256), dtype=torch.bfloat16, device="cuda")
+        Kn.gemm(inp, w[l].contiguous(), epilogue="bias_silu", bias=b[l].contiguous(), c2=o)
+        inp = o
+    yr = torch.empty((E, m, n_out), device="cuda")
+    Kn.head(inp, wh, bh, y=yr)
+    torch.cuda.synchronize()
+    scale = float(yr.abs().max())
+    assert bool(torch.isfinite(y).all())
+    assert float((y - yr).abs().max()) <= 1e-5 * scale, float((y - yr).abs().max())
+    from excalibur_tool_gb300 import _native as N
+    import ctypes as C
+
+    cnt = C.c_uint32(0)
+    N.check(N.load().exc_mlp_error_count(C.byref(cnt)), "exc_mlp_error_count")
+    assert cnt.value == 0
+
+
 def test_graphed_training_equals_eager(cuda):
     """Training steps replayed from a captured CUDA graph (one multi-tensor Adam launch reading
     the step's schedule on the device) follow the eager loop (same batches, per-tensor Adam
