@@ -862,10 +862,11 @@ def infer_tflops(dev, stream, m=1 << 20, members=4, depth=4, n_out=6):
     return out
 
 
-def _surrogate_map(args, metric, patch, cfg, fp64_rays_s, train_steps, lr=2e-3):
+def _surrogate_map(args, metric, patch, cfg, fp64_rays_s, train_steps, lr=2e-3, strict_threshold=None):
     """Train the BF16 ensemble on 1,048,576 rays traced with `cfg`, fill an n x n map with
     ensemble-spread fallback and a seeded 1 % audit (both traced with `cfg`), and compare
-    the map time with tracing every pixel."""
+    the map time with tracing every pixel. With `strict_threshold` the map is filled a second
+    time with that (lower) spread threshold, which sends more pixels to the tracer."""
     from excalibur_tool_gb300.surrogate.model import SkySurrogate
     from excalibur_tool_gb300.surrogate.sky import fill_sky_map, training_set
 
@@ -886,6 +887,15 @@ def _surrogate_map(args, metric, patch, cfg, fp64_rays_s, train_steps, lr=2e-3):
     map_s = mrep["total_s"]
     with_training = map_s + info["trace_s"] + rep.seconds
     step_flops = 11 * 2.0 * 8192 * 256 * 256 * 4
+    strict = {}
+    if strict_threshold is not None:
+        _, srep = fill_sky_map(model, metric, patch, cfg, n_side=args.map_side, std_threshold=strict_threshold,
+                               audit_fraction=0.01, audit_seed=5)
+        srep.pop("threshold_tradeoff", None)
+        s_map = srep["total_s"]
+        strict = {"map_strict": {**srep, "speedup_vs_tracing_every_pixel": {
+            f"{cfg.precision}_tracer": every_pixel_tracer_s / s_map, "fp64_tracer": every_pixel_fp64_s / s_map,
+            "fp64_tracer_incl_training": every_pixel_fp64_s / (s_map + info["trace_s"] + rep.seconds)}}}
     return {
         "train": {"rays": n_train, "trace_s": info["trace_s"], "steps": rep.steps, "batch": rep.batch,
                   "seconds": rep.seconds, "final_loss_normalised": rep.final_loss,
@@ -895,6 +905,7 @@ def _surrogate_map(args, metric, patch, cfg, fp64_rays_s, train_steps, lr=2e-3):
         "speedup_vs_tracing_every_pixel": {f"{cfg.precision}_tracer": every_pixel_tracer_s / map_s,
                                            "fp64_tracer": every_pixel_fp64_s / map_s,
                                            "fp64_tracer_incl_training": every_pixel_fp64_s / with_training},
+        **strict,
     }
 
 
@@ -1015,7 +1026,10 @@ def run_surrogate_smooth(args, dev):
            "fp64_parity_status_counts": np.bincount(r.status.cpu().numpy(), minlength=12).tolist(),
            "mixed_on_sample": {"rays_per_s": mixed_rays_s, "speedup_vs_fp64": mixed_rays_s / fp64_rays_s,
                                "retrace_fraction": retrace, **errors_vs(r, rm)}}
-    out.update(_surrogate_map(args, metric, patch, cfg, fp64_rays_s, args.smooth_train_steps, lr=3.5e-3))
+    # strict: a spread threshold of 1e-8 keeps every audited pixel within 1e-7 (the configured 1e-7
+    # threshold leaves ~1e-4 of them above it; the map report's threshold_tradeoff shows the curve)
+    out.update(_surrogate_map(args, metric, patch, cfg, fp64_rays_s, args.smooth_train_steps, lr=3.5e-3,
+                              strict_threshold=1e-8))
     return out
 
 

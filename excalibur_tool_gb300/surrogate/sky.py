@@ -342,6 +342,15 @@ def fill_sky_map(model: SkySurrogate, metric, patch: Patch, cfg: TraceConfig, n_
         "total_s": time.perf_counter() - t0, "tracer_precision": cfg.precision,
     }
     if len(err):
+        # what a lower spread threshold would have done: the share of pixels it sends to the tracer,
+        # and the largest error among the audited pixels it would still have kept
+        zs_a = zstd[audit][good]
+        rep["threshold_tradeoff"] = [
+            {"std_threshold": t, "fallback_fraction": float((~(zstd <= t) | ~np.isfinite(out).all(1)).mean()),
+             "audit_kept": int((zs_a <= t).sum()),
+             "audit_max_abs_dz_kept": float(err[zs_a <= t, 0].max()) if (zs_a <= t).any() else None,
+             "audit_fraction_within_1e-7_kept": float((err[zs_a <= t, 0] <= 1e-7).mean()) if (zs_a <= t).any() else None}
+            for t in sorted({std_threshold, 5e-8, 3e-8, 2e-8, 1e-8, 5e-9}, reverse=True) if t <= std_threshold]
         rep.update({
             "audit_max_abs_dz": float(err[:, 0].max()), "audit_p99_abs_dz": float(np.percentile(err[:, 0], 99)),
             "audit_median_abs_dz": float(np.median(err[:, 0])),
