@@ -1151,10 +1151,10 @@ def parity_vs_oracle(res, idx, o):
 
 
 def reference_pool(states, n_rays=2048, n_steps=200):
-    """The reference's own multiprocessing path (Integrator(mode="chunked") from the package
-    installed under baseline/_ref, one worker per host core) on a linspace sample of the batch's
-    initial states, n_steps RK4 steps each, in a process of its own (oracle/reference_pool.py).
-    Returns its measurement, or {"unavailable": why}."""
+    """The reference's own multiprocessing paths (Integrator(mode="chunked"), then
+    PersistentPoolIntegrator, from the package installed under baseline/_ref, one worker per host
+    core) on a linspace sample of the batch's initial states, n_steps RK4 steps each, in a process
+    of its own (oracle/reference_pool.py). Returns its measurement, or {"unavailable": why}."""
     from excalibur_tool_gb300 import workloads
     from excalibur_tool_gb300.core.constants import one_Mpc
     from excalibur_tool_gb300.objects.fields import lens_plus_grf
@@ -1168,7 +1168,7 @@ def reference_pool(states, n_rays=2048, n_steps=200):
         np.savez(inp, phi=phi, box=workloads.BOX, states=np.asarray(states)[idx], dt=workloads.DLAMBDA,
                  n_steps=n_steps)
         r = subprocess.run([sys.executable, os.path.join(ROOT, "oracle", "reference_pool.py"), "--inputs", inp,
-                            "--out", out], capture_output=True, text=True, timeout=600)
+                            "--out", out, "--persistent"], capture_output=True, text=True, timeout=900)
         if r.returncode != 0:
             return {"unavailable": "reference pool run failed: " + (r.stderr.strip().splitlines() or ["?"])[-1]}
         with open(out) as f:

@@ -55,6 +55,8 @@ def main(argv=None):
     ap.add_argument("--ref-dir", default=os.path.join(REPO, "baseline", "_ref"))
     ap.add_argument("--workers", type=int, default=0, help="0: os.cpu_count()")
     ap.add_argument("--chunk-size", type=int, default=0, help="0: photons / workers, rounded up")
+    ap.add_argument("--persistent", action="store_true",
+                    help="also time PersistentPoolIntegrator (parallel_integrator_persistent.py) on the same photons")
     args = ap.parse_args(argv)
     if not os.path.isdir(os.path.join(args.ref_dir, "excalibur")):
         raise SystemExit(f"reference package not installed under {args.ref_dir}")
@@ -92,6 +94,8 @@ def main(argv=None):
     wall = time.perf_counter() - t0
     # the "steps" stop: every photon that did not raise took exactly n_steps accepted steps
     steps = int(ok) * n_steps
+    persistent = _time_persistent(metric, states, dt, n_steps, workers, chunk, Photons, Photon) \
+        if args.persistent else None
     try:
         affinity = len(os.sched_getaffinity(0))
     except AttributeError:
@@ -103,8 +107,52 @@ def main(argv=None):
            "python": platform.python_version(), "numpy": np.__version__, "machine": platform.machine(),
            "path": "excalibur.integration.integrator.Integrator(mode='chunked', integrator='rk4').integrate "
                    "(multiprocessing.Pool, fork), reference installed under baseline/_ref"}
+    if persistent is not None:
+        out["persistent_pool"] = persistent
     with open(args.out, "w") as f:
         json.dump(out, f)
+
+
+def _time_persistent(metric, states, dt, n_steps, workers, chunk, Photons, Photon):
+    """The reference's PersistentPoolIntegrator (excalibur/integration/parallel_integrator_persistent.py:
+    130-336): a pool whose workers each rebuild the grid, interpolator_fast.InterpolatorFast and a
+    PerturbedFLRWMetricFast with its finite-difference adot once at pool start (not timed), then
+    integrate_photons_chunked -> integrator_old.Integrator.integrate(photon, n_steps) per photon
+    (timed). Its arithmetic differs from Integrator's (no dt clip, the FD adot, the legacy
+    interpolator's strict interior), so it is a rate, not a parity reference. That interpolator
+    raises on the grid's outer cells, where the batch's observer sits (x = 0), and the worker
+    evaluates the metric before its own try block, so each photon starts two cells further along
+    its ray. Steps are counted from the returned history lengths (one record before the first step
+    and one per step)."""
+    import contextlib
+    import io
+
+    import numpy as np
+    from excalibur.integration.parallel_integrator_persistent import PersistentPoolIntegrator
+
+    cell = float(np.max(metric.grid.spacing))
+    photons = Photons(metric)
+    for s in states:
+        x = s[:4].copy()
+        d = s[5:8] / np.linalg.norm(s[5:8])
+        x[1:4] += 2.0 * cell * d
+        photons.photons.append(Photon(x, s[4:].copy()))
+    t0 = time.perf_counter()
+    with contextlib.redirect_stdout(io.StringIO()):
+        pool = PersistentPoolIntegrator(metric, dt, n_workers=workers)
+    t_start = time.perf_counter() - t0
+    try:
+        t1 = time.perf_counter()
+        with contextlib.redirect_stdout(io.StringIO()):
+            n_ok, results = pool.integrate_photons_chunked(photons, n_steps, chunk_size=chunk, verbose=False)
+        wall = time.perf_counter() - t1
+    finally:
+        pool.close()
+    steps = int(sum(max(int(r[3]) - 1, 0) for r in results))
+    return {"photon_steps_per_s": steps / wall, "seconds": wall, "pool_start_s": t_start, "succeeded": int(n_ok),
+            "photon_steps": steps, "workers": workers, "chunk_size": chunk,
+            "path": "excalibur.integration.parallel_integrator_persistent.PersistentPoolIntegrator"
+                    ".integrate_photons_chunked (multiprocessing.Pool, fork; workers built once)"}
 
 
 if __name__ == "__main__":
