@@ -1272,8 +1272,10 @@ int exc_mlp_infer(const ExcMlpInfer* a, void* stream) {
   if (a->n_members < 1 || a->depth < 1 || (int64_t)a->depth * a->n_members > 65535)
     return mlp_fail(EXC_ERR_INVALID, "infer: n_members and depth must be >= 1");
   if (a->n_out < 1 || a->n_out > kInferMaxOut) return mlp_fail(EXC_ERR_INVALID, "infer: n_out must be in [1, 8]");
-  if (!a->x || !a->w || !a->b || !a->w_head || !a->b_head || !a->y || !aligned16(a->x) || !aligned16(a->w))
-    return mlp_fail(EXC_ERR_INVALID, "infer: x, w (16-byte aligned), b, w_head, b_head and y are required");
+  if (!a->x || !a->w || !a->b || !a->w_head || !a->b_head || !a->y || !aligned16(a->x) || !aligned16(a->w) ||
+      !aligned16(a->w_head) || ((uintptr_t)a->b & 7u))
+    return mlp_fail(EXC_ERR_INVALID,
+                    "infer: x, w, w_head (16-byte aligned), b (8-byte aligned), b_head and y are required");
   if (a->m > (int64_t)INT32_MAX - kTileM) return mlp_fail(EXC_ERR_INVALID, "infer: m too large for one launch");
   CUtensorMap tx, tw;
   if (!make_map(&tx, a->x, a->m, 256, 0, 1, kTileM) ||

@@ -86,7 +86,8 @@ int exc_mlp_head(const void* h, int64_t m, int32_t width, int32_t n_out, int32_t
  * x: [m][width] bf16 (m a multiple of 128); w: [depth][n_members][width][width] bf16 (layer l of
  * member e maps its input through w[l][e] (out x in)); b: [depth][n_members][width] f32;
  * w_head: [n_members][n_out][width] f32; b_head: [n_members][n_out] f32; y: [n_members][m][n_out]
- * f32. Limits: width 256, n_out <= 8. No reference counterpart (the surrogate is new). */
+ * f32. x, w and w_head 16-byte aligned, b 8-byte aligned (vector loads). Limits: width 256,
+ * n_out <= 8. No reference counterpart (the surrogate is new). */
 typedef struct ExcMlpInfer {
   const void* x;
   const void* w;

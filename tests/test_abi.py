@@ -221,3 +221,23 @@ def test_map_entry_points_validate_before_any_launch(lib):
     assert L.exc_sky_bin(P, P, P, 10, 4, 4, bad, P, P, P, None) == N.EXC_ERR_INVALID
     assert b"x1 > x0" in L.exc_last_error()
     assert L.exc_sky_bin(None, P, P, 10, 4, 4, ext, P, P, P, None) == N.EXC_ERR_INVALID
+
+
+def test_fused_inference_validates_on_the_host(lib):
+    """exc_mlp_infer refuses bad shapes and pointers that its vector loads could not take (a
+    misaligned head weight or bias) before any device work."""
+    L = N.load()
+
+    def args(**kw):
+        a = N.ExcMlpInfer()
+        a.x, a.w, a.b, a.w_head, a.b_head, a.y = 4096, 8192, 4096, 4096, 4096, 4096
+        a.m, a.width, a.n_members, a.n_out, a.depth = 256, 256, 4, 6, 4
+        for k, v in kw.items():
+            setattr(a, k, v)
+        return a
+
+    for kw, msg in ((dict(m=100), b"multiple of 128"), (dict(width=128), b"width"), (dict(n_out=9), b"n_out"),
+                    (dict(depth=0), b"depth"), (dict(w_head=4100), b"aligned"), (dict(b=4100), b"aligned"),
+                    (dict(x=4104), b"aligned"), (dict(y=None), b"required")):
+        assert L.exc_mlp_infer(C.byref(args(**kw)), None) == N.EXC_ERR_INVALID, kw
+        assert msg in L.exc_last_error(), (kw, L.exc_last_error())
