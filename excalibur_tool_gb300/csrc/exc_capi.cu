@@ -221,8 +221,12 @@ int exc_trace(const ExcMetric* metric, const ExcTraceArgs* a, void* stream) {
         if (ce != cudaSuccess) return cuda_fail(ce, "queue reset");
       }
       D.retrace_only = 1;
+      D.retrace_sms = sms;
       D.stage_table = stage_table;
-      ce = exc_fast::trace(D, *a, block, a->blocks_per_sm, sms, s);
+      // with a work queue the re-trace launch fills the SMs and sizes its active blocks on the
+      // device from the handed-back share (trace_kernel); the plan's blocks per SM is the mixed
+      // pass's
+      ce = exc_fast::trace(D, *a, block, a->queue ? 0 : a->blocks_per_sm, sms, s);
       if (ce != cudaSuccess) return cuda_fail(ce, "re-trace launch");
     }
     return EXC_SUCCESS;

@@ -12,6 +12,7 @@ struct DevMetric {
   double finv[EXC_MAX_FIELDS][8];   // 1/s0, 1/s1, 1/s2, 1/s3, 1/(2 s0), 1/(2 s1), 1/(2 s2), 1/(2 s3)
   int retrace_only;                 // trace only photons whose status is EXC_PH_RETRACE
   int stage_table;                  // the a(eta) table is read from the block's shared-memory copy
+  int retrace_sms;                  // SMs of the device (re-trace launches: sizes the active blocks)
 };
 
 }  // namespace exc

@@ -505,10 +505,35 @@ __device__ __forceinline__ int64_t next_work(const DevMetric& D, const ExcTraceA
 
 template <int MK, class FT, int STEPPER, bool REC>
 __global__ void __launch_bounds__(128) trace_kernel(const DevMetric D, const ExcTraceArgs A) {
+  // Re-tracing the rays the mixed tracer handed back. A few of them (a guard's share of one
+  // batch) run fastest in as few warps an SM as hold them: the warps of an SM share its FP64
+  // throughput, and a lone warp's dependent FP64 chain waits least. Many run fastest with every
+  // resident warp. The share is estimated from the same 1,024 statuses in every block; the warps
+  // an SM needs at 32 rays a warp stay (blocks 0 .. SMs-1 first, one on each SM as the launch
+  // hands them out), the rest leave at once -- the work queue hands every ray to the warps that
+  // stay (the static assignment, without a queue, keeps every warp).
+  bool retrace_idle = false;
+  if (D.retrace_only && A.queue) {
+    __shared__ int s_hits;
+    if (threadIdx.x == 0) s_hits = 0;
+    __syncthreads();
+    int hits = 0;
+    for (int k = threadIdx.x; k < 1024; k += blockDim.x)
+      hits += A.status[(int64_t)k * A.n_photons / 1024] == EXC_PH_RETRACE;
+    if (hits) atomicAdd(&s_hits, hits);
+    __syncthreads();
+    const double rays = (double)s_hits * (double)A.n_photons * (1.0 / 1024.0);
+    const int sms = D.retrace_sms > 0 ? D.retrace_sms : 1;
+    const double need = ceil(rays / ((double)sms * 32.0));   // warps an SM
+    const int warps = blockDim.x >> 5;
+    const double rank = (double)(blockIdx.x / sms) * warps + (threadIdx.x >> 5);   // the warp's rank on its SM
+    retrace_idle = rank >= (need < 1.0 ? 1.0 : need);
+  }
   if (D.stage_table) {
     for (int64_t i = threadIdx.x; i < D.m.a_table_n; i += blockDim.x) stage_tab_s[i] = __ldg(D.m.a_table + i);
     __syncthreads();
   }
+  if (retrace_idle) return;   // warp-uniform, and no block barrier follows
   Tracer<MK, FT> T(D, A);
   Photon P;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;

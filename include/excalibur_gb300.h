@@ -220,7 +220,9 @@ typedef struct ExcTraceArgs {
   int32_t stop_flags;            /* EXC_STOP_* */
   int32_t obs_flags;             /* EXC_OBS_* bits */
   int32_t block_size;            /* 0 = library default */
-  int32_t blocks_per_sm;         /* 0 = library default */
+  int32_t blocks_per_sm;         /* 0 = library default (EXC_PREC_MIXED with a queue: the
+                                    mixed pass's; its FP64 re-trace pass sizes itself on the
+                                    device from the share of rays handed back) */
   int32_t staging;               /* EXC_STAGING_*: where the FP64 tracers read the a(eta) table */
   double dt, dt_min, dt_max, rtol, atol;
   int64_t max_iter;              /* reference: 10000 */
