@@ -145,6 +145,24 @@ def test_mixed_raw_hands_back_untouched_rays(patch):
     assert rel_err(mixed["state"][back], o.state[back]).max() <= 1e-12
 
 
+def test_device_sized_retrace_equals_every_warp(patch):
+    """The re-trace pass with the work queue keeps one warp an SM for the ~1,000 rays handed back
+    on the lens patch (the rest of the launch leaves at once); without the queue every warp takes
+    its static share. The results are the same bits, and for several schedules of the launch."""
+    import torch
+    from excalibur_tool_gb300.trace import trace_batch
+
+    wl, states, o = patch
+    cfg = dataclasses.replace(wl.cfg, precision="mixed")
+    ref = trace_batch(wl.metric, wl.states, dataclasses.replace(cfg, use_queue=False))
+    for block, per_sm in ((0, 0), (64, 4), (128, 4), (96, 3)):
+        got = trace_batch(wl.metric, wl.states, dataclasses.replace(cfg, block_size=block, blocks_per_sm=per_sm))
+        torch.cuda.synchronize()
+        for k in ("state", "status", "n_steps", "n_iter"):
+            assert torch.equal(getattr(got, k), getattr(ref, k)), (k, block, per_sm)
+        assert torch.allclose(got.obs, ref.obs, rtol=0, atol=0, equal_nan=True)
+
+
 def test_pipelined_batches_match_single_launches(patch):
     """Re-traces overlapped on a side stream give the same photons as precision "mixed"."""
     import torch
