@@ -89,3 +89,33 @@ def test_records_to_runner_layout(cuda, tmp_path):
         assert rel_err(traj[i, :n[i]], o.records[i, :n[i]]).max() <= 1e-12
     p = write_trajectories(str(tmp_path / "t.h5"), traj, {"record_every": 7})
     assert np.array_equal(np.load(p)["trajectories"] if p.endswith(".npz") else traj, traj, equal_nan=True)
+
+
+def test_staged_table_with_records_and_isw(cuda):
+    """The a(eta) table staged in shared memory (TraceConfig.staging = "shared") in the
+    record-writing kernel with a time-dependent potential: records, states and the ISW integral
+    are the same bits as with the table read through the cache."""
+    import dataclasses
+
+    import torch
+    from excalibur_tool_gb300.core.constants import c, one_Mpc
+    from excalibur_tool_gb300.trace import trace_batch
+    from helpers import gpu_metric
+
+    spec, eta1, box = _spec4d()
+    st = torch.as_tensor(_states(spec, eta1, 6)).cuda()
+    dl = 0.5 * one_Mpc / c
+    cfg = TraceConfig(stepper="rk4", dt=dl, dt_min=dl, dt_max=dl, max_steps=300, max_iter=300, record_every=3,
+                      isw=True)
+    m = gpu_metric(spec)
+    a = trace_batch(m, st, cfg)
+    b = trace_batch(m, st, dataclasses.replace(cfg, staging="shared"))
+    torch.cuda.synchronize()
+    for k in ("state", "status", "n_steps", "n_records"):
+        assert torch.equal(getattr(a, k), getattr(b, k)), k
+    n = a.n_records.cpu().numpy()
+    ra, rb = a.records.cpu().numpy(), b.records.cpu().numpy()
+    assert n.min() > 10
+    for i in range(len(n)):   # the recorded rows (the buffer past them is not written)
+        assert np.array_equal(ra[i, :n[i]], rb[i, :n[i]], equal_nan=True), i
+    assert torch.allclose(a.obs, b.obs, rtol=0, atol=0, equal_nan=True)
