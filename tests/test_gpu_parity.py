@@ -1,7 +1,7 @@
 """GPU parity: the CUDA tracer (through the C ABI) against the reference's
 golden vectors and against the C oracle on identical seeded inputs.
 
-Tolerances (spec: 1e-12 relative on final state and observables):
+Tolerances (the parity target: 1e-12 relative on final state and observables):
 * FLRW, parity build ("fp64"): the reference's IEEE operation order with no
   FMA contraction -> bit-identical interpolation/RHS/RK4. The one exception is
   x**3 in adot: the library's correctly rounded double-double cube, where the
