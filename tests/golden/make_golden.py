@@ -423,8 +423,8 @@ def gen_integrate_modes(cz):
     save("integrate_modes.npz", **out)
 
 
-# ------------------------------------------------------------- cfg1 subset
-def cfg1_initial_states():
+# ------------------------------------------------ Schwarzschild polar cone, 1,024 rays
+def schw_polar_initial_states():
     """1024 photons: Schwarzschild lens (1e15 Msun at the box centre), observer at (0,500,500) Mpc,
     32x32 polar grid theta_i = (i+1/2) 5deg/32, phi_j = 2 pi j/32, rotated onto the lens direction with
     the reference's Rodrigues formula, spherical velocities via cartesian_velocity_to_spherical and
@@ -456,8 +456,8 @@ def cfg1_initial_states():
     return m, states
 
 
-def gen_cfg1():
-    m, states = cfg1_initial_states()
+def gen_schw_polar():
+    m, states = schw_polar_initial_states()
     dl = 0.5 * one_Mpc / c
     rng = np.random.default_rng(101)
     sel = np.unique(np.concatenate([[0, 1, 8, 15, 16, 17, 31, 511, 520, 1023],
@@ -476,13 +476,13 @@ def gen_cfg1():
         finals.append(s)
         status.append(st)
         nsteps.append(k)
-    save("cfg1.npz", states=states, sel=sel, final=np.array(finals), failed=np.array(status),
+    save("schw_polar_1024.npz", states=states, sel=sel, final=np.array(finals), failed=np.array(status),
          n_steps=np.array(nsteps), dl=dl, mass=m.mass, radius=m.radius)
 
 
-# ------------------------------------------------------------- cfg2 (small)
-def gen_cfg2_small(cz):
-    """cfg2 construction on a 32^3 grid: Plummer (1e15 Msun, eps 5 Mpc) + GRF (seed 2, rms 1e-5),
+# ------------------------------------------------ FLRW lens + random-field patch, 32^3
+def gen_flrw_patch_32(cz):
+    """The lens patch construction on a 32^3 grid: Plummer (1e15 Msun, eps 5 Mpc) + GRF (seed 2, rms 1e-5),
     periodic interpolation, LCDM, observer (0,500,500) Mpc at eta = _eta_at_a1, 6x6 directions in a
     10x10 degree tangent patch, RK4 dl = 0.5 Mpc/c, stop at box exit (after each accepted step)."""
     n, box = 32, 1000 * one_Mpc
@@ -520,7 +520,7 @@ def gen_cfg2_small(cz):
                 break
         finals.append(s)
         nsteps.append(steps)
-    save("cfg2_small.npz", field=phi, box=box, states=states, final=np.array(finals), n_steps=np.array(nsteps),
+    save("flrw_patch_32.npz", field=phi, box=box, states=states, final=np.array(finals), n_steps=np.array(nsteps),
          dl=dl)
 
 
@@ -781,7 +781,7 @@ def gen_time_delays():
 
 
 GENERATORS = ["cosmology", "interp", "interp_slow", "rhs", "steps", "integrate", "integrate_modes", "generators",
-              "observables", "cfg2_small", "cfg1", "compare_job", "manifest", "time_delays"]
+              "observables", "flrw_patch_32", "schw_polar", "compare_job", "manifest", "time_delays"]
 
 if __name__ == "__main__":
     if not os.path.isdir(REF):
@@ -790,11 +790,11 @@ if __name__ == "__main__":
     which = sys.argv[1:] or GENERATORS
     cz = gen_cosmology() if "cosmology" in which else None
     if cz is None and set(which) & {"interp_slow", "rhs", "steps", "integrate", "integrate_modes", "generators",
-                                    "observables", "cfg2_small"}:
+                                    "observables", "flrw_patch_32"}:
         cz = LCDM_Cosmology(70, 0.3, 0.0, 0.7)
     for name in which:
         if name == "cosmology":
             continue
         fn = globals()["gen_" + name]
         fn(cz) if name in ("interp_slow", "rhs", "steps", "integrate", "integrate_modes", "generators",
-                           "observables", "cfg2_small") else fn()
+                           "observables", "flrw_patch_32") else fn()

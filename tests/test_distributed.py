@@ -86,10 +86,10 @@ def _shard_worker(rank, world, port, out):
     import bench
     from excalibur_tool_gb300.distributed import gather_rows, shard_range
     from oracle import oracle as O
-    from test_gpu_parity import _cfg2_like
+    from test_gpu_parity import _flrw_patch_case
 
     r, w, _ = bench.dist_setup(world)
-    spec, st, cfg = _cfg2_like(16, 5)          # 25 rays through a 16^3 lens-plus-random-field box
+    spec, st, cfg = _flrw_patch_case(16, 5)          # 25 rays through a 16^3 lens-plus-random-field box
     a, b = shard_range(len(st), r, w)
     mine = O.trace(spec, st[a:b], cfg, threads=1)
     cols = np.concatenate([mine.state, mine.status[:, None], mine.n_steps[:, None], mine.obs], axis=1)
@@ -107,7 +107,7 @@ def test_two_rank_sharded_trace_gathers_the_whole_batch():
 
     sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
     from oracle import oracle as O
-    from test_gpu_parity import _cfg2_like
+    from test_gpu_parity import _flrw_patch_case
 
     ctx = mp.get_context("spawn")
     mgr = ctx.Manager()
@@ -119,7 +119,7 @@ def test_two_rank_sharded_trace_gathers_the_whole_batch():
     for p in procs:
         p.join(timeout=300)
     assert all(p.exitcode == 0 for p in procs)
-    spec, st, cfg = _cfg2_like(16, 5)
+    spec, st, cfg = _flrw_patch_case(16, 5)
     whole = O.trace(spec, st, cfg, threads=1)
     want = np.concatenate([whole.state, whole.status[:, None], whole.n_steps[:, None], whole.obs], axis=1)
     for r in range(2):

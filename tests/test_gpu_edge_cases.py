@@ -12,7 +12,7 @@ pytestmark = pytest.mark.gpu
 
 
 def _setup():
-    g = golden("cfg2_small.npz")
+    g = golden("flrw_patch_32.npz")
     box = float(g["box"])
     m = gpu_metric(lcdm_spacetime(g["field"], box))
     dl = float(g["dl"])

@@ -22,7 +22,7 @@ import numpy as np
 import pytest
 
 from helpers import gpu_trace, rel_err
-from test_gpu_parity import _cfg2_like
+from test_gpu_parity import _flrw_patch_case
 from excalibur_tool_gb300 import _native as N
 from excalibur_tool_gb300.observables import lensing as L
 from oracle import oracle as O
@@ -51,7 +51,7 @@ def _check_observables(r, o):
 
 @pytest.mark.parametrize("n_grid,side", [(128, 24), (32, 16)])
 def test_mixed_matches_fp64_oracle(cuda, n_grid, side):
-    spec, st, cfg = _cfg2_like(n_grid, side)
+    spec, st, cfg = _flrw_patch_case(n_grid, side)
     cfg = dataclasses.replace(cfg, precision="mixed")
     r = gpu_trace(spec, st, cfg)
     o = O.trace(spec, st, cfg, threads=8)
@@ -61,7 +61,7 @@ def test_mixed_matches_fp64_oracle(cuda, n_grid, side):
 @pytest.mark.parametrize("a_stop,max_steps,want", [(0.93, 10000, "A_STOP"), (None, 300, "STEPS")])
 def test_mixed_a_stop_and_step_cap(cuda, a_stop, max_steps, want):
     """The a(eta) stop and the step cap end photons where the FP64 tracer does."""
-    spec, st, cfg = _cfg2_like(32, 8)
+    spec, st, cfg = _flrw_patch_case(32, 8)
     cfg = dataclasses.replace(cfg, precision="mixed", a_stop=a_stop, max_steps=max_steps)
     r = gpu_trace(spec, st, cfg)
     o = O.trace(spec, st, cfg, threads=8)
@@ -70,7 +70,7 @@ def test_mixed_a_stop_and_step_cap(cuda, a_stop, max_steps, want):
 
 
 def test_mixed_queue_and_static_schedules_agree(cuda):
-    spec, st, cfg = _cfg2_like(32, 12)
+    spec, st, cfg = _flrw_patch_case(32, 12)
     cfg = dataclasses.replace(cfg, precision="mixed")
     a = gpu_trace(spec, st, dataclasses.replace(cfg, use_queue=True))
     b = gpu_trace(spec, st, dataclasses.replace(cfg, use_queue=False))
@@ -84,7 +84,7 @@ def test_mixed_float32_grid(cuda):
     from helpers import gpu_metric
     from excalibur_tool_gb300.trace import trace_batch
 
-    spec, st, cfg = _cfg2_like(32, 8)
+    spec, st, cfg = _flrw_patch_case(32, 8)
     spec.fields[0].data = spec.fields[0].data.astype(np.float32).astype(np.float64)
     cfg = dataclasses.replace(cfg, precision="mixed")
     m = gpu_metric(spec, field_dtype=np.float32)
@@ -186,7 +186,7 @@ def test_mixed_slow_interpolator_matches_fp64_oracle(cuda, n_grid, side):
     here the formula changes only at the grid's outer cells, which the rays do not reach)."""
     from excalibur_tool_gb300.core.constants import one_Mpc
 
-    spec, st, cfg = _cfg2_like(n_grid, side)
+    spec, st, cfg = _flrw_patch_case(n_grid, side)
     spec.fields[0].boundary = "error"
     spec.fields[0].gradient = "trilinear"
     hi = 990 * one_Mpc if n_grid == 128 else 960 * one_Mpc     # inside the bounds [0, (n-1) spacing)
@@ -205,7 +205,7 @@ def _rk45_face_case(n_grid, side, renormalize_every=0):
     1.5 cells inside the last node (the slow class's bounds)."""
     from excalibur_tool_gb300.core.constants import one_Mpc
 
-    spec, st, cfg = _cfg2_like(n_grid, side)
+    spec, st, cfg = _flrw_patch_case(n_grid, side)
     spec.fields[0].gradient = "trilinear"
     hi = (n_grid - 1.5) * 1000 * one_Mpc / n_grid
     cfg = dataclasses.replace(cfg, stepper="rk45", tableau="fehlberg", rtol=1e-8, atol=1e-12, dt_min=1e10,
@@ -269,7 +269,7 @@ def test_mixed_renormalisation_matches_fp64_oracle(cuda):
     about -1.24 across the patch while |u|/c grows to 1.49), so each renormalisation moves u^0
     by a finite amount, and with RK45 "every N accepted steps" falls where each tracer's step
     sequence puts it."""
-    spec, st, cfg = _cfg2_like(32, 8)
+    spec, st, cfg = _flrw_patch_case(32, 8)
     cfg = dataclasses.replace(cfg, renormalize_every=10)
     r = gpu_trace(spec, st, dataclasses.replace(cfg, precision="mixed"))
     o = O.trace(spec, st, cfg, threads=8)

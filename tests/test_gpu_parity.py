@@ -188,8 +188,8 @@ def test_steppers_match_oracle(cuda):
         assert np.array_equal(r["state"], o.state) and np.array_equal(r["dt"], o.dt), stepper
 
 
-def test_cfg1_subset_matches_reference(cuda):
-    g = golden("cfg1.npz")
+def test_schw_polar_subset_matches_reference(cuda):
+    g = golden("schw_polar_1024.npz")
     spec = schw_spacetime(float(g["mass"]), float(g["radius"]))
     dl = float(g["dl"])
     sel = g["sel"]
@@ -206,8 +206,8 @@ def test_cfg1_subset_matches_reference(cuda):
     assert err[ok & pole].max() <= 1e-8
 
 
-def test_cfg2_small_matches_reference(cuda):
-    g = golden("cfg2_small.npz")
+def test_flrw_patch_32_matches_reference(cuda):
+    g = golden("flrw_patch_32.npz")
     box = float(g["box"])
     spec = lcdm_spacetime(g["field"], box)
     dl = float(g["dl"])
@@ -219,8 +219,8 @@ def test_cfg2_small_matches_reference(cuda):
     assert rel_err(r["state"], g["final"]).max() <= 1e-13
 
 
-def test_cfg1_full_matches_oracle(cuda):
-    g = golden("cfg1.npz")
+def test_schw_polar_full_matches_oracle(cuda):
+    g = golden("schw_polar_1024.npz")
     spec = schw_spacetime(float(g["mass"]), float(g["radius"]))
     dl = float(g["dl"])
     cfg = TraceConfig(stepper="rk4", dt=dl, dt_min=dl, dt_max=dl, max_steps=2000, observables=True)
@@ -239,7 +239,7 @@ def test_cfg1_full_matches_oracle(cuda):
         assert rel_err(r["obs"][good, i], o.obs[good, i], floor=1.0).max() <= 1e-12, col
 
 
-def _cfg2_like(n_grid, n_side, seed=2, pick=None):
+def _flrw_patch_case(n_grid, n_side, seed=2, pick=None):
     from excalibur_tool_gb300.objects.fields import lens_plus_grf
     from excalibur_tool_gb300.core.constants import one_Mpc, one_Msun, c
 
@@ -293,17 +293,17 @@ def _assert_matches_oracle(r, spec, st, cfg, tol):
             assert rel_err(r["obs"][:, i], o.obs[:, i]).max() <= tol, col
 
 
-def test_cfg2_grid128_matches_oracle(cuda):
-    spec, st, cfg = _cfg2_like(128, 24)
+def test_flrw_patch_grid128_matches_oracle(cuda):
+    spec, st, cfg = _flrw_patch_case(128, 24)
     r = gpu_trace(spec, st, cfg)
     _assert_matches_oracle(r, spec, st, cfg, 1e-12)
 
 
-def test_cfg2_patch_subset_matches_oracle(cuda):
+def test_flrw_patch_subset_matches_oracle(cuda):
     """4,096 seeded pixels of the 256 x 256 patch of the 65,536-ray FLRW workload (128^3 Plummer +
     random-field potential, LCDM, RK4 at 0.5 Mpc to box exit), the benchmark's own geometry."""
     pick = np.sort(np.random.default_rng(22).choice(256 * 256, 4096, replace=False))
-    spec, st, cfg = _cfg2_like(128, 256, pick=pick)
+    spec, st, cfg = _flrw_patch_case(128, 256, pick=pick)
     r = gpu_trace(spec, st, cfg)
     assert (r["status"] == N.PH_LEFT_BOX).all()
     _assert_matches_oracle(r, spec, st, cfg, 1e-12)
@@ -319,7 +319,7 @@ def test_box_face_stop_matches_oracle(cuda, stepper, gradient):
 
     from excalibur_tool_gb300.core.constants import one_Mpc
 
-    spec, st, cfg = _cfg2_like(32, 8)
+    spec, st, cfg = _flrw_patch_case(32, 8)
     spec.fields[0].gradient = gradient
     hi = 1000 * one_Mpc if gradient == "base_node" else 29.5 * 1000 * one_Mpc / 32   # slow class: inside its nodes
     kw = dict(stop_face=True, stop_box=((0.0, 0.0, 0.0), (hi, hi, hi)))
@@ -339,10 +339,10 @@ def test_box_face_stop_matches_oracle(cuda, stepper, gradient):
     assert np.abs(to_face).max() <= (1e-3 if stepper == "rk4" else 0.05) * one_Mpc
 
 
-def test_cfg2_grid128_fast_build_matches_oracle(cuda):
+def test_flrw_patch_grid128_fast_build_matches_oracle(cuda):
     import dataclasses
 
-    spec, st, cfg = _cfg2_like(128, 24)
+    spec, st, cfg = _flrw_patch_case(128, 24)
     cfg = dataclasses.replace(cfg, precision="fp64_fast")
     r = gpu_trace(spec, st, cfg)
     o = O.trace(spec, st, cfg, threads=8)
@@ -357,7 +357,7 @@ def test_cfg2_grid128_fast_build_matches_oracle(cuda):
 def test_queue_and_static_schedules_agree(cuda):
     import dataclasses
 
-    spec, st, cfg = _cfg2_like(32, 12)
+    spec, st, cfg = _flrw_patch_case(32, 12)
     a = gpu_trace(spec, st, dataclasses.replace(cfg, use_queue=True))
     b = gpu_trace(spec, st, dataclasses.replace(cfg, use_queue=False))
     for k in ("state", "status", "n_steps", "obs"):
@@ -369,7 +369,7 @@ def test_multi_field_batch_matches_single(cuda):
     from excalibur_tool_gb300.objects.fields import lens_plus_grf
     from excalibur_tool_gb300.core.constants import one_Mpc, one_Msun
 
-    spec, st, cfg = _cfg2_like(32, 8)
+    spec, st, cfg = _flrw_patch_case(32, 8)
     box = 1000 * one_Mpc
     lens = np.array([500.0, 500.0, 500.0]) * one_Mpc
     f2 = lens_plus_grf(16, box, 1e15 * one_Msun, 5 * one_Mpc, lens, seed=5)
@@ -416,7 +416,7 @@ def test_abort_flag_and_deadline(cuda):
     import torch
     from excalibur_tool_gb300.trace import trace_batch
 
-    spec, st, cfg = _cfg2_like(32, 16)
+    spec, st, cfg = _flrw_patch_case(32, 16)
     m = gpu_metric(spec)
     s = torch.as_tensor(st).cuda()
     flag = torch.ones(1, dtype=torch.int32, device="cuda")

@@ -27,7 +27,7 @@ def test_operator_equals_trace_batch(cuda):
     from excalibur_tool_gb300 import ops
     from excalibur_tool_gb300.trace import TraceConfig, trace_batch
 
-    g = golden("cfg2_small.npz")
+    g = golden("flrw_patch_32.npz")
     spec = lcdm_spacetime(g["field"], float(g["box"]))
     m = gpu_metric(spec)
     states = torch.as_tensor(g["states"], device=cuda)

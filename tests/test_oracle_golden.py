@@ -143,8 +143,8 @@ def test_integrate_single_records(k):
     assert rel_err(got[:, 8:][q], want[:, 8:][q]).max() <= (1e-8 if is45 else tol)
 
 
-def test_cfg1_subset_matches_reference():
-    g = golden("cfg1.npz")
+def test_schw_polar_subset_matches_reference():
+    g = golden("schw_polar_1024.npz")
     st = schw_spacetime(float(g["mass"]), float(g["radius"]), center=(0, 0, 0))
     dl = float(g["dl"])
     sel = g["sel"]
@@ -157,8 +157,8 @@ def test_cfg1_subset_matches_reference():
     assert np.array_equal(res.state[ok], g["final"][ok])
 
 
-def test_cfg2_small_matches_reference():
-    g = golden("cfg2_small.npz")
+def test_flrw_patch_32_matches_reference():
+    g = golden("flrw_patch_32.npz")
     box = float(g["box"])
     st = lcdm_spacetime(g["field"], box)
     dl = float(g["dl"])

@@ -15,7 +15,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 @pytest.mark.skipif(not os.path.isdir(os.path.join(ROOT, "baseline", "_ref", "excalibur")),
                     reason="reference package not installed under baseline/_ref")
 def test_reference_pools_run_and_report(tmp_path):
-    d = np.load(os.path.join(ROOT, "tests", "golden", "cfg2_small.npz"))
+    d = np.load(os.path.join(ROOT, "tests", "golden", "flrw_patch_32.npz"))
     inp, out = tmp_path / "in.npz", tmp_path / "out.json"
     np.savez(inp, phi=d["field"], box=float(d["box"]), states=d["states"][:6], dt=float(d["dl"]), n_steps=5)
     r = subprocess.run([sys.executable, os.path.join(ROOT, "oracle", "reference_pool.py"), "--inputs", str(inp),
