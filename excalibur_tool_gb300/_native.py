@@ -92,7 +92,7 @@ class ExcPhotonGen(C.Structure):
                 ("reserved", C.c_int32), ("b_edges", C.c_void_p), ("bin_offsets", C.c_void_p)]
 
 
-EXC_TUNE_MAX_TRIALS = 32
+EXC_TUNE_MAX_TRIALS = 48
 # where the FP64 tracers read the a(eta) table (ExcTraceArgs.staging)
 STAGING = {"cache": 0, "shared": 1}
 STAGING_MAX_TABLE = 12288

@@ -34,8 +34,8 @@ extern "C" int exc_autotune(const ExcMetric* metric, const ExcTraceArgs* args, c
   cudaStream_t s = (cudaStream_t)stream;
   const size_t bytes = (size_t)args->n_photons * 8 * sizeof(double);
   int cand_b[EXC_TUNE_MAX_TRIALS], cand_p[EXC_TUNE_MAX_TRIALS], n = 0;
-  const int per_sm[] = {0, 2, 3, 4, 5, 6, 8};
-  for (int b = 64; b <= 128; b += 32)
+  const int per_sm[] = {0, 2, 3, 4, 5, 6, 7, 8};
+  for (int b = 32; b <= 128; b += 32)
     for (int p : per_sm)
       if (p * b <= 2048 && n < EXC_TUNE_MAX_TRIALS) {
         cand_b[n] = b;
@@ -48,7 +48,7 @@ extern "C" int exc_autotune(const ExcMetric* metric, const ExcTraceArgs* args, c
                     args->precision == EXC_PREC_MIXED || args->precision == EXC_PREC_RETRACE;
   const bool can_stage = fp64 && metric->kind == EXC_METRIC_FLRW && metric->cosmology != EXC_COSMO_STATIC &&
                          metric->a_table_n <= EXC_STAGING_MAX_TABLE;
-  const int n_staged = can_stage ? 3 : 0;
+  const int n_staged = can_stage ? (EXC_TUNE_MAX_TRIALS - n_cache < 3 ? EXC_TUNE_MAX_TRIALS - n_cache : 3) : 0;
   cudaEvent_t e0, e1;
   if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
     exc::set_last_error("autotune: cudaEventCreate failed");

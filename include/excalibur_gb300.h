@@ -358,8 +358,9 @@ int exc_spherical_mass_grid(const int64_t n[3], const double origin[3], const do
 
 /* ---- launch-schedule autotuner (no reference counterpart: the reference has no
  * GPU schedule). Runs exc_trace on a sample batch for each candidate (block size
- * 64, 96, 128) x (blocks per SM 2, 3, 4, 5, 6, 8 within 2048 threads per SM, and
- * 0 = the occupancy limit), then the three fastest of those again with the a(eta) table
+ * 32, 64, 96, 128) x (blocks per SM 2 .. 8, and 0 = the occupancy limit) -- the lane
+ * count sets how evenly a batch of similar trajectories fills its last wave, and the
+ * warps an SM how they share its FP64 throughput --, then the three fastest of those again with the a(eta) table
  * staged in shared memory (EXC_STAGING_SHARED; FP64 launches of an FLRW metric with a
  * table of at most EXC_STAGING_MAX_TABLE entries), and returns the one with the highest
  * rate (args->staging is ignored; plan->staging is the chosen staging). The sample's
@@ -371,7 +372,7 @@ int exc_spherical_mass_grid(const int64_t n[3], const double origin[3], const do
  * shuffled sample measures the steady state rather than the longest trajectory);
  * without it the rate is 1 / elapsed time. One untimed warm-up trial precedes the
  * timed ones. Synchronous on `stream`; allocates no device memory. */
-#define EXC_TUNE_MAX_TRIALS 32
+#define EXC_TUNE_MAX_TRIALS 48
 typedef struct ExcLaunchPlan {
   int32_t block_size;
   int32_t blocks_per_sm;

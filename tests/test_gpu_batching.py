@@ -71,10 +71,10 @@ def test_autotune_and_graph_replay_reproduce_the_launch(cuda):
     ref = trace_batch(wl.metric, wl.states, wl.cfg, field_index=wl.field_index)
     tuned = autotune(wl.metric, wl.states, wl.cfg, field_index=wl.field_index, sample=1024, use_cache=False)
     assert tune_report()  # plan recorded
-    assert tuned.block_size in (64, 96, 128) and tuned.blocks_per_sm in (0, 2, 3, 4, 5, 6, 8)
+    assert tuned.block_size in (32, 64, 96, 128) and tuned.blocks_per_sm in (0, 2, 3, 4, 5, 6, 7, 8)
     assert tuned.staging in N.STAGING
     rep = next(iter(tune_report().values()))
-    assert len(rep["trials"]) >= 24 and rep["best_rate"] > 0
+    assert len(rep["trials"]) == 35 and rep["best_rate"] > 0
     # the three fastest schedules again with the a(eta) table in shared memory
     assert [t[2] for t in rep["trials"]].count("shared") == 3
     cap = CapturedTrace(wl.metric, wl.states, tuned, field_index=wl.field_index)
