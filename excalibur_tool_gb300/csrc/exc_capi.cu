@@ -206,8 +206,10 @@ int exc_trace(const ExcMetric* metric, const ExcTraceArgs* a, void* stream) {
   }
   if (a->precision == EXC_PREC_FP64_EXACT || a->precision == EXC_PREC_FP64_FAST) {
     D.stage_table = stage_table;
-    ce = a->precision == EXC_PREC_FP64_EXACT ? exc_exact::trace(D, *a, block, a->blocks_per_sm, sms, s)
-                                              : exc_fast::trace(D, *a, block, a->blocks_per_sm, sms, s);
+    // no schedule given: the FP64 launchers' balanced default (32-thread blocks, the last wave full)
+    const int b64 = (a->block_size > 0 || a->blocks_per_sm > 0) ? block : 0;
+    ce = a->precision == EXC_PREC_FP64_EXACT ? exc_exact::trace(D, *a, b64, a->blocks_per_sm, sms, s)
+                                              : exc_fast::trace(D, *a, b64, a->blocks_per_sm, sms, s);
   } else {
     if (a->precision != EXC_PREC_RETRACE) {
       ce = exc_mixed::trace(D, *a, block, a->blocks_per_sm, sms, s);

@@ -574,17 +574,35 @@ cudaError_t launch_trace_t(const DevMetric& D, const ExcTraceArgs& A, LaunchCfg 
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
   }
-  int per_sm = lc.blocks_per_sm;
+  int block = lc.block, per_sm = lc.blocks_per_sm;
+  if (block <= 0) {
+    // The library's default for a batch: 32-thread blocks, and as many of them an SM as make the
+    // last wave of similar trajectories full -- the batch over the waves it needs at the occupancy
+    // limit, rounded up to whole warps an SM (65,536 rays: 7 warps an SM, 1.92 rays a lane,
+    // where 128-thread blocks at the limit put 1.68 and ran the second wave two thirds full).
+    block = 32;
+    if (per_sm <= 0) {
+      int occ = 0;
+      cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, block, smem);
+      if (e != cudaSuccess) return e;
+      if (occ < 1) occ = 1;
+      const int64_t lanes_sm = (int64_t)lc.sm_count * 32;
+      const int64_t waves = (A.n_photons + lanes_sm * occ - 1) / (lanes_sm * occ);
+      const int64_t lanes = (A.n_photons + waves - 1) / waves;
+      const int64_t warps = (lanes + lanes_sm - 1) / lanes_sm;
+      per_sm = (int)(warps < 1 ? 1 : (warps > occ ? occ : warps));
+    }
+  }
   if (per_sm <= 0) {
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, lc.block, smem);
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, block, smem);
     if (e != cudaSuccess) return e;
     if (per_sm < 1) per_sm = 1;
   }
   int64_t grid = (int64_t)lc.sm_count * per_sm;
-  const int64_t need = (A.n_photons + lc.block - 1) / lc.block;
+  const int64_t need = (A.n_photons + block - 1) / block;
   if (grid > need) grid = need;
   if (grid < 1) grid = 1;
-  kern<<<(int)grid, lc.block, smem, s>>>(D, A);
+  kern<<<(int)grid, block, smem, s>>>(D, A);
   return cudaGetLastError();
 }
 

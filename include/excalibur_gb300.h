@@ -219,7 +219,9 @@ typedef struct ExcTraceArgs {
   int32_t renormalize_every;     /* 0 = off (integrator.py:376-377) */
   int32_t stop_flags;            /* EXC_STOP_* */
   int32_t obs_flags;             /* EXC_OBS_* bits */
-  int32_t block_size;            /* 0 = library default */
+  int32_t block_size;            /* 0 = library default (FP64 builds with blocks_per_sm 0 too:
+                                    32-thread blocks, as many an SM as fill the batch's last
+                                    wave; otherwise 128) */
   int32_t blocks_per_sm;         /* 0 = library default (EXC_PREC_MIXED with a queue: the
                                     mixed pass's; its FP64 re-trace pass sizes itself on the
                                     device from the share of rays handed back) */
