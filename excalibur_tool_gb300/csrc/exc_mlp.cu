@@ -451,9 +451,10 @@ __global__ void features_kernel(const double* dirs, int64_t n, int64_t n_pad, in
 // the bias, applies SiLU and rounds to BF16 exactly as the layer-by-layer kernel stores its
 // outputs, and writes the result back into shared memory in the 128-byte-swizzled K-major layout
 // that TMA would have produced (16-byte unit u of row r of a chunk at unit u ^ (r % 8)), where
-// the next layer's MMAs read it. The last layer's epilogue forms the linear head in FP32
-// registers. Activations never leave the SM: per row, HBM sees the 512 B of features and the
-// outputs.
+// the next layer's MMAs read it. The last layer's epilogue forms the linear head in FP32 (packed
+// FMA pairs) from the member's head weights, copied into activation chunk 3 once that layer's
+// MMAs have read it. Activations never leave the SM: per row, HBM sees the 512 B of features and
+// the outputs.
 //
 // Sixteen epilogue warps walk the accumulator K chunk by K chunk (warp w reads TMEM lanes
 // 32 (w % 4) .. and, in chunk c, columns 64 c + 16 (w / 4) ..) and release each chunk of the next
@@ -465,8 +466,10 @@ __global__ void features_kernel(const double* dirs, int64_t n, int64_t n_pad, in
 // chunk's MMAs run in two column halves, and `mdone_lo[b]` lets the epilogue start on columns
 // 0-127 while those of columns 128-255 finish),
 // `hready[c]` (chunk c of a layer's activations written), `tfree[b]` (the epilogue is done with
-// accumulator b) and `ybar` (the head's partial sums of column quarters 1-3 are in shared
-// memory). Every wait is bounded, as in the GEMM.
+// accumulator b), `wbar` (a member's head weights are in shared memory) and `ybar` (the head's
+// partial sums of column quarters 1-3 are in shared memory). A layer's bias reaches the epilogue
+// warps spread over their lanes a layer ahead and is shuffled to every lane. Every wait is
+// bounded, as in the GEMM.
 constexpr int kInferEpiWarps = 16;
 constexpr int kInferThreads = (kInferEpiWarps + 2) * 32;
 constexpr int kInferStages = 3;
