@@ -159,6 +159,7 @@ EXPORTS = {
                                           C.c_void_p, C.c_void_p]),
     "exc_generate_photons": (C.c_int, [C.POINTER(ExcMetric), C.POINTER(ExcPhotonGen), C.c_void_p, C.c_void_p,
                                        C.c_void_p]),
+    "exc_balanced_blocks_per_sm": (C.c_int32, [C.c_int64, C.c_int32, C.c_int32]),
     "exc_autotune": (C.c_int, [C.POINTER(ExcMetric), C.POINTER(ExcTraceArgs), C.c_void_p,
                                C.POINTER(ExcLaunchPlan), C.c_void_p]),
     "exc_probe_scratch_len": (C.c_int64, []),

@@ -13,6 +13,7 @@
 
 #include "exc_dispatch.h"
 #include "exc_mixed.h"
+#include "exc_sched.h"
 
 namespace {
 
@@ -134,6 +135,10 @@ void set_last_error(const char* msg) { snprintf(g_err, sizeof(g_err), "%s", msg)
 extern "C" {
 
 int exc_abi_version(void) { return EXC_ABI_VERSION; }
+
+int32_t exc_balanced_blocks_per_sm(int64_t n_photons, int32_t sm_count, int32_t occupancy) {
+  return exc::balanced_warps_per_sm(n_photons, sm_count, occupancy);
+}
 
 const char* exc_last_error(void) { return g_err; }
 

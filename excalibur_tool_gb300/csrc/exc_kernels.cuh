@@ -15,6 +15,7 @@
 
 #include <cooperative_groups.h>
 #include "exc_device.cuh"
+#include "exc_sched.h"
 #include "exc_stepctl.h"
 
 namespace EXC_NS {
@@ -585,12 +586,7 @@ cudaError_t launch_trace_t(const DevMetric& D, const ExcTraceArgs& A, LaunchCfg 
       int occ = 0;
       cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, block, smem);
       if (e != cudaSuccess) return e;
-      if (occ < 1) occ = 1;
-      const int64_t lanes_sm = (int64_t)lc.sm_count * 32;
-      const int64_t waves = (A.n_photons + lanes_sm * occ - 1) / (lanes_sm * occ);
-      const int64_t lanes = (A.n_photons + waves - 1) / waves;
-      const int64_t warps = (lanes + lanes_sm - 1) / lanes_sm;
-      per_sm = (int)(warps < 1 ? 1 : (warps > occ ? occ : warps));
+      per_sm = exc::balanced_warps_per_sm(A.n_photons, lc.sm_count, occ);
     }
   }
   if (per_sm <= 0) {

@@ -392,6 +392,12 @@ typedef struct ExcLaunchPlan {
 int exc_autotune(const ExcMetric* metric, const ExcTraceArgs* args, const double* pristine_state,
                  ExcLaunchPlan* plan, void* stream);
 
+/* The FP64 builds' default launch size (block_size and blocks_per_sm both 0): 32-thread blocks,
+ * this many an SM for n_photons similar trajectories on sm_count SMs with at most occupancy
+ * 32-thread blocks resident an SM -- the batch over the waves it needs at that limit, rounded up
+ * to whole warps an SM, so that its last wave is as full as the others. Host only. */
+int32_t exc_balanced_blocks_per_sm(int64_t n_photons, int32_t sm_count, int32_t occupancy);
+
 /* ---- FP64 pipe probe (measurement only; no reference counterpart) --------
  * Throughput of the FP64 operations the parity build issues, measured on the
  * current device with IEEE semantics and no FMA contraction (the parity

@@ -241,3 +241,17 @@ def test_fused_inference_validates_on_the_host(lib):
                     (dict(x=4104), b"aligned"), (dict(y=None), b"required")):
         assert L.exc_mlp_infer(C.byref(args(**kw)), None) == N.EXC_ERR_INVALID, kw
         assert msg in L.exc_last_error(), (kw, L.exc_last_error())
+
+
+@pytest.mark.parametrize("n,sms,occ,want", [
+    (65536, 152, 9, 7),        # 2 waves at 9 warps an SM; 7 fills the second (1.92 rays a lane)
+    (65536, 152, 8, 7),
+    (2097152, 152, 9, 9),      # many waves: the occupancy limit
+    (1000, 152, 9, 1),         # fewer rays than an SM's lanes each: one warp an SM
+    (43776, 152, 9, 9),        # exactly one full wave
+    (43777, 152, 9, 5),        # one ray over: two waves of ~21,900 rays
+    (0, 152, 9, 1), (5, 0, 0, 1),
+])
+def test_balanced_schedule(lib, n, sms, occ, want):
+    """The FP64 builds' default launch size: whole warps an SM that make the last wave full."""
+    assert N.load().exc_balanced_blocks_per_sm(n, sms, occ) == want
