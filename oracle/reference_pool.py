@@ -1,4 +1,5 @@
-"""The reference's own CPU path, timed: `Integrator(mode="chunked")` and its multiprocessing pool.
+"""The reference's own CPU paths, timed: `Integrator(mode="chunked")` and its multiprocessing pool,
+and (--persistent) its `PersistentPoolIntegrator`.
 
 Measurement infrastructure: only bench.py's CPU-baseline leg and its `--impl reference` arm run
 this, as a process of its own (the pool forks, so the parent must not have touched CUDA). It
@@ -16,7 +17,7 @@ RK4 and the per-step history records of `integrate_single` included, the metric 
 construction excluded. The reference has no box-exit stop, so every photon takes `n_steps`
 steps (the grid is periodic).
 
-    python oracle/reference_pool.py --inputs IN.npz --out OUT.json [--workers N] [--chunk-size K]
+    python oracle/reference_pool.py --inputs IN.npz --out OUT.json [--workers N] [--chunk-size K] [--persistent]
 
 IN.npz: phi [n, n, n] float64 (SI), box (m), states [N, 8], dt (s), n_steps.
 """
