@@ -364,6 +364,34 @@ def gen_integrate(cz):
     save("integrate.npz", **out)
 
 
+# ------------------------------------- integrate_single with the Leapfrog4 stepper
+def gen_integrate_lf4(cz):
+    """Integrator(integrator="leapfrog4").integrate_single on the integrate.npz field: two photons,
+    40 fixed steps, record_every 1 and 3."""
+    g, data, ip = _flrw_setup(cz, seed=9)
+    box = 40 * one_Mpc
+    m = PerturbedFLRWMetricFast(cz.a_of_eta, g, ip, adot_of_eta=cz.adot_of_eta)
+    dt = 0.25 * one_Mpc / c
+    eta0 = cz._eta_at_a1
+    rng = np.random.default_rng(37)
+    out = {"field": data, "box": box, "dt": dt}
+    recs = []
+    for k, rec in enumerate((1, 3)):
+        d = rng.standard_normal(3)
+        d /= np.linalg.norm(d)
+        x0 = np.array([eta0, *(rng.uniform(0.3, 0.7, 3) * box)])
+        u0 = Photons(m)._solve_u0_from_null_condition(x0, d * c, sign=-1.0)
+        p = Photon(x0, np.array([u0, *(d * c)]))
+        Integrator(m, dt=dt, integrator="leapfrog4", dt_min=dt, dt_max=dt).integrate_single(
+            p, "steps", 40, record_every=rec)
+        out[f"case{k}_init"] = np.concatenate([x0, [u0], d * c])
+        out[f"case{k}_final"] = np.concatenate([p.x, p.u])
+        out[f"case{k}_records"] = _history_array(p)
+        recs.append(rec)
+    out["record_every"] = np.array(recs)
+    save("integrate_lf4.npz", **out)
+
+
 # ------------------------------------------- Integrator.integrate (per mode)
 def _history_array(p, width=14):
     hist = p.history.states
@@ -781,7 +809,8 @@ def gen_time_delays():
 
 
 GENERATORS = ["cosmology", "interp", "interp_slow", "rhs", "steps", "integrate", "integrate_modes", "generators",
-              "observables", "flrw_patch_32", "schw_polar", "compare_job", "manifest", "time_delays"]
+              "observables", "flrw_patch_32", "schw_polar", "compare_job", "manifest", "time_delays",
+              "integrate_lf4"]
 
 if __name__ == "__main__":
     if not os.path.isdir(REF):
@@ -790,11 +819,11 @@ if __name__ == "__main__":
     which = sys.argv[1:] or GENERATORS
     cz = gen_cosmology() if "cosmology" in which else None
     if cz is None and set(which) & {"interp_slow", "rhs", "steps", "integrate", "integrate_modes", "generators",
-                                    "observables", "flrw_patch_32"}:
+                                    "observables", "flrw_patch_32", "integrate_lf4"}:
         cz = LCDM_Cosmology(70, 0.3, 0.0, 0.7)
     for name in which:
         if name == "cosmology":
             continue
         fn = globals()["gen_" + name]
         fn(cz) if name in ("interp_slow", "rhs", "steps", "integrate", "integrate_modes", "generators",
-                           "observables", "flrw_patch_32") else fn()
+                           "observables", "flrw_patch_32", "integrate_lf4") else fn()

@@ -170,6 +170,33 @@ def test_rk45_integrate_single(cuda):
     assert np.array_equal(r["state"], o.state)
 
 
+def test_leapfrog4_integrate_single(cuda):
+    """integrate_single with the Leapfrog4 stepper from the reference's own run (40 fixed steps,
+    record_every 1 and 3): the records and final state at the parity bar, and bit-identical to the
+    oracle run with the library's correctly rounded cube."""
+    g = golden("integrate_lf4.npz")
+    spec = lcdm_spacetime(g["field"], float(g["box"]))
+    dt = float(g["dt"])
+    for k in range(2):
+        cfg = TraceConfig(stepper="leapfrog4", dt=dt, dt_min=dt, dt_max=dt, max_steps=40,
+                          record_every=int(g["record_every"][k]), observables=False, precision="fp64")
+        r = gpu_trace(spec, g[f"case{k}_init"][None], cfg)
+        assert r["status"][0] == 0
+        want = g[f"case{k}_records"]
+        got = r["records"][0, :r["n_records"][0]]
+        assert got.shape == want.shape
+        assert np.array_equal(np.isnan(got), np.isnan(want))
+        both = ~np.isnan(want)
+        assert rel_err(got[both], want[both]).max() <= 1e-14, k
+        assert rel_err(r["state"][0], g[f"case{k}_final"]).max() <= 1e-14
+        with O.power_mode("dd"):
+            o = O.trace(spec, g[f"case{k}_init"][None], cfg)
+        nr = int(o.n_records[0])
+        assert r["n_records"][0] == nr
+        assert np.array_equal(r["records"][0, :nr], o.records[0, :nr], equal_nan=True)
+        assert np.array_equal(r["state"], o.state)
+
+
 def test_steppers_match_oracle(cuda):
     """Single steps of every stepper, GPU vs oracle."""
     g = golden("steps.npz")

@@ -143,6 +143,24 @@ def test_integrate_single_records(k):
     assert rel_err(got[:, 8:][q], want[:, 8:][q]).max() <= (1e-8 if is45 else tol)
 
 
+@pytest.mark.parametrize("k", [0, 1])
+def test_leapfrog4_integrate_single_records(k):
+    """integrate_single with the Leapfrog4 stepper (40 fixed steps, record_every 1 and 3) from the
+    reference's own run: every record row and the final state, bit for bit."""
+    g = golden("integrate_lf4.npz")
+    st = lcdm_spacetime(g["field"], float(g["box"]))
+    dt = float(g["dt"])
+    cfg = TraceConfig(stepper="leapfrog4", dt=dt, dt_min=dt, dt_max=dt, max_steps=40,
+                      record_every=int(g["record_every"][k]), observables=False)
+    res = O.trace(st, g[f"case{k}_init"][None], cfg)
+    assert res.status[0] == 0
+    want = g[f"case{k}_records"]
+    got = res.records[0, :res.n_records[0]]
+    assert got.shape == want.shape
+    assert np.array_equal(got, want, equal_nan=True)
+    assert np.array_equal(res.state[0], g[f"case{k}_final"])
+
+
 def test_schw_polar_subset_matches_reference():
     g = golden("schw_polar_1024.npz")
     st = schw_spacetime(float(g["mass"]), float(g["radius"]), center=(0, 0, 0))
