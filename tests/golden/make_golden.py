@@ -364,6 +364,37 @@ def gen_integrate(cz):
     save("integrate.npz", **out)
 
 
+# --------------------------- integrate_single, RK45 (reference tableau), slow Interpolator
+def gen_rk45_slow(cz):
+    """Integrator(integrator="rk45").integrate_single through PerturbedFLRWMetricFast read with the
+    slow Interpolator (continuous trilinear-blended gradient): three photons, 30 iterations,
+    record_every 1, tolerances loose enough that trial steps are both accepted and rejected."""
+    from excalibur.grid.interpolator import Interpolator
+
+    n, box = 16, 40 * one_Mpc
+    rng = np.random.default_rng(23)
+    field = rng.standard_normal((n, n, n)) * 1e-5 * c ** 2
+    g = Grid((n, n, n), (box / n,) * 3, (0.0, 0.0, 0.0))
+    g.add_field("Phi", field)
+    m = PerturbedFLRWMetricFast(cz.a_of_eta, g, Interpolator(g), adot_of_eta=cz.adot_of_eta)
+    dt = 0.25 * one_Mpc / c
+    eta0 = cz._eta_at_a1
+    tol = (1e-6, 1e-3, dt / 50, dt)
+    out = {"field": field, "box": box, "dt": dt, "tol": np.array(tol)}
+    for k in range(3):
+        d = rng.standard_normal(3)
+        d /= np.linalg.norm(d)
+        x0 = np.array([eta0, *(rng.uniform(0.35, 0.65, 3) * box)])
+        u0 = Photons(m)._solve_u0_from_null_condition(x0, d * c, sign=-1.0)
+        p = Photon(x0, np.array([u0, *(d * c)]))
+        Integrator(m, dt=dt, integrator="rk45", rtol=tol[0], atol=tol[1], dt_min=tol[2], dt_max=tol[3]) \
+            .integrate_single(p, "steps", 30, record_every=1)
+        out[f"case{k}_init"] = np.concatenate([x0, [u0], d * c])
+        out[f"case{k}_final"] = np.concatenate([p.x, p.u])
+        out[f"case{k}_records"] = _history_array(p)
+    save("rk45_slow.npz", **out)
+
+
 # ------------------------------------- integrate_single with the Leapfrog4 stepper
 def gen_integrate_lf4(cz):
     """Integrator(integrator="leapfrog4").integrate_single on the integrate.npz field: two photons,
@@ -810,7 +841,7 @@ def gen_time_delays():
 
 GENERATORS = ["cosmology", "interp", "interp_slow", "rhs", "steps", "integrate", "integrate_modes", "generators",
               "observables", "flrw_patch_32", "schw_polar", "compare_job", "manifest", "time_delays",
-              "integrate_lf4"]
+              "integrate_lf4", "rk45_slow"]
 
 if __name__ == "__main__":
     if not os.path.isdir(REF):
@@ -819,11 +850,11 @@ if __name__ == "__main__":
     which = sys.argv[1:] or GENERATORS
     cz = gen_cosmology() if "cosmology" in which else None
     if cz is None and set(which) & {"interp_slow", "rhs", "steps", "integrate", "integrate_modes", "generators",
-                                    "observables", "flrw_patch_32", "integrate_lf4"}:
+                                    "observables", "flrw_patch_32", "integrate_lf4", "rk45_slow"}:
         cz = LCDM_Cosmology(70, 0.3, 0.0, 0.7)
     for name in which:
         if name == "cosmology":
             continue
         fn = globals()["gen_" + name]
         fn(cz) if name in ("interp_slow", "rhs", "steps", "integrate", "integrate_modes", "generators",
-                           "observables", "flrw_patch_32", "integrate_lf4") else fn()
+                           "observables", "flrw_patch_32", "integrate_lf4", "rk45_slow") else fn()

@@ -79,6 +79,32 @@ def test_oracle_slow_trace_matches_reference():
     assert np.array_equal(res.records[:, :want.shape[1], :8], want)
 
 
+@pytest.mark.parametrize("k", [0, 1, 2])
+def test_oracle_rk45_slow_trace_matches_reference(k):
+    """integrate_single with the reference's RK45 (its own tableau and controller, dt clip) through
+    the slow Interpolator, from the reference's own run (tests/golden/rk45_slow.npz; 37 iterations
+    a photon, 7 of them rejected): the same accepted steps, the states within the ~1e-12 that the
+    reference's BLAS-ordered y5 leaves in the step-size control (as for the base-node RK45 case;
+    measured: two photons bit for bit, one within 1.0e-13), the quantity columns within 1e-8."""
+    g = golden("rk45_slow.npz")
+    st = lcdm_spacetime(g["field"], float(g["box"]), boundary="error")
+    st.fields[0].gradient = "trilinear"
+    rtol, atol, dmin, dmax = (float(v) for v in g["tol"])
+    cfg = TraceConfig(stepper="rk45", dt=float(g["dt"]), dt_min=dmin, dt_max=dmax, rtol=rtol, atol=atol,
+                      max_steps=30, record_every=1, observables=False)
+    res = O.trace(st, g[f"case{k}_init"][None], cfg)
+    assert res.status[0] == 0
+    want = g[f"case{k}_records"]
+    got = res.records[0, :res.n_records[0]]
+    assert got.shape == want.shape
+    assert np.array_equal(np.isnan(got), np.isnan(want))
+    assert rel_err(res.state[0], g[f"case{k}_final"]).max() <= 1e-12
+    st8 = ~np.isnan(want[:, :8])
+    assert rel_err(got[:, :8][st8], want[:, :8][st8]).max() <= 1e-12
+    q = ~np.isnan(want[:, 8:])
+    assert rel_err(got[:, 8:][q], want[:, 8:][q]).max() <= 1e-8
+
+
 def test_slow_descriptor_validation():
     """grad_mode "trilinear" needs the error boundary (the slow class's single bounds rule)."""
     from excalibur_tool_gb300 import _native as N
