@@ -539,6 +539,34 @@ def gen_schw_polar():
          n_steps=np.array(nsteps), dl=dl, mass=m.mass, radius=m.radius)
 
 
+# -------------------------------- Schwarzschild polar cone: Leapfrog4 and RK45 integrate_single
+def gen_schw_steppers():
+    """Six off-pole photons of the polar cone through Integrator.integrate_single with the Leapfrog4
+    stepper (300 fixed steps, record_every 10) and with the reference's RK45 (rtol 1e-4, atol 1e12,
+    dt in [dl/50, dl], 80 iterations, record_every 2)."""
+    m, states = schw_polar_initial_states()
+    dl = 0.5 * one_Mpc / c
+    pick = np.array([1, 9, 100, 333, 700, 1000])
+    out = {"dl": dl, "mass": m.mass, "radius": m.radius, "pick": pick, "states": states[pick]}
+    for name, kw, n_steps, rec in (("lf4", dict(integrator="leapfrog4", dt_min=dl, dt_max=dl), 300, 10),
+                                   ("rk45", dict(integrator="rk45", rtol=1e-4, atol=1e12, dt_min=dl / 50, dt_max=dl),
+                                    80, 2)):
+        finals, recs = [], []
+        for s in states[pick]:
+            p = Photon(s[:4].copy(), s[4:].copy())
+            Integrator(m, dt=dl, **kw).integrate_single(p, "steps", n_steps, record_every=rec)
+            finals.append(np.concatenate([p.x, p.u]))
+            recs.append(_history_array(p, width=12))
+        width = max(r.shape[0] for r in recs)
+        arr = np.full((len(recs), width, 12), np.nan)
+        for i, r in enumerate(recs):
+            arr[i, :r.shape[0]] = r
+        out[f"{name}_final"] = np.array(finals)
+        out[f"{name}_records"] = arr
+        out[f"{name}_n_records"] = np.array([r.shape[0] for r in recs])
+    save("schw_steppers.npz", **out)
+
+
 # ------------------------------------------------ FLRW lens + random-field patch, 32^3
 def gen_flrw_patch_32(cz):
     """The lens patch construction on a 32^3 grid: Plummer (1e15 Msun, eps 5 Mpc) + GRF (seed 2, rms 1e-5),
@@ -841,7 +869,7 @@ def gen_time_delays():
 
 GENERATORS = ["cosmology", "interp", "interp_slow", "rhs", "steps", "integrate", "integrate_modes", "generators",
               "observables", "flrw_patch_32", "schw_polar", "compare_job", "manifest", "time_delays",
-              "integrate_lf4", "rk45_slow"]
+              "integrate_lf4", "rk45_slow", "schw_steppers"]
 
 if __name__ == "__main__":
     if not os.path.isdir(REF):
