@@ -197,22 +197,26 @@ def test_leapfrog4_integrate_single(cuda):
         assert np.array_equal(r["state"], o.state)
 
 
-@pytest.mark.parametrize("name", ["lf4", "rk45"])
+@pytest.mark.parametrize("name", ["lf4", "rk45", "rk4ren"])
 def test_schw_steppers_integrate_single(cuda, name):
     """Six off-pole cone photons through the analytical Schwarzschild metric with
     integrate_single, from the reference's own run: Leapfrog4 (300 fixed steps, record_every 10)
-    and RK45 (80 iterations, record_every 2) give the same records row for row: Leapfrog4 bit for
-    bit, RK45 within the 1e-15 that the reference's BLAS-ordered tensordot leaves (measured on a
-    GB300: 0.0 and 4.3e-16)."""
+    RK45 (80 iterations, record_every 2) and RK4 renormalised onto the null cone every 7 steps
+    (300 steps, record_every 5) give the same records row for row: Leapfrog4 bit for bit, RK45 and
+    the renormalised RK4 within the 1e-15 that the reference's BLAS-ordered tensordot and
+    u_i g_ij u_j leave (measured on a GB300: 0.0, 4.3e-16 and 4.0e-16, the oracle's own figures)."""
     g = golden("schw_steppers.npz")
     spec = schw_spacetime(float(g["mass"]), float(g["radius"]))
     dl = float(g["dl"])
     if name == "lf4":
         cfg = TraceConfig(stepper="leapfrog4", dt=dl, dt_min=dl, dt_max=dl, max_steps=300,
                           record_every=10, observables=False, precision="fp64")
-    else:
+    elif name == "rk45":
         cfg = TraceConfig(stepper="rk45", dt=dl, dt_min=dl / 50, dt_max=dl, rtol=1e-4, atol=1e12,
                           max_steps=80, record_every=2, observables=False, precision="fp64")
+    else:
+        cfg = TraceConfig(stepper="rk4", dt=dl, dt_min=dl, dt_max=dl, max_steps=300, record_every=5,
+                          renormalize_every=7, observables=False, precision="fp64")
     r = gpu_trace(spec, g["states"], cfg)
     assert (r["status"] == 0).all()
     assert np.array_equal(r["n_records"], g[f"{name}_n_records"])
