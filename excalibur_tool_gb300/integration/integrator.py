@@ -223,9 +223,7 @@ class Integrator:
     def integrate_single(self, photon, stop_mode="steps", stop_value=100, *, record_every: int = 1,
                          trace_norm: bool = False, renormalize_every: int = 0):
         """Integrator.integrate_single (integrator.py:218-409): mutates `photon`
-        (x, u, quantities, history) exactly as the reference does."""
-        from .._evaluate import null_error
-
+        (x, u, quantities, history, norm_history) exactly as the reference does."""
         if record_every < 0:
             raise ValueError("record_every must be >= 0")
         if renormalize_every < 0:
@@ -236,13 +234,24 @@ class Integrator:
             photon.norm_history = []
         _, st, rows, final = next(self._trace_recorded([photon], stop_mode, stop_value, record_every,
                                                        renormalize_every))
-        self._finish_single(photon, st, rows, final, trace_norm, record_every)
+        norm_rows = None
+        if trace_norm:
+            # the reference appends the relative null error at the initial state, after every
+            # accepted step (after its renormalisation) and once more at the end
+            # (integrator.py:343-345, 384-385, 406-407): the rows of a record_every=1 trace of
+            # the same trajectory, which also stops, without a final row, where a failure raises
+            norm_rows = rows if record_every == 1 else next(self._trace_recorded(
+                [photon], stop_mode, stop_value, 1, renormalize_every))[2]
+        self._finish_single(photon, st, rows, final, record_every, norm_rows)
         return photon
 
-    def _finish_single(self, photon, st, rows, final, trace_norm=False, record_every=1):
+    def _finish_single(self, photon, st, rows, final, record_every=1, norm_rows=None):
         from .._evaluate import null_error
 
         self._apply(photon, rows, final)
+        if norm_rows is not None and len(norm_rows):
+            rel, _ = null_error(self.metric, np.ascontiguousarray(np.asarray(norm_rows)[:, :8]))
+            photon.norm_history.extend(np.atleast_1d(rel.cpu().numpy()).tolist())
         if st in N.FAILED_STATUSES:
             # the reference evaluated the quantities at its last recorded state before it failed
             # (integrator.py:387-394); they are in no record yet
@@ -253,9 +262,6 @@ class Integrator:
                     pass
             raise ValueError(f"integration failed: {N.STATUS_NAMES.get(st, st)}")
         photon.quantities = rows[-1][8:] if len(rows) else np.array([])
-        if trace_norm:
-            rel, _ = null_error(self.metric, np.stack([rows[0][:8], final]))
-            photon.norm_history.extend(rel.cpu().numpy().tolist())
 
     def integrate(self, photons, stop_mode="steps", stop_value=100, verbose=True):
         """Integrator.integrate (integrator.py:434-476), with the reference's per-mode results

@@ -544,7 +544,8 @@ def gen_schw_steppers():
     """Six off-pole photons of the polar cone through Integrator.integrate_single with the Leapfrog4
     stepper (300 fixed steps, record_every 10), with the reference's RK45 (rtol 1e-4, atol 1e12,
     dt in [dl/50, dl], 80 iterations, record_every 2) and with RK4 renormalised onto the null cone
-    every 7 steps (300 fixed steps, record_every 5)."""
+    every 7 steps (300 fixed steps, record_every 5, with trace_norm: its norm_history, the relative
+    null error at the initial state, after every step and at the end)."""
     m, states = schw_polar_initial_states()
     dl = 0.5 * one_Mpc / c
     pick = np.array([1, 9, 100, 333, 700, 1000])
@@ -553,13 +554,17 @@ def gen_schw_steppers():
             ("lf4", dict(integrator="leapfrog4", dt_min=dl, dt_max=dl), 300, 10, 0),
             ("rk45", dict(integrator="rk45", rtol=1e-4, atol=1e12, dt_min=dl / 50, dt_max=dl), 80, 2, 0),
             ("rk4ren", dict(integrator="rk4", dt_min=dl, dt_max=dl), 300, 5, 7)):
-        finals, recs = [], []
+        finals, recs, norms = [], [], []
         for s in states[pick]:
             p = Photon(s[:4].copy(), s[4:].copy())
             Integrator(m, dt=dl, **kw).integrate_single(p, "steps", n_steps, record_every=rec,
-                                                        renormalize_every=ren)
+                                                        renormalize_every=ren, trace_norm=bool(ren))
             finals.append(np.concatenate([p.x, p.u]))
             recs.append(_history_array(p, width=12))
+            if ren:
+                norms.append(np.array(p.norm_history, dtype=float))
+        if norms:
+            out[f"{name}_norm"] = np.array(norms)
         width = max(r.shape[0] for r in recs)
         arr = np.full((len(recs), width, 12), np.nan)
         for i, r in enumerate(recs):

@@ -96,6 +96,71 @@ def test_integrator_config_mapping():
         Integrator(M(), integrator="euler")
 
 
+def _fake_trajectory(n_steps, record_every, failed):
+    """Record rows as the tracer writes them for a trajectory of n_steps accepted steps: the
+    initial state, the state after step s when s % record_every == 0 (every step for 1), and the
+    final state unless the photon failed. Row k's first column is the step count it follows."""
+    steps = [] if record_every == 0 else [s for s in range(n_steps) if s % record_every == 0]
+    idx = [-1] + steps + ([] if failed else [n_steps - 1])
+    rows = np.zeros((len(idx), 14))
+    rows[:, 0] = idx
+    rows[:, 8:] = 5.0
+    return rows
+
+
+@pytest.mark.parametrize("record_every,failed", [(1, False), (3, False), (0, False), (4, True)])
+def test_integrate_single_trace_norm(monkeypatch, record_every, failed):
+    """trace_norm appends the null error at the initial state, after every accepted step and at
+    the end (integrator.py:343-345, 384-385, 406-407), whatever record_every; a failing photon
+    has the entries up to its last accepted step when the error is raised."""
+    import torch
+
+    from excalibur_tool_gb300 import _evaluate
+    from excalibur_tool_gb300 import _native as N
+    from excalibur_tool_gb300.integration.integrator import Integrator
+    from excalibur_tool_gb300.photon.photon import Photon
+
+    class M:
+        grid = None
+
+        def metric_physical_quantities(self, x):
+            return np.full(6, 5.0)
+
+    n_steps = 7
+    calls = []
+
+    def fake_trace(plist, stop_mode, stop_value, rec, ren):
+        calls.append(rec)
+        st = N.PH_OUTSIDE_GRID if failed else 0
+        yield plist[0], st, _fake_trajectory(n_steps, rec, failed), np.arange(8.0)
+
+    def fake_null_error(metric, states):
+        # the step count of each row, so that the test sees which states were evaluated
+        return torch.as_tensor(np.asarray(states)[:, 0] + 1.0), torch.zeros(len(states), dtype=torch.int32)
+
+    it = Integrator(M(), dt=1.0, integrator="rk4")
+    monkeypatch.setattr(it, "_trace_recorded", fake_trace)
+    monkeypatch.setattr(_evaluate, "null_error", fake_null_error)
+    p = Photon(np.zeros(4), np.ones(4))
+    if failed:
+        with pytest.raises(ValueError):
+            it.integrate_single(p, "steps", n_steps, record_every=record_every, trace_norm=True)
+    else:
+        it.integrate_single(p, "steps", n_steps, record_every=record_every, trace_norm=True)
+    # one extra trace for the per-step states unless the records already hold them
+    assert calls == ([1] if record_every == 1 else [record_every, 1])
+    want = [0.0] + [s + 1.0 for s in range(n_steps)] + ([] if failed else [float(n_steps)])
+    assert p.norm_history == want
+    # the history keeps the caller's record_every
+    assert len(p.history.states) == len(_fake_trajectory(n_steps, record_every, failed))
+    # without trace_norm: one trace, no norm_history
+    calls.clear()
+    q = Photon(np.zeros(4), np.ones(4))
+    if not failed:
+        it.integrate_single(q, "steps", n_steps, record_every=record_every)
+        assert calls == [record_every] and not hasattr(q, "norm_history")
+
+
 def test_exit_geometry_crossing():
     """The straight-line exit and the back-extrapolated crossing of a box face."""
     from excalibur_tool_gb300.surrogate.sky import ExitGeometry, Patch

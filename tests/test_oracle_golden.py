@@ -199,6 +199,28 @@ def test_schw_steppers_integrate_single(name):
             assert rel_err(res.state[i], g[f"{name}_final"][i]).max() <= 1e-15
 
 
+def test_schw_trace_norm_history():
+    """integrate_single's trace_norm list from the reference's own run (RK4 renormalised every 7
+    steps, 300 steps, record_every 5): one entry at the initial state, one after every accepted
+    step, one at the end -- the relative null error of the states a record_every=1 trace of the
+    same trajectory records. The entries are cancellation residuals (~1e-16) whose last bits
+    depend on the reference's BLAS-ordered u.g.u: compared absolutely at the float64 noise floor
+    (measured: ~1e-31 where the states agree bit for bit, 2.0e-16 on the photon whose state
+    differs by an ulp after a renormalisation)."""
+    g = golden("schw_steppers.npz")
+    st = schw_spacetime(float(g["mass"]), float(g["radius"]), center=(0, 0, 0))
+    dl = float(g["dl"])
+    cfg = TraceConfig(stepper="rk4", dt=dl, dt_min=dl, dt_max=dl, max_steps=300, record_every=1,
+                      renormalize_every=7, observables=False)
+    res = O.trace(st, g["states"], cfg)
+    want = g["rk4ren_norm"]
+    assert (res.n_records == want.shape[1]).all() and want.shape[1] == 300 + 2
+    for i in range(len(want)):
+        rel, status = O.null_error(st, res.records[i, :res.n_records[i], :8])
+        assert (status == 0).all()
+        assert np.abs(rel - want[i]).max() <= 4.5e-16
+
+
 def test_schw_polar_subset_matches_reference():
     g = golden("schw_polar_1024.npz")
     st = schw_spacetime(float(g["mass"]), float(g["radius"]), center=(0, 0, 0))
