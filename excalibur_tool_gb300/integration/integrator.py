@@ -70,7 +70,20 @@ class RK45Adaptive(_Stepper):
     name = "rk45"
 
     def __init__(self, tableau="reference"):
+        if tableau not in ("reference", "fehlberg"):
+            raise ValueError("tableau must be 'reference' or 'fehlberg'")
         self.tableau = tableau
+        # the tableau the kernels step with, as arrays for callers that read it: stage
+        # coefficients B (lower triangular), 5th-order weights C5, embedded 4th-order weights C4
+        self.B = np.zeros((6, 6))
+        self.B[1, :1] = [1 / 4]
+        self.B[2, :2] = [3 / 32, 9 / 32]
+        self.B[3, :3] = [1932 / 2197, -7200 / 2197, 7296 / 2197]
+        self.B[4, :4] = [439 / 216, -8, 3680 / 513, -845 / 4104]
+        self.B[5, :5] = [-8 / 27, 2, -3544 / 2565, 1859 / 4104, -11 / 40]
+        c5_2 = 665 / 1287 if tableau == "reference" else 6656 / 12825
+        self.C5 = np.array([16 / 135, 0, c5_2, 28561 / 56430, -9 / 50, 2 / 55])
+        self.C4 = np.array([25 / 216, 0, 1408 / 2565, 2197 / 4104, -1 / 5, 0])
 
 
 class Integrator:

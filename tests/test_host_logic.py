@@ -241,3 +241,19 @@ def test_square_extent_edge_cases():
     assert x0 < 0.01 < x1 and y0 < -0.02 < y1
     with pytest.raises(ValueError):
         square_extent([], [])
+
+
+def test_rk45_tableau_arrays():
+    """RK45Adaptive's B, C5, C4 arrays (integrator.py:103-115): Fehlberg's nodes as the row sums
+    of B, C4 summing to 1; the reference's C5[2] = 665/1287, whose weights sum to 1 - 2.3e-3,
+    and Fehlberg's 6656/12825 (sum 1) under tableau="fehlberg"."""
+    from excalibur_tool_gb300.integration.integrator import RK45Adaptive
+
+    r, f = RK45Adaptive(), RK45Adaptive("fehlberg")
+    assert np.allclose(r.B.sum(axis=1), [0, 1 / 4, 3 / 8, 12 / 13, 1, 1 / 2], rtol=0, atol=1e-15)
+    assert np.array_equal(np.triu(r.B), np.zeros((6, 6)))
+    assert abs(r.C4.sum() - 1) < 1e-15 and abs(f.C5.sum() - 1) < 1e-15
+    assert r.C5[2] == 665 / 1287 and f.C5[2] == 6656 / 12825
+    assert np.isclose(r.C5.sum(), 1 + 665 / 1287 - 6656 / 12825, rtol=0, atol=1e-15)
+    with pytest.raises(ValueError):
+        RK45Adaptive("dopri")
