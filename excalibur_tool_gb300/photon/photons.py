@@ -113,6 +113,103 @@ class Photons:
         for p in self.photons:
             p.record()
 
+    def update_quantities_all(self, relevant_quantities_func):
+        """photon.state_quantities for every photon (photons.py:708-711)."""
+        for p in self.photons:
+            p.state_quantities(relevant_quantities_func)
+
+    # ---- files (photons.py:713-910) ------------------------------------------
+    def _replace(self, photons):
+        self._batch, self._pending, self._photons = [], [], list(photons)
+
+    def save_to_binary(self, filename):
+        """Every photon's weight, x, u and history rows in one compressed .npz (object arrays,
+        read back with allow_pickle). The reference reads photon.position / photon.velocity,
+        which its Photon never sets; the photon's x and u are what they name."""
+        data = np.empty(len(self.photons), dtype=object)
+        for i, p in enumerate(self.photons):
+            data[i] = {"weight": p.weight, "initial_position": np.asarray(p.x, dtype=float),
+                       "initial_velocity": np.asarray(p.u, dtype=float),
+                       "history_states": [np.asarray(h) for h in p.history.states]}
+        np.savez_compressed(filename, n_photons=len(data), photon_data=data)
+
+    def load_from_binary(self, filename):
+        """Replace the photons by those of a save_to_binary file (trusted files only: the rows
+        are pickled objects)."""
+        data = np.load(filename, allow_pickle=True)
+        out = []
+        for d in data["photon_data"][:int(data["n_photons"])]:
+            p = Photon(np.asarray(d["initial_position"]), np.asarray(d["initial_velocity"]), float(d["weight"]))
+            for h in d["history_states"]:
+                p.history.append(np.asarray(h))
+            out.append(p)
+        self._replace(out)
+
+    @staticmethod
+    def _h5py():
+        try:
+            import h5py
+        except ImportError:
+            return None
+        return h5py
+
+    def save_all_histories(self, filename):
+        """The runners' HDF5 layout: attribute n_photons, one dataset photon_{i}_states per photon
+        (its history rows, NaN-padded to the longest row; an empty array without history) and
+        the structured dataset photon_info (id, n_states, initial_position, initial_velocity from
+        the first row, weight). Needs h5py, as in the reference."""
+        h5py = self._h5py()
+        if h5py is None:
+            raise RuntimeError("h5py is not available; cannot save photon histories. Install h5py or skip saving.")
+        plist = self.photons
+        info = np.empty(len(plist), dtype=[("id", "i4"), ("n_states", "i4"), ("initial_position", "4f8"),
+                                           ("initial_velocity", "4f8"), ("weight", "f8")])
+        with h5py.File(filename, "w") as f:
+            f.attrs["n_photons"] = len(plist)
+            for i, p in enumerate(plist):
+                rows = p.history.states
+                if rows:
+                    f.create_dataset(f"photon_{i}_states", data=p.history.as_array())
+                    first = np.asarray(rows[0], dtype=float)
+                    info[i] = (i, len(rows), first[:4], first[4:8] if len(first) >= 8 else np.nan, p.weight)
+                else:
+                    f.create_dataset(f"photon_{i}_states", data=np.array([]))
+                    info[i] = (i, 0, np.nan, np.nan, p.weight)
+            if len(plist):
+                f.create_dataset("photon_info", data=info)
+
+    def load_from_hdf5(self, filename):
+        """Replace the photons by those of a save_all_histories file: x and u from photon_info
+        (else from the first row), history rows with their NaN padding removed."""
+        h5py = self._h5py()
+        if h5py is None:
+            raise RuntimeError("h5py is not available; cannot load photon histories. Install h5py or skip loading.")
+        out = []
+        with h5py.File(filename, "r") as f:
+            n = int(f.attrs["n_photons"])
+            meta = {int(r["id"]): r for r in f["photon_info"][:]} if "photon_info" in f else {}
+            for i in range(n):
+                name = f"photon_{i}_states"
+                if name not in f:
+                    continue
+                rows = f[name][:]
+                if i in meta:
+                    x0, u0, w = meta[i]["initial_position"], meta[i]["initial_velocity"], float(meta[i]["weight"])
+                elif len(rows):
+                    first = rows[0][~np.isnan(rows[0])]
+                    x0 = first[:4] if len(first) >= 4 else np.zeros(4)
+                    u0 = first[4:8] if len(first) >= 8 else np.array([1.0, 1.0, 0.0, 0.0])
+                    w = 1.0
+                else:
+                    x0, u0, w = np.zeros(4), np.array([1.0, 1.0, 0.0, 0.0]), 1.0
+                p = Photon(np.array(x0, dtype=float), np.array(u0, dtype=float), w)
+                for r in rows:
+                    r = r[~np.isnan(r)]
+                    if len(r):
+                        p.history.append(r)
+                out.append(p)
+        self._replace(out)
+
     # ---- u^0 on the device ------------------------------------------------
     def _finish(self, origins, u_spatial, sign=-1.0):
         import torch
@@ -176,15 +273,16 @@ class Photons:
         return rotate_to_direction(vector, target_direction)[0]
 
     # ---- reference generators ---------------------------------------------
-    def generate_cone_grid(self, n_photons, origin, central_direction, cone_angle, direction_basis="coordinates",
-                           *, direction_coords=None):
-        """Regular (theta, phi) grid in a cone (photons.py:295-424), skipping duplicate theta = 0 points."""
-        direction_basis = self._basis_alias(direction_basis, direction_coords)
+    @staticmethod
+    def _cone_grid_directions(n_photons, central_direction, cone_angle):
+        """Unit directions of the regular (theta, phi) cone grid (photons.py:159-232, 295-390):
+        n_photons an int (floor(sqrt(n)) thetas and phis) or (n_theta, n_phi); theta in
+        linspace(0, cone_angle), phi in [0, 2 pi) without the end point; the theta = 0 row kept
+        once; rotated from +z onto the central direction and normalised."""
         if type(n_photons) == int:
             n_phi = n_theta = int(np.floor(np.sqrt(n_photons)))
         else:
             n_theta, n_phi = n_photons[0], n_photons[1]
-        origin = np.asarray(origin, dtype=float)
         central = np.asarray(central_direction, dtype=float)
         central = central / np.linalg.norm(central)
         thetas = np.linspace(0, cone_angle, n_theta)
@@ -196,9 +294,42 @@ class Photons:
                     continue
                 dirs.append([np.sin(th) * np.cos(ph), np.sin(th) * np.sin(ph), np.cos(th)])
         d = rotate_to_direction(np.array(dirs), central)
-        d = d / np.linalg.norm(d, axis=1)[:, None]
+        return d / np.linalg.norm(d, axis=1)[:, None]
+
+    def generate_cone_grid(self, n_photons, origin, central_direction, cone_angle, direction_basis="coordinates",
+                           *, direction_coords=None):
+        """Regular (theta, phi) grid in a cone (photons.py:295-424), skipping duplicate theta = 0 points."""
+        direction_basis = self._basis_alias(direction_basis, direction_coords)
+        origin = np.asarray(origin, dtype=float)
+        d = self._cone_grid_directions(n_photons, central_direction, cone_angle)
         u_sp = self._spatial_from_directions(origin, d, direction_basis)
         return self._finish(np.tile(origin, (len(d), 1)), u_sp, -1.0)
+
+    def generate_cone_grid_metric_tensor(self, n_photons, origin, central_direction, cone_angle,
+                                         direction_basis="coordinates", *, direction_coords=None):
+        """The cone grid with u^0 from the diagonal metric at the origin (photons.py:159-293):
+        u^0 = -sqrt(|-(g11 u1^2 + g22 u2^2 + g33 u3^2) / g00|), the metric evaluated once on the
+        device; a photon whose relative null error exceeds 1e-5 is reported as the reference
+        does. Returns the [n, 8] states (host)."""
+        from .._evaluate import null_error
+
+        direction_basis = self._basis_alias(direction_basis, direction_coords)
+        origin = np.asarray(origin, dtype=float)
+        d = self._cone_grid_directions(n_photons, central_direction, cone_angle)
+        u_sp = self._spatial_from_directions(origin, d, direction_basis)
+        g = np.asarray(self.metric.metric_tensor(origin), dtype=float)
+        spatial = g[1, 1] * u_sp[:, 0] ** 2 + g[2, 2] * u_sp[:, 1] ** 2 + g[3, 3] * u_sp[:, 2] ** 2
+        st = np.zeros((len(d), 8))
+        st[:, :4] = origin
+        st[:, 4] = -np.sqrt(np.abs(-spatial / g[0, 0]))
+        st[:, 5:8] = u_sp
+        self._append_batch(st)
+        rel, _ = null_error(self.metric, st)
+        rel = np.atleast_1d(rel.cpu().numpy() if hasattr(rel, "cpu") else np.asarray(rel))
+        for i in np.flatnonzero(rel > 1e-5):
+            uu = float(st[i, 4:] @ (g @ st[i, 4:]))
+            print(f"Warning: Photon {i} null condition violated: u.u = {uu:.3e}, rel_error = {rel[i]:.3e}")
+        return st
 
     def generate_cone_random(self, n_photons, origin, central_direction, cone_angle,
                              direction_basis="coordinates", *, direction_coords=None, seed=None):

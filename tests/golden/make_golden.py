@@ -634,6 +634,11 @@ def gen_generators(cz):
                               cone_angle=np.deg2rad(7), direction_basis="cartesian")
     flrw_cone = np.array([np.concatenate([p.x, p.u]) for p in ph.photons])
     flrw_null = np.array([p.null_condition_relative_error(m) for p in ph.photons])
+    ph5 = Photons(m)
+    with contextlib.redirect_stdout(io.StringIO()):
+        ph5.generate_cone_grid_metric_tensor(n_photons=49, origin=origin, central_direction=[1.0, 0.5, -0.3],
+                                             cone_angle=np.deg2rad(7), direction_basis="cartesian")
+    flrw_cone_mt = np.array([np.concatenate([p.x, p.u]) for p in ph5.photons])
     ph2 = Photons(m)
     ph2.generate_impact_parameter_bins(origin, [1.0, 0.2, 0.1], np.linspace(0.1, 2.0, 4) * one_Mpc, 5, seed=3)
     flrw_bins = np.array([np.concatenate([p.x, p.u]) for p in ph2.photons])
@@ -648,6 +653,11 @@ def gen_generators(cz):
                            direction_basis="cartesian")
     schw_cone = np.array([np.concatenate([p.x, p.u]) for p in ph3.photons])
     schw_null = np.array([p.null_condition_relative_error(ms) for p in ph3.photons])
+    ph6 = Photons(ms)
+    with contextlib.redirect_stdout(io.StringIO()):
+        ph6.generate_cone_grid_metric_tensor(n_photons=(4, 9), origin=o_sph, central_direction=center - obs,
+                                             cone_angle=np.deg2rad(2), direction_basis="cartesian")
+    schw_cone_mt = np.array([np.concatenate([p.x, p.u]) for p in ph6.photons])
     ph4 = Photons(ms)
     ph4.generate_impact_parameter_bins(o_sph, center - obs, np.linspace(0.5, 10, 3) * one_Mpc, 4, seed=0)
     schw_bins = np.array([np.concatenate([p.x, p.u]) for p in ph4.photons])
@@ -658,7 +668,8 @@ def gen_generators(cz):
     rot = np.array([ph._rotate_to_direction(v, t) for v, t in zip(vecs, targets)])
     save("generators.npz", field=data, box=box, flrw_origin=origin, flrw_cone=flrw_cone, flrw_null=flrw_null,
          flrw_bins=flrw_bins, schw_origin=o_sph, schw_center=center, schw_cone=schw_cone, schw_null=schw_null,
-         schw_bins=schw_bins, rot_vecs=vecs, rot_targets=targets, rot_out=rot)
+         schw_bins=schw_bins, rot_vecs=vecs, rot_targets=targets, rot_out=rot, flrw_cone_mt=flrw_cone_mt,
+         schw_cone_mt=schw_cone_mt)
 
 
 # ------------------------------------------------------------ observables
