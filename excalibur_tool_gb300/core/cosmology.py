@@ -125,6 +125,36 @@ class LCDM_Cosmology:
         z = 1.0 / a - 1.0
         return self.H0 * self.E(z) / a ** 2
 
+    # -- host helpers of the reference's class (setup, not the traced path) --
+    def H_of_z(self, z):
+        """H0 E(z) in s^-1 (cosmology.py:74-76)."""
+        return self.H0 * self.E(z)
+
+    def a_of_z(self, z):
+        """1 / (1 + z) (cosmology.py:95-97)."""
+        return 1.0 / (1.0 + z)
+
+    def a_of_t(self, t):
+        """Scale factor at cosmic time t [s] (cosmology.py:99-128): t(a) = (1/H0) integral from 0
+        to a of da' / (a' E(1/a' - 1)) by quad, and a refined from 1 by a <- a t / t(a) until
+        |t(a) - t| < 1e-6 s or 100 updates. Scalar in, float out; arrays elementwise."""
+        from scipy.integrate import quad
+
+        def t_of_a(a):
+            return quad(lambda x: 1.0 / (x * self.E(1.0 / x - 1.0)), 0, a)[0] / self.H0
+
+        t = np.asarray(t, dtype=float)
+        out = np.empty(t.shape if t.ndim else (1,))
+        for i, tv in enumerate(np.atleast_1d(t)):
+            a = 1.0
+            for _ in range(100):
+                ta = t_of_a(a)
+                if abs(ta - tv) < 1e-6:
+                    break
+                a *= tv / ta
+            out[i] = a
+        return float(out[0]) if t.ndim == 0 else out
+
 
 class StaticCosmology:
     """a(eta) = 1, adot = 0 (excalibur/core/cosmology.py:236-257)."""

@@ -84,8 +84,13 @@ def gen_cosmology():
                             cz._eta_at_a1 - 5.1e13, 1e18, 1.2e18]])
     a = np.array([cz.a_of_eta(float(e)) for e in etas])
     adot = np.array([cz.adot_of_eta(float(e)) for e in etas])
+    # the class's host helpers: H(z), a(z), and a(t) by its quad-and-update search
+    zs = np.array([0.0, 0.5, 1.0, 3.0, 1100.0])
+    ts = np.array([1.0e16, 1.0e17, 3.0e17, 4.3e17])
     save("cosmology.npz", a_grid=cz.a_grid, eta_min=cz.eta_min, eta_step=cz.eta_step, N_eta=cz.N_eta,
-         eta_at_a1=cz._eta_at_a1, H0=cz.H0, etas=etas, a=a, adot=adot)
+         eta_at_a1=cz._eta_at_a1, H0=cz.H0, etas=etas, a=a, adot=adot, zs=zs,
+         H_of_z=np.array([cz.H_of_z(z) for z in zs]), a_of_z=np.array([cz.a_of_z(z) for z in zs]),
+         ts=ts, a_of_t=cz.a_of_t(ts), a_of_t_scalar=cz.a_of_t(3.0e17))
     return cz
 
 

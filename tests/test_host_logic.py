@@ -257,3 +257,17 @@ def test_rk45_tableau_arrays():
     assert np.isclose(r.C5.sum(), 1 + 665 / 1287 - 6656 / 12825, rtol=0, atol=1e-15)
     with pytest.raises(ValueError):
         RK45Adaptive("dopri")
+
+
+def test_lcdm_host_helpers_match_reference():
+    """H_of_z, a_of_z and a_of_t (cosmology.py:74-128) against the reference's own values: the same
+    expressions and the same quad-and-update search, bit for bit."""
+    from excalibur_tool_gb300.core.cosmology import LCDM_Cosmology
+
+    cz = golden("cosmology.npz")
+    lc = LCDM_Cosmology(70, 0.3, 0.0, 0.7)
+    assert np.array_equal([lc.H_of_z(z) for z in cz["zs"]], cz["H_of_z"])
+    assert np.array_equal([lc.a_of_z(z) for z in cz["zs"]], cz["a_of_z"])
+    assert np.array_equal(lc.a_of_t(cz["ts"]), cz["a_of_t"])
+    got = lc.a_of_t(3.0e17)
+    assert isinstance(got, float) and got == float(cz["a_of_t_scalar"])
