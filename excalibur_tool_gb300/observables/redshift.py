@@ -96,3 +96,8 @@ class RedshiftCalculator:
 
 def compute_redshift_components(trajectory, a_of_eta, potential_func, velocity_func=None, verbose=False):
     return RedshiftCalculator(trajectory, a_of_eta, potential_func, velocity_func).compute_all_components(verbose)
+
+
+def compute_total_redshift(trajectory, a_of_eta, potential_func, velocity_func=None):
+    """z_total of compute_redshift_components (redshift.py:454-479)."""
+    return compute_redshift_components(trajectory, a_of_eta, potential_func, velocity_func, verbose=False)["z_total"]

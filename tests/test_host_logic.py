@@ -55,6 +55,11 @@ def test_redshift_calculator_matches_reference():
     r = RedshiftCalculator(g["traj"]).compute_all_components()
     got = np.array([r["z_H"], r["z_SW"], r["z_ISW"], r["z_D"], r["z_total"], r["z_total_exact"]])
     assert np.allclose(got, g["redshift"], rtol=1e-14, atol=0)
+    # the package-level names of the reference's observables module
+    from excalibur_tool_gb300.observables import compute_redshift_components, compute_total_redshift
+
+    assert compute_total_redshift(g["traj"], None, None) == r["z_total"]
+    assert compute_redshift_components(g["traj"], None, None)["z_total"] == r["z_total"]
 
 
 def test_observables_from_accumulators():
