@@ -891,9 +891,29 @@ def gen_time_delays():
          distances_deflected=np.asarray(dd), distances_straight=np.asarray(ds), x_proj=xp, y_proj=yp)
 
 
+# ------------------------------------------------------------ lens mass profiles
+def gen_objects():
+    """The uniform sphere and the NFW halo of objects/spherical_mass.py: density, potential,
+    enclosed mass and containment at points inside, outside and at the centre."""
+    sm = _load_file("excalibur_spherical_mass", "excalibur", "objects", "spherical_mass.py")
+    centre = np.array([0.5, 0.5, 0.5]) * one_Gpc
+    rng = np.random.default_rng(21)
+    pts = centre + rng.normal(0.0, 8.0, (64, 3)) * one_Mpc
+    pts[0] = centre
+    x, y, z = (v.reshape(8, 8) for v in pts.T)      # 2-D: broadcast point by point, no meshgrid
+    u = sm.spherical_mass(3e14 * one_Msun, 6 * one_Mpc, centre)
+    h = sm.spherical_mass_nfw(1e15 * one_Msun, 2 * one_Mpc, 5.0, centre)
+    save("objects.npz", pts=pts, u_mass=u.mass, u_radius=u.radius, u_density=u.density(x, y, z),
+         u_potential=u.potential(x, y, z), u_mass_enclosed=u.mass_enclosed(x, y, z), u_contains=u.contains(x, y, z),
+         h_mass=h.mass, h_radius=h.radius, h_concentration=h.concentration, h_rho0=h.rho0,
+         h_density=h.density(x, y, z), h_potential=h.potential(x, y, z),
+         h_mass_enclosed=h.mass_enclosed(x[1:], y[1:], z[1:]), h_contains=h.contains(x, y, z),
+         u_grid_axes=pts[:4].T, u_grid_potential=u.potential(*pts[:4].T), u_grid_mass=u.mass_enclosed(*pts[:4].T))
+
+
 GENERATORS = ["cosmology", "interp", "interp_slow", "rhs", "steps", "integrate", "integrate_modes", "generators",
               "observables", "flrw_patch_32", "schw_polar", "compare_job", "manifest", "time_delays",
-              "integrate_lf4", "rk45_slow", "schw_steppers"]
+              "integrate_lf4", "rk45_slow", "schw_steppers", "objects"]
 
 if __name__ == "__main__":
     if not os.path.isdir(REF):

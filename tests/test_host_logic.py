@@ -276,3 +276,25 @@ def test_lcdm_host_helpers_match_reference():
     assert np.array_equal(lc.a_of_t(cz["ts"]), cz["a_of_t"])
     got = lc.a_of_t(3.0e17)
     assert isinstance(got, float) and got == float(cz["a_of_t_scalar"])
+
+
+def test_mass_profiles_match_reference():
+    """The uniform sphere and the NFW halo (objects/spherical_mass.py): density, potential,
+    enclosed mass and containment at 64 points (the centre among them) and on a 4^3 grid spanned
+    by 1-D axes, bit for bit with the reference's values."""
+    from excalibur_tool_gb300.objects.spherical_mass import spherical_mass, spherical_mass_nfw
+
+    g = golden("objects.npz")
+    centre = g["pts"][0]
+    x, y, z = (v.reshape(8, 8) for v in g["pts"].T)
+    u = spherical_mass(float(g["u_mass"]), float(g["u_radius"]), centre)
+    for name, got in (("density", u.density(x, y, z)), ("potential", u.potential(x, y, z)),
+                      ("mass_enclosed", u.mass_enclosed(x, y, z)), ("contains", u.contains(x, y, z))):
+        assert np.array_equal(got, g[f"u_{name}"]), name
+    assert np.array_equal(u.potential(*g["u_grid_axes"]), g["u_grid_potential"])
+    assert np.array_equal(u.mass_enclosed(*g["u_grid_axes"]), g["u_grid_mass"])
+    h = spherical_mass_nfw(float(g["h_mass"]), float(g["h_radius"]), float(g["h_concentration"]), centre)
+    assert h.rho0 == float(g["h_rho0"]) and h.compute_rho0_nfw() == h.rho0
+    for name, got in (("density", h.density(x, y, z)), ("potential", h.potential(x, y, z)),
+                      ("mass_enclosed", h.mass_enclosed(x[1:], y[1:], z[1:])), ("contains", h.contains(x, y, z))):
+        assert np.array_equal(got, g[f"h_{name}"]), name
