@@ -75,5 +75,9 @@ class Grid:
             self._device[key] = t
         return t
 
+    def reconnect_shared(self):
+        """A worker's re-attachment of the shared-memory fields (grid.py:99-106): no field is held
+        in shared memory here, so there is nothing to re-attach."""
+
     def close_shared(self):
         pass

@@ -298,3 +298,18 @@ def test_mass_profiles_match_reference():
     for name, got in (("density", h.density(x, y, z)), ("potential", h.potential(x, y, z)),
                       ("mass_enclosed", h.mass_enclosed(x[1:], y[1:], z[1:])), ("contains", h.contains(x, y, z))):
         assert np.array_equal(got, g[f"h_{name}"]), name
+
+
+def test_grid_shared_memory_calls_are_accepted():
+    """Grid's shared-memory calls (grid.py:72-112) are accepted: the fields stay ordinary arrays
+    that the tracer uploads once."""
+    from excalibur_tool_gb300.grid.grid import Grid
+
+    g = Grid((2, 3, 4), (1.0, 1.0, 1.0))
+    data = np.arange(24.0).reshape(2, 3, 4)
+    g.add_field("Phi", data, shared=True)
+    g.reconnect_shared()
+    assert g.get_value("Phi", 1, 2, 3) == 23.0
+    g.close_shared()
+    with pytest.raises(ValueError):
+        g.add_field("Phi", np.zeros((2, 3)))
