@@ -161,6 +161,33 @@ def compute_redshift_map(trajectories, a_of_eta=None, potential_func=None, veloc
     return data, extract_sky_positions(trajectories)
 
 
+def load_trajectories(filename, clean=True):
+    """Trajectories of a save_all_histories file (n_photons attribute, photon_{i}_states
+    datasets, optional photon_info): (list of [rows, cols] arrays, metadata dict with n_photons
+    and photon_info). clean=True drops every row that holds a NaN, as the redshift-map script's
+    loader does (compute_redshift_map.py:30-51); clean=False keeps the rows as stored, for
+    compute_time_delays, which applies the time-delay script's own row filter. Needs h5py."""
+    try:
+        import h5py
+    except ImportError as e:
+        raise RuntimeError("h5py is not available; cannot read trajectory files.") from e
+    out, meta = [], {}
+    with h5py.File(filename, "r") as f:
+        n = int(f.attrs["n_photons"])
+        meta["n_photons"] = n
+        if "photon_info" in f:
+            meta["photon_info"] = f["photon_info"][:]
+        for i in range(n):
+            name = f"photon_{i}_states"
+            if name not in f:
+                continue
+            rows = np.asarray(f[name][:], dtype=float)
+            if clean and rows.ndim == 2:
+                rows = rows[~np.isnan(rows).any(axis=1)]
+            out.append(rows)
+    return out, meta
+
+
 def compute_time_delays(trajectories, metadata=None):
     """compute_time_delay_map.py:244-310 on the device, over the photons its loader keeps
     (load_trajectories, :76-92: a clean row, |x| < 1e26 m, |eta| < 3e18 s): (time_delays,

@@ -313,3 +313,38 @@ def test_grid_shared_memory_calls_are_accepted():
     g.close_shared()
     with pytest.raises(ValueError):
         g.add_field("Phi", np.zeros((2, 3)))
+
+
+def test_load_trajectories_layout(monkeypatch, tmp_path):
+    """observables.maps.load_trajectories reads the save_all_histories layout (through a stand-in
+    h5py module holding the file's datasets, since h5py is absent): the redshift script's
+    cleaning drops every row holding a NaN; clean=False keeps the stored rows."""
+    import sys
+    import types
+
+    from excalibur_tool_gb300.observables import maps
+
+    a = np.array([[1.0, 2.0, 3.0], [4.0, np.nan, 6.0], [7.0, 8.0, 9.0]])
+    b = np.array([[np.nan, 1.0, 1.0]])
+    store = {"photon_0_states": a, "photon_2_states": b, "photon_info": np.arange(3)}
+
+    class _File(dict):
+        def __init__(self, name, mode):
+            super().__init__(store)
+            self.attrs = {"n_photons": 3}
+
+        def __enter__(self):
+            return self
+
+        def __exit__(self, *exc):
+            return False
+
+    monkeypatch.setitem(sys.modules, "h5py", types.SimpleNamespace(File=_File))
+    trajs, meta = maps.load_trajectories(str(tmp_path / "x.h5"))
+    assert meta["n_photons"] == 3 and np.array_equal(meta["photon_info"], np.arange(3))
+    assert len(trajs) == 2 and np.array_equal(trajs[0], a[[0, 2]]) and trajs[1].shape == (0, 3)
+    raw, _ = maps.load_trajectories(str(tmp_path / "x.h5"), clean=False)
+    assert np.array_equal(raw[0], a, equal_nan=True) and np.array_equal(raw[1], b, equal_nan=True)
+    monkeypatch.setitem(sys.modules, "h5py", None)
+    with pytest.raises(RuntimeError):
+        maps.load_trajectories(str(tmp_path / "x.h5"))
