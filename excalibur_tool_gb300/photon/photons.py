@@ -389,8 +389,10 @@ class Photons:
             for b, ph in zip(bs, phis):
                 xyz = oxyz + float(b) * (np.cos(ph) * e1 + np.sin(ph) * e2)
                 if spherical:
-                    r = np.sqrt(xyz @ xyz)
-                    origins.append([t0, r, np.arccos(np.clip(xyz[2] / r, -1.0, 1.0)), np.arctan2(xyz[1], xyz[0])])
+                    # the reference's scalar x*x + y*y + z*z (a BLAS dot may fuse or reorder it)
+                    px, py, pz = float(xyz[0]), float(xyz[1]), float(xyz[2])
+                    r = np.sqrt(px * px + py * py + pz * pz)
+                    origins.append([t0, r, np.arccos(np.clip(pz / r, -1.0, 1.0)), np.arctan2(py, px)])
                     u_sp.append(cartesian_velocity_to_spherical(xyz[0], xyz[1], xyz[2], *u_cart))
                 else:
                     origins.append([t0, *xyz])

@@ -197,3 +197,37 @@ def test_hdf5_needs_h5py(tmp_path):
         ph.save_all_histories(str(tmp_path / "h.h5"))
     with pytest.raises(RuntimeError):
         ph.load_from_hdf5(str(tmp_path / "h.h5"))
+
+
+def _oracle_finish(spacetime):
+    """Photons._finish with the oracle's null-condition solve in place of the device's."""
+
+    def finish(self, origins, u_spatial, sign=-1.0):
+        s = np.zeros((len(u_spatial), 8))
+        s[:, :4] = origins
+        s[:, 5:8] = u_spatial
+        out, status = O.null_init(spacetime, s, sign)
+        assert (status == 0).all()
+        self._append_batch(out)
+        return out
+
+    return finish
+
+
+@pytest.mark.parametrize("name", ["flrw", "schw"])
+def test_impact_parameter_bins(monkeypatch, name):
+    """generate_impact_parameter_bins (photons.py:570-701) against the reference's states, bit for
+    bit: 3 FLRW annuli of 5 photons (seed 3) from a cartesian origin, 2 Schwarzschild annuli of 4
+    (seed 0) from a spherical one (screen points converted with the reference's scalar r)."""
+    from excalibur_tool_gb300.photon.photons import Photons
+
+    g = golden("generators.npz")
+    st, origin, _, _ = _cases(g)[name]
+    if name == "flrw":
+        axis, edges, n, seed = [1.0, 0.2, 0.1], np.linspace(0.1, 2.0, 4) * ONE_MPC, 5, 3
+    else:
+        obs = np.array([0.01, 0.01, 0.01]) * 1e3 * ONE_MPC
+        axis, edges, n, seed = g["schw_center"] - obs, np.linspace(0.5, 10, 3) * ONE_MPC, 4, 0
+    monkeypatch.setattr(Photons, "_finish", _oracle_finish(st))
+    out = Photons(None).generate_impact_parameter_bins(origin, axis, edges, n, seed=seed)
+    assert np.array_equal(out, g[f"{name}_bins"])
