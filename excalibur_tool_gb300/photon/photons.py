@@ -333,12 +333,21 @@ class Photons:
 
     def generate_cone_random(self, n_photons, origin, central_direction, cone_angle,
                              direction_basis="coordinates", *, direction_coords=None, seed=None):
-        """Random directions in a cone (photons.py:33-156); u^0 > 0 as in the reference."""
+        """Random directions in a cone (photons.py:33-156); u^0 > 0 as in the reference. Without
+        `seed` the angles come from numpy's global stream as the reference draws them (theta
+        uniform in [0, cone_angle], then phi uniform in [0, 2 pi), photon after photon), so a
+        caller's np.random.seed gives the reference's photons; `seed` selects a private
+        generator instead."""
         direction_basis = self._basis_alias(direction_basis, direction_coords)
-        rng = np.random.default_rng(seed)
         origin = np.asarray(origin, dtype=float)
-        th = rng.uniform(0, cone_angle, n_photons)
-        ph = rng.uniform(0, 2 * np.pi, n_photons)
+        if seed is None:
+            u = np.random.random_sample(2 * n_photons)
+            th = 0.0 + (cone_angle - 0.0) * u[0::2]
+            ph = 0.0 + (2 * np.pi - 0.0) * u[1::2]
+        else:
+            rng = np.random.default_rng(seed)
+            th = rng.uniform(0, cone_angle, n_photons)
+            ph = rng.uniform(0, 2 * np.pi, n_photons)
         d = np.stack([np.sin(th) * np.cos(ph), np.sin(th) * np.sin(ph), np.cos(th)], axis=1)
         d = rotate_to_direction(d, central_direction)
         d = d / np.linalg.norm(d, axis=1)[:, None]

@@ -644,6 +644,12 @@ def gen_generators(cz):
         ph5.generate_cone_grid_metric_tensor(n_photons=49, origin=origin, central_direction=[1.0, 0.5, -0.3],
                                              cone_angle=np.deg2rad(7), direction_basis="cartesian")
     flrw_cone_mt = np.array([np.concatenate([p.x, p.u]) for p in ph5.photons])
+    ph7 = Photons(m)
+    np.random.seed(17)
+    with contextlib.redirect_stdout(io.StringIO()):
+        ph7.generate_cone_random(n_photons=25, origin=origin, central_direction=[1.0, 0.5, -0.3],
+                                 cone_angle=np.deg2rad(7), direction_basis="cartesian")
+    flrw_cone_random = np.array([np.concatenate([p.x, p.u]) for p in ph7.photons])
     ph2 = Photons(m)
     ph2.generate_impact_parameter_bins(origin, [1.0, 0.2, 0.1], np.linspace(0.1, 2.0, 4) * one_Mpc, 5, seed=3)
     flrw_bins = np.array([np.concatenate([p.x, p.u]) for p in ph2.photons])
@@ -674,7 +680,7 @@ def gen_generators(cz):
     save("generators.npz", field=data, box=box, flrw_origin=origin, flrw_cone=flrw_cone, flrw_null=flrw_null,
          flrw_bins=flrw_bins, schw_origin=o_sph, schw_center=center, schw_cone=schw_cone, schw_null=schw_null,
          schw_bins=schw_bins, rot_vecs=vecs, rot_targets=targets, rot_out=rot, flrw_cone_mt=flrw_cone_mt,
-         schw_cone_mt=schw_cone_mt)
+         schw_cone_mt=schw_cone_mt, flrw_cone_random=flrw_cone_random)
 
 
 # ------------------------------------------------------------ observables

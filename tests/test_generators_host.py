@@ -231,3 +231,23 @@ def test_impact_parameter_bins(monkeypatch, name):
     monkeypatch.setattr(Photons, "_finish", _oracle_finish(st))
     out = Photons(None).generate_impact_parameter_bins(origin, axis, edges, n, seed=seed)
     assert np.array_equal(out, g[f"{name}_bins"])
+
+
+def test_cone_random_follows_numpy_global_stream(monkeypatch):
+    """generate_cone_random without a seed (photons.py:33-156) draws theta, then phi, photon after
+    photon, from numpy's global stream: after np.random.seed(17) its 25 photons are the
+    reference's (u^0 > 0), within the cone grid's ulp of direction."""
+    from excalibur_tool_gb300.photon.photons import Photons
+
+    g = golden("generators.npz")
+    st, origin, axis, deg = _cases(g)["flrw"]
+    monkeypatch.setattr(Photons, "_finish", _oracle_finish(st))
+    state = np.random.get_state()
+    try:
+        np.random.seed(17)
+        out = Photons(None).generate_cone_random(25, origin, axis, np.deg2rad(deg), direction_basis="cartesian")
+    finally:
+        np.random.set_state(state)
+    want = g["flrw_cone_random"]
+    assert (out[:, 4] > 0).all()
+    _check("flrw", out, want)
