@@ -25,3 +25,8 @@ C2_F64 = float(c ** 2)
 C4_F64 = float(c ** 4)
 
 unit_system = "si"
+
+# the reference's SI names (constants.py:7-16); with the SI system selected they are the values above
+c_si, G_si, one_Msun_si, one_pc_si = c, G, one_Msun, one_pc
+one_kpc_si, one_Mpc_si, one_Gpc_si = one_kpc, one_Mpc, one_Gpc
+one_yr_si, one_Myr_si, one_Gyr_si = one_yr, one_Myr, one_Gyr

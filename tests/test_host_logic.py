@@ -348,3 +348,21 @@ def test_load_trajectories_layout(monkeypatch, tmp_path):
     monkeypatch.setitem(sys.modules, "h5py", None)
     with pytest.raises(RuntimeError):
         maps.load_trajectories(str(tmp_path / "x.h5"))
+
+
+def test_si_constant_names_and_history_file(monkeypatch, tmp_path):
+    """The reference's *_si constant names hold the SI values; PhotonHistory.save_to_hdf5 needs
+    h5py, as the reference's does."""
+    import sys
+
+    from excalibur_tool_gb300.core import constants as K
+    from excalibur_tool_gb300.photon.photon_history import PhotonHistory
+
+    assert (K.c_si, K.G_si, K.one_Mpc_si, K.one_Gyr_si) == (299792458, 6.67430e-11, 1e6 * 3.085677581e16,
+                                                            1e9 * 365.25 * 24 * 3600)
+    assert K.one_Mpc_si == K.one_Mpc and K.one_Msun_si == K.one_Msun
+    h = PhotonHistory()
+    h.append(np.arange(8.0))
+    monkeypatch.setitem(sys.modules, "h5py", None)
+    with pytest.raises(RuntimeError):
+        h.save_to_hdf5(str(tmp_path / "h.h5"))
