@@ -917,9 +917,34 @@ def gen_objects():
          u_grid_axes=pts[:4].T, u_grid_potential=u.potential(*pts[:4].T), u_grid_mass=u.mass_enclosed(*pts[:4].T))
 
 
+# ------------------------------------------------------------ coordinate conversions
+def gen_coordinates():
+    """The six conversions of core/coordinates.py on seeded points (the poles and the axis among
+    them), velocities, and radii around a Schwarzschild radius."""
+    import excalibur.core.coordinates as co
+    rng = np.random.default_rng(31)
+    xyz = rng.normal(0.0, 1.0, (40, 3)) * one_Mpc
+    xyz[0] = [0.0, 0.0, 2.0 * one_Mpc]
+    xyz[1] = [0.0, 0.0, -3.0 * one_Mpc]
+    xyz[2] = [1.0 * one_Mpc, 0.0, 0.0]
+    v = rng.normal(0.0, 1.0, (40, 3)) * c
+    sph = np.array(co.cartesian_to_spherical(*xyz.T))
+    back = np.array(co.spherical_to_cartesian(*sph))
+    vsph = np.array([co.cartesian_velocity_to_spherical(*xyz[i], *v[i]) for i in range(3, 40)])
+    rs = 2 * G * 1e15 * one_Msun / c ** 2
+    r = np.linspace(1.01, 50.0, 25) * rs
+    iso = np.array(co.spherical_to_isotropic_radius(r, rs))
+    sch = np.array(co.isotropic_to_spherical_radius(iso, rs))
+    centre = np.array([0.5, 0.5, 0.5]) * one_Gpc
+    pts = centre + rng.normal(0.0, 10.0, (20, 3)) * one_Mpc
+    iso_xyz = np.array(co.cartesian_to_isotropic_radius(pts[:, 0], pts[:, 1], pts[:, 2], centre, rs))
+    save("coordinates.npz", xyz=xyz, v=v, sph=sph, back=back, vsph=vsph, rs=rs, r=r, iso=iso, sch=sch,
+         centre=centre, pts=pts, iso_xyz=iso_xyz)
+
+
 GENERATORS = ["cosmology", "interp", "interp_slow", "rhs", "steps", "integrate", "integrate_modes", "generators",
               "observables", "flrw_patch_32", "schw_polar", "compare_job", "manifest", "time_delays",
-              "integrate_lf4", "rk45_slow", "schw_steppers", "objects"]
+              "integrate_lf4", "rk45_slow", "schw_steppers", "objects", "coordinates"]
 
 if __name__ == "__main__":
     if not os.path.isdir(REF):

@@ -366,3 +366,23 @@ def test_si_constant_names_and_history_file(monkeypatch, tmp_path):
     monkeypatch.setitem(sys.modules, "h5py", None)
     with pytest.raises(RuntimeError):
         h.save_to_hdf5(str(tmp_path / "h.h5"))
+
+
+def test_coordinate_conversions_match_reference():
+    """core/coordinates.py's six conversions (coordinates.py:8-150) on the reference's own outputs,
+    bit for bit: cartesian <-> spherical (the poles and the x axis among the points), cartesian
+    velocities to spherical, and the isotropic radius both ways and from a cartesian point."""
+    from excalibur_tool_gb300.core import coordinates as co
+
+    g = golden("coordinates.npz")
+    xyz, v = g["xyz"], g["v"]
+    assert np.array_equal(np.array(co.cartesian_to_spherical(*xyz.T)), g["sph"])
+    assert np.array_equal(np.array(co.spherical_to_cartesian(*g["sph"])), g["back"])
+    vs = np.array([co.cartesian_velocity_to_spherical(*xyz[i], *v[i]) for i in range(3, 40)])
+    assert np.array_equal(vs, g["vsph"])
+    rs = float(g["rs"])
+    assert np.array_equal(np.array(co.spherical_to_isotropic_radius(g["r"], rs)), g["iso"])
+    assert np.array_equal(np.array(co.isotropic_to_spherical_radius(g["iso"], rs)), g["sch"])
+    p = g["pts"]
+    got = np.array(co.cartesian_to_isotropic_radius(p[:, 0], p[:, 1], p[:, 2], g["centre"], rs))
+    assert np.array_equal(got, g["iso_xyz"])
