@@ -29,6 +29,8 @@ integrator.py:204-211, so they cannot work there).
 """
 from __future__ import annotations
 
+import os
+
 import numpy as np
 
 from .. import _native as N
@@ -101,7 +103,8 @@ class Integrator:
         self.dt_min = dt_min
         self.dt_max = dt_max
         self.chunk_size = chunk_size
-        self.n_workers = n_workers
+        # the reference's default worker count (integrator.py:188); it selects nothing here
+        self.n_workers = n_workers if n_workers is not None else max(1, (os.cpu_count() or 1) - 1)
         if integrator.lower() not in self.INTEGRATORS:
             raise ValueError(f"Integrator '{integrator}' not supported. Available: {list(self.INTEGRATORS.keys())}")
         self.integrator_name = integrator.lower()

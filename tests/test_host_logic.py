@@ -100,6 +100,13 @@ def test_integrator_config_mapping():
         it.config("redshift", 1.0)
     with pytest.raises(ValueError):
         Integrator(M(), integrator="euler")
+    # the reference's name handling and defaults (integrator.py:167-196)
+    it = Integrator(M(), integrator="RK4")
+    assert type(it.integrator).__name__ == "RK4" and it.config("steps", 3).stepper == "rk4"
+    import os
+
+    assert it.n_workers == max(1, (os.cpu_count() or 1) - 1) and it.chunk_size == 50
+    assert (it.dt_min, it.dt_max, it.rtol, it.atol) == (1e14, 1e17, 1e-9, 1e-13)
 
 
 def _fake_trajectory(n_steps, record_every, failed):
